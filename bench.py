@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Throughput of the MOLOCH dynamical-core step on GB300, in grid-point-steps/s.
+
+Workload (the 512 x 512 x 60 single-domain case): the reference's idealized
+state (param + fill_atmosphere) on a 512 x 512 x 60 grid, a Gaussian hill of
+500 m and 20-gridpoint e-folding radius at the domain centre, and a seeded
+U(-0.5, +0.5) K theta perturbation on the lowest 10 levels (seed 1234).
+Synthetic seeded inputs: the reference has no dataset.
+
+A step is one moloch() call: dt = 30 s = 3 advection steps and 15 acoustic
+substeps.  value = jx*iy*kz*steps / time of the timed steps (device time,
+CUDA events on the library's stream), summed over replicas for --gpus N
+(one independent domain per GPU, "replicas only": the path has no exchange
+between domains).  The headline path is FP32 storage with the FP64
+tridiagonal solve; the plain FP64 step is timed beside it on the same state
+and the error of the FP32 path against it is reported.
+
+--impl reference times the CPU restatement of the reference (the reference
+itself is Fortran and no Fortran compiler exists on these machines) on the
+host cores, on bounded samples of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt-steps/s on 1 GB300: FP32+surrogate vs plain FP64 GPU at stated error"
+UNIT = "grid-point-steps/s"
+JX, IY, KZ = 512, 512, 60
+HILLS = ((500.0, (JX + 1) / 2.0, (IY + 1) / 2.0, 20.0),)
+SEED = 1234
+
+# Algorithmic words (one bulk-type element each) per grid point per launch:
+# the distinct global arrays each kernel must read or write.  Intermediates
+# that an ideal kernel would keep on chip (zdiv2b, the FP64 Thomas stash) are
+# not counted; their traffic shows up as measured traffic above algorithmic.
+ALG_WORDS = {
+    "k_prediag": 13,          # r: pai t q(5) | w: p qsat tvirt qwltot qwitot tetav
+    "k_sound_div": 7,         # r: u v fmz rfw rfs | w: s zdiv2
+    "k_sound_column": 21,     # r: zdiv2 u v s fmz w fmzf tetav qv qsat pai t qc qwltot qwitot | w: u v w deltaw tetav pai
+    "k_sound_momentum": 7,    # r: u v deltaw tetav pai | w: u v
+    "k_stag_to_x": 6,         # r: u v w | w: ux vx wx
+    "k_waf_vertical": 23,     # r: 10 fields s wafu wafd | w: 10 wz
+    "k_waf_meridional": 33,   # r: 10 wz 10 pp v wafn wafs | w: 10 p0
+    "k_waf_zonal": 33,        # r: 10 p0 10 pp u wafe wafw | w: 10 pp
+    "k_stag_from_x": 6,       # r: ux vx wx | w: u v w
+    "k_postdiag": 12,         # r: pai tetav q(5) | w: tvirt t p rho qsat
+}
+# whole-step algorithmic words per grid point of the fused design target
+# (pre-diag 11 + 3 sound cycles x 91 + 3 advection steps x 23 + post-diag 11)
+B_ALG_WORDS = 364
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu=0):
+        self.gpu = gpu
+        self.proc = None
+        self.out = None
+
+    def start(self):
+        try:
+            self.out = open(os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv"), "w") \
+                if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.lines = []
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+            if self.out:
+                self.out.write(line)
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        if self.out:
+            self.out.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        backend = "nccl" if os.environ.get("MOLOCH_BENCH_BACKEND", "nccl") == "nccl" else "gloo"
+        dist.init_process_group(backend)
+        return dist, rank, ws
+    return None, 0, 1
+
+
+def reduce_max(dist, x, device=None):
+    """Maximum of a float over ranks (identity without a process group)."""
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def reduce_sum(dist, x, device=None):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(dist, device=None):
+    if dist is not None:
+        if device is not None:
+            dist.barrier(device_ids=[device.index])
+        else:
+            dist.barrier()
+
+
+def rmse(a, b):
+    return float(np.sqrt(np.mean((np.asarray(a) - np.asarray(b)) ** 2)))
+
+
+def cpu_sample(steps, jx=256, iy=256, kz=KZ, threads=None):
+    """Oracle throughput on the host cores: a bounded sample of the workload."""
+    from oracle import oracle
+    threads = threads or os.cpu_count() or 1
+    L = oracle.lib()
+    L.oracle_set_threads(threads)
+    hills = ((500.0, (jx + 1) / 2.0, (iy + 1) / 2.0, 20.0 * jx / JX),)
+    o = oracle.Oracle(oracle.make_cfg(jx, iy, kz, hills=hills, seed=SEED))
+    t0 = time.perf_counter()
+    for s in range(steps):
+        o.step(s + 1)
+    dt = time.perf_counter() - t0
+    o.close()
+    return jx * iy * kz * steps / dt, dt, threads
+
+
+def run_reference(args, dist, rank, ws):
+    if rank != 0:
+        return 0
+    per_step = []
+    for _ in range(args.warmup):
+        cpu_sample(1)
+    for _ in range(args.steps):
+        v, dt, threads = cpu_sample(1)
+        per_step.append(dt)
+    total = sum(per_step)
+    gp = 256 * 256 * KZ
+    value = gp * args.steps / total
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+        "config": {"workload": f"{JX}x{IY}x{KZ} idealized state, 500 m hill, seeded theta noise",
+                   "sample": "each step: one moloch() step on a 256x256x60 sample of the workload"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "256x256x60, 1 step per timed step; C restatement of nompi/mod_moloch.F90 "
+                                   "(reference build unavailable: no Fortran compiler on the host)"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def make_domain(dm, mode, stream):
+    d = dm.Moloch(JX, IY, KZ, mode=mode, stream=stream)
+    d.setup_idealized(hills=HILLS, pert_amp=0.5, pert_levels=10, seed=SEED)
+    return d
+
+
+def time_steps(torch, d, stream, steps, graph=True):
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    d.sync()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    k0 = d.kernel_count
+    d.run(steps, graph=graph)
+    e1.record(stream)
+    e1.synchronize()
+    d.sync()
+    return e0.elapsed_time(e1), d.kernel_count - k0
+
+
+def e2e_steps(torch, dm, d, stream, steps):
+    """Through the reference-facing C ABI with host arrays: upload the
+    prognostic state, one moloch() call, download the output fields t, ps
+    (the fields the reference driver writes, regcm_dynamical_core.F90:203-216)."""
+    names_in = ("u", "v", "w", "pai", "t", "qx")
+    host = {n: d.download(n) for n in names_in}
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    d.sync()
+    e0.record(stream)
+    t0 = time.perf_counter()
+    out = None
+    for s in range(steps):
+        for n in names_in:
+            d.upload(n, host[n])
+        d.moloch(s + 1)
+        out = (d.download("t"), d.download("ps"))
+        host["t"] = out[0]
+    e1.record(stream)
+    e1.synchronize()
+    wall = time.perf_counter() - t0
+    h2d = sum(host[n].nbytes for n in names_in)
+    d2h = out[0].nbytes + out[1].nbytes
+    return max(e0.elapsed_time(e1), 1e3 * wall), h2d, d2h
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--size", default=None, help="JXxIYxKZ override (profiling a smaller case)")
+    ap.add_argument("--only", default=None, choices=["mixed", "fp64"], help="time one path only (profiling)")
+    args = ap.parse_args()
+    global JX, IY, KZ, HILLS
+    if args.size:
+        JX, IY, KZ = (int(x) for x in args.size.lower().split("x"))
+        HILLS = ((500.0, (JX + 1) / 2.0, (IY + 1) / 2.0, 20.0 * JX / 512.0),)
+    if args.warmup < 3:
+        args.warmup = 3
+    dist, rank, ws = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, dist, rank, ws)
+
+    import torch
+    import dynamical_model_gb300 as dm
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=device)
+    sptr = stream.cuda_stream
+
+    # ---- headline path: FP32 storage + FP64 solve --------------------------
+    if args.only:
+        d = make_domain(dm, "fp32_mixed" if args.only == "mixed" else "fp64", sptr)
+        d.run(args.warmup, graph=True)
+        ms, launches = time_steps(torch, d, stream, args.steps)
+        if rank == 0:
+            print(json.dumps({"only": args.only, "size": [JX, IY, KZ], "ms_per_step": ms / args.steps,
+                              "value": JX * IY * KZ * args.steps / (ms / 1e3), "gpu_launches": launches}))
+        d.close()
+        return 0
+    dmix = make_domain(dm, "fp32_mixed", sptr)
+    d64 = make_domain(dm, "fp64", sptr)
+    dmix.run(args.warmup, graph=True)
+    d64.run(args.warmup, graph=True)
+    dmix.sync(); d64.sync()
+
+    clk = ClockSampler(local)
+    barrier(dist, device)
+    clk.start()
+    ms_mix, launches_mix = time_steps(torch, dmix, stream, args.steps)
+    barrier(dist, device)
+    clocks = clk.stop()
+    ms_mix = reduce_max(dist, ms_mix, device)
+    # plain FP64 on the same state and the same number of steps
+    ms_64, launches_64 = time_steps(torch, d64, stream, args.steps)
+    ms_64 = reduce_max(dist, ms_64, device)
+
+    gp = JX * IY * KZ
+    n_dom = reduce_sum(dist, 1.0, device)
+    value = n_dom * gp * args.steps / (ms_mix / 1e3)
+    value64 = n_dom * gp * args.steps / (ms_64 / 1e3)
+
+    # error of the FP32 path against the FP64 GPU step after warmup+steps steps
+    th_mix = dmix.get("tetav")
+    err = {"steps": args.warmup + args.steps,
+           "theta_rmse_K": rmse(dmix.get("t") / dmix.get("pai"), d64.get("t") / d64.get("pai")),
+           "u_rmse_ms": rmse(dmix.get("u"), d64.get("u")),
+           "v_rmse_ms": rmse(dmix.get("v"), d64.get("v")),
+           "w_rmse_ms": rmse(dmix.get("w"), d64.get("w")),
+           "ps_rmse_Pa": rmse(dmix.get("ps"), d64.get("ps"))}
+    del th_mix
+
+    # ---- per-kernel CUDA-event profile of one step (roofline) ---------------
+    prof = dmix.profile_step()
+    prof64 = d64.profile_step()
+    peak, peak_kind = peaks()
+    top = max(prof.items(), key=lambda kv: kv[1][0])
+    tname, (tms, tcount) = top
+    words = ALG_WORDS.get(tname, 0)
+    esz = 4
+    alg_bytes = words * esz * gp  # per launch
+    avg_ms = tms / max(tcount, 1)
+    achieved = alg_bytes / (avg_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak,
+                "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
+                "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
+                "traffic": None,
+                "step_alg_GBps": B_ALG_WORDS * esz * value / n_dom / 1e9}
+    kernels = {k: {"ms": round(v[0], 4), "launches": v[1],
+                   "GBps_alg": (ALG_WORDS.get(k, 0) * esz * gp * v[1] / (v[0] / 1e3) / 1e9) if v[0] > 0 else None}
+               for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    kernels64 = {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in sorted(prof64.items(), key=lambda kv: -kv[1][0])}
+
+    # ---- end to end through the C ABI with host arrays ----------------------
+    e2e = None
+    if not args.no_e2e:
+        ms_e2e, h2d, d2h = e2e_steps(torch, dm, dmix, stream, max(2, min(args.steps, 5)))
+        n_e2e = max(2, min(args.steps, 5))
+        ms_e2e = reduce_max(dist, ms_e2e, device)
+        e2e = {"value": n_dom * gp * n_e2e / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "steps": n_e2e,
+               "path": "moloch_gpu_upload(u,v,w,pai,t,qx) + moloch_gpu_step + moloch_gpu_download(t,ps), FP64 host arrays"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        v, dt, threads = cpu_sample(2)
+        cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"2 steps of a 256x256x60 sample of the workload, {dt:.1f} s, OpenMP C restatement "
+                         f"of nompi/mod_moloch.F90 (no Fortran compiler: reference build unavailable)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_mix / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 tridiagonal solve)",
+            "data": "synthetic",
+            "config": {"workload": f"{JX}x{IY}x{KZ} idealized state, 500 m hill r=20 gp, seeded +-0.5 K theta noise",
+                       "jx": JX, "iy": IY, "kz": KZ, "path": "fp32_mixed (surrogate not in this path)",
+                       "graph": True, "parallelism": f"replicas x{ws}",
+                       "l2": "inputs larger than L2 (state > 1 GB per domain)"},
+            "fp64_plain": {"value": value64, "ms_per_step": ms_64 / args.steps, "dtype": "f64",
+                           "gpu_launches": launches_64},
+            "speedup_vs_fp64": value / value64,
+            "error_vs_fp64": err,
+            "roofline": roofline,
+            "kernels": kernels,
+            "kernels_fp64": kernels64,
+            "cpu_baseline": cpu,
+            "e2e": e2e,
+            "gpu_launches": launches_mix,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    dmix.close()
+    d64.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,266 @@
+"""GB300-native MOLOCH dynamical-core step.
+
+Python mirror of the reference module `mod_moloch` (nompi/mod_moloch.F90):
+``Moloch`` holds one domain on the GPU and offers the reference's three
+entry points -- ``allocate_moloch`` (constructor), ``init_moloch`` (upload +
+init) and ``moloch(istep, lprint)`` -- over the C ABI in
+include/moloch_gb300.h.  There is no CPU fallback: the native library must
+load, and every step runs the CUDA kernels in csrc/.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .build import LIB as _LIB_PATH, build as _build
+
+__all__ = ["Moloch", "MolochError", "Params", "Grid", "Diag", "Ideal", "lib", "FIELD",
+           "FP64", "FP64_EXACT", "FP32_MIXED", "field_bounds"]
+
+FP64, FP64_EXACT, FP32_MIXED = 0, 1, 2
+_MODES = {"fp64": FP64, "fp64_exact": FP64_EXACT, "fp32_mixed": FP32_MIXED, "mixed": FP32_MIXED}
+
+# field ids, same order as enum moloch_field
+_FIELD_NAMES = ["u", "v", "w", "pai", "t", "tetav", "qv", "qc", "qi", "qr", "qs", "qx",
+                "p", "tvirt", "qsat", "rho", "ps", "zeta", "fmz", "fmzf", "ht",
+                "msfx", "msfu", "msfv", "hx", "hy", "ulat", "vlat", "zita", "zitah", "s", "deltaw"]
+FIELD = {n: i for i, n in enumerate(_FIELD_NAMES)}
+
+ERRORS = {0: "ok", 1: "bad argument", 2: "bounds mismatch", 3: "CUDA error", 4: "CFL violation",
+          5: "call out of order", 6: "device wait timed out", 7: "out of device memory"}
+
+
+class MolochError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Grid(ctypes.Structure):
+    _fields_ = [("jx", ctypes.c_int), ("iy", ctypes.c_int), ("kz", ctypes.c_int)]
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("dt", ctypes.c_double), ("dx", ctypes.c_double), ("mo_ztop", ctypes.c_double),
+                ("mo_h", ctypes.c_double), ("mo_a0", ctypes.c_double), ("mo_anu2", ctypes.c_double),
+                ("mo_nadv", ctypes.c_int), ("mo_nsound", ctypes.c_int), ("mode", ctypes.c_int),
+                ("mo_divfilter", ctypes.c_int), ("do_filterpai", ctypes.c_int),
+                ("do_filtertheta", ctypes.c_int), ("rotllr", ctypes.c_int)]
+
+
+class Diag(ctypes.Structure):
+    _fields_ = [("maxps", ctypes.c_double), ("minps", ctypes.c_double), ("maxu", ctypes.c_double),
+                ("minu", ctypes.c_double), ("maxv", ctypes.c_double), ("minv", ctypes.c_double),
+                ("mass", ctypes.c_double), ("energy", ctypes.c_double),
+                ("status", ctypes.c_int), ("nonfinite", ctypes.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class Ideal(ctypes.Structure):
+    _fields_ = [("nhills", ctypes.c_int), ("hill_h", ctypes.c_double * 4), ("hill_j", ctypes.c_double * 4),
+                ("hill_i", ctypes.c_double * 4), ("hill_r", ctypes.c_double * 4),
+                ("pert_amp", ctypes.c_double), ("pert_levels", ctypes.c_int),
+                ("seed", ctypes.c_ulonglong), ("u0", ctypes.c_double), ("v0", ctypes.c_double)]
+
+
+# exported symbols and their prototypes (must cover every function of the header)
+_PROTOS = {
+    "moloch_gpu_create": (ctypes.c_int, [ctypes.POINTER(Grid), ctypes.POINTER(Params), ctypes.c_void_p,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "moloch_gpu_default_params": (None, [ctypes.POINTER(Params)]),
+    "moloch_gpu_upload": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                         ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "moloch_gpu_init": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(Diag)]),
+    "moloch_gpu_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "moloch_gpu_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
+    "moloch_gpu_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "moloch_gpu_kernel_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "moloch_gpu_phase": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "moloch_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_last_error": (ctypes.c_char_p, []),
+    "moloch_gpu_setup_idealized": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Ideal)]),
+    "moloch_gpu_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                               ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+    "moloch_gpu_kernel_kinds": (ctypes.c_int, []),
+    "moloch_gpu_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+}
+
+_lib = None
+
+
+def lib(build_if_missing=True):
+    """Load libmoloch_gb300.so (building it first when it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build()
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError(f"native library {_LIB_PATH} is missing; run dynamical_model_gb300.build.build()")
+    L = ctypes.CDLL(_LIB_PATH)
+    for name, (res, args) in _PROTOS.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != 0:
+        raise MolochError(rc, lib().moloch_gpu_last_error().decode())
+
+
+def field_bounds(name, jx, iy, kz):
+    """Fortran (lower, upper) bounds of a reference array (nompi/mod_atmosphere.F90:104-169)."""
+    nj, ni = jx, iy
+    b = {
+        "u": ((-1, nj + 2), (0, ni + 1), (1, kz)),
+        "v": ((0, nj + 1), (-1, ni + 2), (1, kz)),
+        "w": ((1, nj), (1, ni), (1, kz + 1)),
+        "zeta": ((-1, nj + 2), (-1, ni + 2), (1, kz)),
+        "fmzf": ((1, nj), (1, ni), (1, kz + 1)),
+        "s": ((1, nj), (1, ni), (1, kz + 1)),
+        "deltaw": ((0, nj + 1), (0, ni + 1), (1, kz + 1)),
+        "ps": ((0, nj + 1), (0, ni + 1)),
+        "ht": ((-1, nj + 2), (-1, ni + 2)),
+        "msfx": ((1, nj), (1, ni)), "ulat": ((1, nj), (1, ni)), "vlat": ((1, nj), (1, ni)),
+        "msfu": ((0, nj + 1), (1, ni)), "hx": ((0, nj + 1), (1, ni)),
+        "msfv": ((1, nj), (0, ni + 1)), "hy": ((1, nj), (0, ni + 1)),
+        "zita": ((1, kz + 1),), "zitah": ((1, kz),),
+        "qx": ((0, nj + 1), (0, ni + 1), (1, kz), (1, 5)),
+    }
+    if name in b:
+        return b[name]
+    if name in ("pai", "t", "tetav", "fmz", "qv", "qc", "qi", "qr", "qs"):
+        return ((0, nj + 1), (0, ni + 1), (1, kz))
+    if name in ("p", "tvirt", "qsat", "rho"):
+        return ((1, nj), (1, ni), (1, kz))
+    raise KeyError(name)
+
+
+class Moloch:
+    """One MOLOCH domain resident on the GPU.
+
+    ``Moloch(jx, iy, kz, mode=...)`` is allocate_moloch; ``setup_idealized``
+    runs the reference driver's param()+init() and init_moloch;
+    ``moloch(istep, lprint)`` is one dt step.  ``get(name)`` returns the
+    interior of a field as a (nk, iy, jx) float64 array (C order: the last
+    axis is the reference's contiguous j index).
+    """
+
+    def __init__(self, jx, iy, kz, mode="fp64", stream=None, **opts):
+        self.L = lib()
+        self.jx, self.iy, self.kz = jx, iy, kz
+        self.grid = Grid(jx, iy, kz)
+        self.params = Params()
+        self.L.moloch_gpu_default_params(ctypes.byref(self.params))
+        self.params.mode = _MODES[mode] if isinstance(mode, str) else int(mode)
+        for k, v in opts.items():
+            if not hasattr(self.params, k):
+                raise TypeError(f"unknown option {k}")
+            setattr(self.params, k, v)
+        h = ctypes.c_void_p()
+        _check(self.L.moloch_gpu_create(ctypes.byref(self.grid), ctypes.byref(self.params),
+                                        ctypes.c_void_p(stream) if stream else None, ctypes.byref(h)))
+        self.h = h
+
+    # -- init_moloch ----------------------------------------------------------
+    def setup_idealized(self, hills=(), pert_amp=0.5, pert_levels=10, seed=1234, u0=1.0, v0=1.0):
+        z = Ideal()
+        z.nhills = len(hills)
+        for n, (hh, cj, ci, r) in enumerate(hills):
+            z.hill_h[n], z.hill_j[n], z.hill_i[n], z.hill_r[n] = hh, cj, ci, r
+        z.pert_amp, z.pert_levels, z.seed, z.u0, z.v0 = pert_amp, pert_levels, seed, u0, v0
+        _check(self.L.moloch_gpu_setup_idealized(self.h, ctypes.byref(z)))
+
+    def upload(self, name, arr):
+        """Upload a reference-layout array (Fortran order, with its halo)."""
+        bnds = field_bounds(name, self.jx, self.iy, self.kz)
+        a = np.asfortranarray(arr, dtype=np.float64)
+        shape = tuple(u - l + 1 for l, u in bnds)
+        if a.shape != shape:
+            raise ValueError(f"{name}: shape {a.shape}, expected {shape}")
+        lb = (ctypes.c_int * 4)(*[l for l, _ in bnds])
+        ub = (ctypes.c_int * 4)(*[u for _, u in bnds])
+        _check(self.L.moloch_gpu_upload(self.h, FIELD[name], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                        lb, ub))
+
+    def init(self):
+        _check(self.L.moloch_gpu_init(self.h))
+
+    # -- moloch ---------------------------------------------------------------
+    def moloch(self, istep=1, lprint=False):
+        d = Diag()
+        _check(self.L.moloch_gpu_step(self.h, istep, int(lprint), ctypes.byref(d)))
+        return d if lprint else None
+
+    step = moloch
+
+    def run(self, nsteps, graph=True):
+        _check(self.L.moloch_gpu_run(self.h, nsteps, int(graph)))
+
+    def phase(self, p):
+        _check(self.L.moloch_gpu_phase(self.h, p))
+
+    def sync(self):
+        _check(self.L.moloch_gpu_sync(self.h))
+
+    def profile_step(self):
+        """One step with CUDA events around every kernel: {kernel: (ms, launches)}."""
+        n = self.L.moloch_gpu_kernel_kinds()
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int * n)()
+        _check(self.L.moloch_gpu_profile_step(self.h, ms, cnt, n))
+        return {self.L.moloch_gpu_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n) if cnt[k]}
+
+    @property
+    def stream(self):
+        return self.L.moloch_gpu_stream(self.h)
+
+    @property
+    def kernel_count(self):
+        return self.L.moloch_gpu_kernel_count(self.h)
+
+    def download(self, name):
+        """The reference-layout array (Fortran order, halo rings included)."""
+        bnds = field_bounds(name, self.jx, self.iy, self.kz)
+        shape = tuple(u - l + 1 for l, u in bnds)
+        a = np.zeros(shape, dtype=np.float64, order="F")
+        lb = (ctypes.c_int * 4)(*[l for l, _ in bnds])
+        ub = (ctypes.c_int * 4)(*[u for _, u in bnds])
+        _check(self.L.moloch_gpu_download(self.h, FIELD[name], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                          lb, ub))
+        return a
+
+    def get(self, name):
+        """Interior of a field as (nk, iy, jx) float64 (or (iy, jx) for 2-D)."""
+        a = self.download(name)
+        bnds = field_bounds(name, self.jx, self.iy, self.kz)
+        sl = tuple(slice(1 - l, 1 - l + n) for (l, _), n in zip(bnds[:2], (self.jx, self.iy)))
+        if len(bnds) == 2:
+            return np.ascontiguousarray(a[sl].T)
+        k0 = 1 - bnds[2][0]
+        return np.ascontiguousarray(a[sl + (slice(k0, None),)].transpose(2, 1, 0))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.moloch_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

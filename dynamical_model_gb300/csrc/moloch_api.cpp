@@ -1,0 +1,813 @@
+// C-ABI implementation of the GB300 MOLOCH step (include/moloch_gb300.h).
+//
+// Compiled by the host C++ compiler with -ffp-contract=off: the static
+// metric terms computed here (init_moloch's derived arrays and the
+// reciprocals the kernels reuse) must round exactly like the reference's
+// FP64 expressions, which never fuse a multiply with an add.
+//
+// Host-side flow, mirroring the reference program:
+//   allocate_moloch  -> moloch_gpu_create     (device arena for one domain)
+//   init_moloch      -> moloch_gpu_upload * n, moloch_gpu_init
+//   moloch(i,lprint) -> moloch_gpu_step        (or moloch_gpu_run for a loop)
+// Device layout and kernel map: moloch_view.h, moloch_kernels.cuh.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/moloch_gb300.h"
+#include "moloch_constants.h"
+#include "moloch_launch.h"
+#include "moloch_view.h"
+
+using namespace moloch;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CUDA_TRY(x)                                                                          \
+  do {                                                                                       \
+    cudaError_t e_ = (x);                                                                    \
+    if (e_ != cudaSuccess) return fail(MOLOCH_ERR_CUDA, "%s: %s (%s:%d)", #x,               \
+                                       cudaGetErrorString(e_), __FILE__, __LINE__);          \
+  } while (0)
+
+// expected Fortran bounds of each field (see the table in moloch_gb300.h)
+struct FieldShape {
+  int ndim;
+  int lb[4], ub[4];
+};
+
+FieldShape shape_of(int f, int nj, int ni, int kz) {
+  FieldShape s{};
+  auto set3 = [&](int l1, int u1, int l2, int u2, int l3, int u3) {
+    s.ndim = 3;
+    s.lb[0] = l1; s.ub[0] = u1; s.lb[1] = l2; s.ub[1] = u2; s.lb[2] = l3; s.ub[2] = u3;
+  };
+  auto set2 = [&](int l1, int u1, int l2, int u2) {
+    s.ndim = 2;
+    s.lb[0] = l1; s.ub[0] = u1; s.lb[1] = l2; s.ub[1] = u2;
+  };
+  switch (f) {
+    case MOLOCH_F_U: set3(-1, nj + 2, 0, ni + 1, 1, kz); break;
+    case MOLOCH_F_V: set3(0, nj + 1, -1, ni + 2, 1, kz); break;
+    case MOLOCH_F_W: set3(1, nj, 1, ni, 1, kz + 1); break;
+    case MOLOCH_F_PAI: case MOLOCH_F_T: case MOLOCH_F_TETAV: case MOLOCH_F_FMZ:
+    case MOLOCH_F_QV: case MOLOCH_F_QC: case MOLOCH_F_QI: case MOLOCH_F_QR: case MOLOCH_F_QS:
+      set3(0, nj + 1, 0, ni + 1, 1, kz); break;
+    case MOLOCH_F_QX:
+      set3(0, nj + 1, 0, ni + 1, 1, kz);
+      s.ndim = 4; s.lb[3] = 1; s.ub[3] = 5; break;
+    case MOLOCH_F_P: case MOLOCH_F_TVIRT: case MOLOCH_F_QSAT: case MOLOCH_F_RHO:
+      set3(1, nj, 1, ni, 1, kz); break;
+    case MOLOCH_F_PS: set2(0, nj + 1, 0, ni + 1); break;
+    case MOLOCH_F_ZETA: set3(-1, nj + 2, -1, ni + 2, 1, kz); break;
+    case MOLOCH_F_FMZF: set3(1, nj, 1, ni, 1, kz + 1); break;
+    case MOLOCH_F_HT: set2(-1, nj + 2, -1, ni + 2); break;
+    case MOLOCH_F_MSFX: case MOLOCH_F_ULAT: case MOLOCH_F_VLAT: set2(1, nj, 1, ni); break;
+    case MOLOCH_F_MSFU: case MOLOCH_F_HX: set2(0, nj + 1, 1, ni); break;
+    case MOLOCH_F_MSFV: case MOLOCH_F_HY: set2(1, nj, 0, ni + 1); break;
+    case MOLOCH_F_ZITA: s.ndim = 1; s.lb[0] = 1; s.ub[0] = kz + 1; break;
+    case MOLOCH_F_ZITAH: s.ndim = 1; s.lb[0] = 1; s.ub[0] = kz; break;
+    case MOLOCH_F_S: set3(1, nj, 1, ni, 1, kz + 1); break;
+    case MOLOCH_F_DELTAW: set3(0, nj + 1, 0, ni + 1, 1, kz + 1); break;
+    default: s.ndim = 0;
+  }
+  return s;
+}
+
+inline int wrap(int x, int n) {
+  int y = (x - 1) % n;
+  if (y < 0) y += n;
+  return y;  // 0-based interior index of 1-based x with period n
+}
+
+// interior (1..nj, 1..ni, 1..nk) of a bounded host array -> dense j-fastest
+void gather_interior(const double* base, const FieldShape& s, int nj, int ni, int nk, int level4,
+                     std::vector<double>& out) {
+  long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1;
+  long n3 = s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1;
+  out.resize((size_t)nj * ni * nk);
+  long off4 = (long)level4 * n1 * n2 * n3;
+  for (int k = 1; k <= nk; ++k)
+    for (int i = 1; i <= ni; ++i) {  // rows are contiguous in j
+      long q = off4 + (long)(s.ndim >= 3 ? k - s.lb[2] : 0) * n1 * n2 +
+               (long)(s.ndim >= 2 ? i - s.lb[1] : 0) * n1 + (1 - s.lb[0]);
+      std::memcpy(&out[(size_t)nj * ((i - 1) + (size_t)ni * (k - 1))], base + q, sizeof(double) * nj);
+    }
+}
+
+// dense interior -> bounded host array; halo positions get periodic images
+void scatter_periodic(const std::vector<double>& in, const FieldShape& s, int nj, int ni, int nk,
+                      int level4, double* base) {
+  long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1;
+  long n3 = s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1;
+  long off4 = (long)level4 * n1 * n2 * n3;
+  int k1 = s.ndim >= 3 ? s.lb[2] : 1, k2 = s.ndim >= 3 ? s.ub[2] : 1;
+  int i1 = s.ndim >= 2 ? s.lb[1] : 1, i2 = s.ndim >= 2 ? s.ub[1] : 1;
+  for (int k = k1; k <= k2; ++k)
+    for (int i = i1; i <= i2; ++i)
+      for (int j = s.lb[0]; j <= s.ub[0]; ++j) {
+        long q = off4 + (long)(k - k1) * n1 * n2 + (long)(i - i1) * n1 + (j - s.lb[0]);
+        int kk = (k >= 1 && k <= nk) ? k - 1 : (k < 1 ? 0 : nk - 1);
+        base[q] = in[(size_t)wrap(j, nj) + (size_t)nj * (wrap(i, ni) + (size_t)ni * kk)];
+      }
+}
+
+double gzita(double zita, double ztop, double a0) {  // nompi/mod_zita.F90:109-120
+  double ratio = zita / ztop;
+  double r2 = ratio * ratio, r3 = r2 * ratio;
+  return (((0.0 - 1.0 * a0) * ratio - (3.0 - 2.0 * a0) * r2) + (2.0 - 1.0 * a0) * r3) + 1.0;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+struct moloch_handle {
+  moloch_grid_t grid{};
+  moloch_params_t prm{};
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int elem = 8;  // bytes per element of the bulk type
+  void* arena = nullptr;
+  size_t arena_bytes = 0;
+  View<double> vd{};
+  View<float> vf{};
+  bool initialized = false;
+  long long kernels = 0;
+  int kernels_per_step = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  double* hres = nullptr;  // pinned diag result
+  void* stage = nullptr;   // pinned staging buffer, one 3-D field (kz+1 levels) of doubles
+  size_t stage_bytes = 0;
+  // host copies of the static inputs (dense interiors)
+  std::vector<double> zeta, fmz, fmzf, msfx, msfu, msfv, hx, hy, ulat, vlat, zita, zitah;
+  unsigned uploaded = 0;  // bit per field id
+  int nj() const { return grid.jx; }
+  int ni() const { return grid.iy; }
+  int kz() const { return grid.kz; }
+};
+
+namespace {
+
+PhaseFlags flags_of(const moloch_handle* h) {
+  PhaseFlags f;
+  f.divfilter = h->prm.mo_divfilter;
+  f.filterpai = h->prm.do_filterpai;
+  f.filtertheta = h->prm.do_filtertheta;
+  f.nsound = h->prm.mo_nsound;
+  f.nadv = h->prm.mo_nadv;
+  return f;
+}
+
+// carve the arena; returns bytes needed when base == nullptr
+template <class T>
+size_t layout(View<T>& v, char* base, const moloch_handle* h) {
+  size_t off = 0;
+  const size_t pl = (size_t)h->nj() * h->ni(), kz = h->kz();
+  const size_t n3 = pl * kz, n3p = pl * (kz + 1), ne = (size_t)std::max(h->nj(), h->ni()) * kz;
+  auto take = [&](size_t bytes) -> void* {
+    off = (off + 255) & ~size_t(255);
+    void* p = base ? base + off : nullptr;
+    off += bytes;
+    return p;
+  };
+  auto T3 = [&]() { return (T*)take(sizeof(T) * n3); };
+  auto T3p = [&]() { return (T*)take(sizeof(T) * n3p); };
+  auto T2 = [&]() { return (T*)take(sizeof(T) * pl); };
+  auto T1 = [&](size_t n) { return (T*)take(sizeof(T) * n); };
+  v.ubuf[0] = T3(); v.ubuf[1] = T3(); v.vbuf[0] = T3(); v.vbuf[1] = T3();
+  v.w = T3p(); v.pai = T3(); v.tetav = T3(); v.t = T3();
+  for (int n = 0; n < 5; ++n) v.q[n] = T3();
+  v.p = T3(); v.qsat = T3(); v.tvirt = T3(); v.rho = T3(); v.ps = T2();
+  v.qwltot = T3(); v.qwitot = T3();
+  v.s = T3p(); v.deltaw = T3p(); v.zdiv2a = T3(); v.zdiv2b = T3();
+  v.wp = (double*)take(sizeof(double) * n3p);
+  v.wwkw = (double*)take(sizeof(double) * n3p);
+  v.ux = T3(); v.vx = T3(); v.wx = T3();
+  v.wz = (T*)take(sizeof(T) * n3 * kNumAdvected);
+  v.p0 = (T*)take(sizeof(T) * n3 * kNumAdvected);
+  const bool filt = h->prm.do_filterpai || h->prm.do_filtertheta;
+  v.pf = h->prm.do_filterpai ? T3() : nullptr;
+  v.tf = h->prm.do_filtertheta ? T3() : nullptr;
+  v.fscr = filt ? T3() : nullptr;
+  v.eu_j = T1(ne); v.eu_i = T1(ne); v.ev_j = T1(ne); v.ev_i = T1(ne); v.ep_j = T1(ne); v.ep_i = T1(ne);
+  v.fmz = T3(); v.fmzf = T3p(); v.zeta = T3(); v.dz = T3();
+  v.rfw = T3(); v.rfs = T3();
+  v.wafu = T3(); v.wafd = T3(); v.wafn = T3(); v.wafs = T3(); v.wafe = T3(); v.wafw = T3();
+  v.hx = T2(); v.hy = T2(); v.mx = T2(); v.mu = T2(); v.mv = T2(); v.rmu = T2(); v.rmv = T2();
+  v.mx2 = T2(); v.coru = T2(); v.corv = T2();
+  v.gzitak = T1(kz + 1); v.gzitakh = T1(kz); v.xknu = T1(kz); v.cdamp = T1(kz); v.ffilt = T1(kz);
+  const int parts = kfast::diag_parts(h->nj(), h->ni());
+  v.dpart = (double*)take(sizeof(double) * 9 * parts);
+  v.dres = (double*)take(sizeof(double) * 16);
+  v.dparts = parts;
+  v.nj = h->nj(); v.ni = h->ni(); v.kz = h->kz(); v.pl = (int)pl; v.rotllr = h->prm.rotllr;
+  v.cur = 0;
+  return off + 256;
+}
+
+// host <-> device through the handle's pinned staging buffer (one 3-D
+// field); the bulk type conversion happens while filling the buffer
+template <class T>
+int upload_dense(moloch_handle* h, T* dst, const std::vector<double>& src) {
+  const size_t bytes = sizeof(T) * src.size();
+  if (bytes > h->stage_bytes) return fail(MOLOCH_ERR_ARG, "upload of %zu bytes exceeds staging", bytes);
+  CUDA_TRY(cudaStreamSynchronize(h->stream));  // staging buffer free again
+  T* st = (T*)h->stage;
+  if (sizeof(T) == sizeof(double))
+    std::memcpy(st, src.data(), bytes);
+  else
+    for (size_t q = 0; q < src.size(); ++q) st[q] = (T)src[q];
+  CUDA_TRY(cudaMemcpyAsync(dst, st, bytes, cudaMemcpyHostToDevice, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return MOLOCH_OK;
+}
+
+template <class T>
+int download_dense(moloch_handle* h, const T* src, size_t n, std::vector<double>& out) {
+  const size_t bytes = sizeof(T) * n;
+  if (bytes > h->stage_bytes) return fail(MOLOCH_ERR_ARG, "download of %zu bytes exceeds staging", bytes);
+  out.resize(n);
+  CUDA_TRY(cudaMemcpyAsync(h->stage, src, bytes, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  const T* st = (const T*)h->stage;
+  if (sizeof(T) == sizeof(double))
+    std::memcpy(out.data(), st, bytes);
+  else
+    for (size_t q = 0; q < n; ++q) out[q] = (double)st[q];
+  return MOLOCH_OK;
+}
+
+// device pointer of a prognostic/diagnostic field in the bulk type
+template <class T>
+T* field_ptr(View<T>& v, int f) {
+  switch (f) {
+    case MOLOCH_F_U: return v.ubuf[v.cur];  // current buffer of the ping-pong pair
+    case MOLOCH_F_V: return v.vbuf[v.cur];
+    case MOLOCH_F_W: return v.w;
+    case MOLOCH_F_PAI: return v.pai;
+    case MOLOCH_F_T: return v.t;
+    case MOLOCH_F_TETAV: return v.tetav;
+    case MOLOCH_F_QV: return v.q[0];
+    case MOLOCH_F_QC: return v.q[1];
+    case MOLOCH_F_QI: return v.q[2];
+    case MOLOCH_F_QR: return v.q[3];
+    case MOLOCH_F_QS: return v.q[4];
+    case MOLOCH_F_P: return v.p;
+    case MOLOCH_F_TVIRT: return v.tvirt;
+    case MOLOCH_F_QSAT: return v.qsat;
+    case MOLOCH_F_RHO: return v.rho;
+    case MOLOCH_F_PS: return v.ps;
+    case MOLOCH_F_S: return v.s;
+    case MOLOCH_F_DELTAW: return v.deltaw;
+    default: return nullptr;
+  }
+}
+
+bool is_static(int f) {
+  switch (f) {
+    case MOLOCH_F_ZETA: case MOLOCH_F_FMZ: case MOLOCH_F_FMZF: case MOLOCH_F_HT:
+    case MOLOCH_F_MSFX: case MOLOCH_F_MSFU: case MOLOCH_F_MSFV: case MOLOCH_F_HX: case MOLOCH_F_HY:
+    case MOLOCH_F_ULAT: case MOLOCH_F_VLAT: case MOLOCH_F_ZITA: case MOLOCH_F_ZITAH:
+      return true;
+    default:
+      return false;
+  }
+}
+
+std::vector<double>* static_store(moloch_handle* h, int f) {
+  switch (f) {
+    case MOLOCH_F_ZETA: return &h->zeta;
+    case MOLOCH_F_FMZ: return &h->fmz;
+    case MOLOCH_F_FMZF: return &h->fmzf;
+    case MOLOCH_F_MSFX: return &h->msfx;
+    case MOLOCH_F_MSFU: return &h->msfu;
+    case MOLOCH_F_MSFV: return &h->msfv;
+    case MOLOCH_F_HX: return &h->hx;
+    case MOLOCH_F_HY: return &h->hy;
+    case MOLOCH_F_ULAT: return &h->ulat;
+    case MOLOCH_F_VLAT: return &h->vlat;
+    case MOLOCH_F_ZITA: return &h->zita;
+    case MOLOCH_F_ZITAH: return &h->zitah;
+    default: return nullptr;
+  }
+}
+
+// init_moloch (nompi/mod_moloch.F90:219-268) and the static terms the
+// kernels reuse, all in FP64 with the reference's evaluation order.
+template <class T>
+int init_impl(moloch_handle* h, View<T>& v) {
+  const int nj = h->nj(), ni = h->ni(), kz = h->kz();
+  const size_t pl = (size_t)nj * ni;
+  const moloch_params_t& P = h->prm;
+  auto I2 = [&](int j, int i) { return (size_t)wrap(j, nj) + (size_t)nj * wrap(i, ni); };
+  auto I3 = [&](int j, int i, int k) { return I2(j, i) + pl * (size_t)(k - 1); };
+  const std::vector<double>&fmz = h->fmz, &fmzf = h->fmzf;
+
+  // scalars (moloch :285-286, sound :495-498, divdamp :863,884, wafone :951-956)
+  const double dzita = h->zita[kz - 1];  // mo_dzita = zita(kz) (regcm_dynamical_core.F90:121)
+  const double dta = P.dt / (double)P.mo_nadv;
+  const double dts = dta / (double)P.mo_nsound;
+  const double dtrdx = dts / P.dx, dtrdy = dts / P.dx, dtrdz = dts / dzita;
+  const double zcs2 = (dtrdz * dtrdz) * kRdrcv;
+  const double ddamp = 0.125 * (P.dx / dts);
+  const double ddamp2 = (kXdamp * 0.015625) / dts;
+  const double dtrdx_a = dta / P.dx, dtrdy_a = dta / P.dx;
+  const double dtrdz_a = 0.5 * (dta / dzita);
+  v.dts = (T)dts; v.dtrdx = (T)dtrdx; v.dtrdy = (T)dtrdy; v.dtrdz = (T)dtrdz; v.zcs2 = (T)zcs2;
+  v.ddamp2 = (T)ddamp2; v.egdts = (T)(kEgrav * dts);
+  v.dts_d = dts; v.dtrdz_d = dtrdz; v.zcs2_d = zcs2; v.egdts_d = kEgrav * dts;
+  v.dtrdx_a = (T)dtrdx_a; v.dtrdy_a = (T)dtrdy_a; v.dtrdz_a = (T)dtrdz_a;
+  v.anu2 = (T)P.mo_anu2;
+
+  // 1-D tables
+  std::vector<double> gzk(kz + 1), gzkh(kz), xknu(kz), cdamp(kz), ffilt(kz, 0.0);
+  for (int k = 1; k <= kz + 1; ++k) gzk[k - 1] = gzita(h->zita[k - 1], P.mo_ztop, P.mo_a0);
+  for (int k = 1; k <= kz; ++k) gzkh[k - 1] = gzita(h->zitah[k - 1], P.mo_ztop, P.mo_a0);
+  for (int k = 1; k <= kz; ++k) {  // allocate_moloch :207-210
+    xknu[k - 1] = kXdamp + (1.0 - kXdamp) * std::sin((0.5 * kPi) * (1.0 - (double)(k - 1) / (double)(kz - 1)));
+    cdamp[k - 1] = xknu[k - 1] * ddamp;
+  }
+  int rc;
+  if ((rc = upload_dense<T>(h, (T*)v.gzitak, gzk))) return rc;
+  if ((rc = upload_dense<T>(h, (T*)v.gzitakh, gzkh))) return rc;
+  if ((rc = upload_dense<T>(h, (T*)v.xknu, xknu))) return rc;
+  if ((rc = upload_dense<T>(h, (T*)v.cdamp, cdamp))) return rc;
+  if ((rc = upload_dense<T>(h, (T*)v.ffilt, ffilt))) return rc;
+
+  // 2-D terms (init_moloch :252-256); msfu/msfv/hx/hy halos are periodic
+  std::vector<double> a(pl), b(pl);
+  auto up2 = [&](const T* dst, const std::vector<double>& src) { return upload_dense<T>(h, (T*)dst, src); };
+  for (int i = 1; i <= ni; ++i)
+    for (int j = 1; j <= nj; ++j) {
+      a[I2(j, i)] = kEomeg2 * std::sin(h->ulat[I2(j, i)] * kDegrad);
+      b[I2(j, i)] = kEomeg2 * std::sin(h->vlat[I2(j, i)] * kDegrad);
+    }
+  if ((rc = up2(v.coru, a)) || (rc = up2(v.corv, b))) return rc;
+  for (size_t q = 0; q < pl; ++q) a[q] = h->msfx[q] * h->msfx[q];
+  if ((rc = up2(v.mx2, a)) || (rc = up2(v.mx, h->msfx))) return rc;
+  if ((rc = up2(v.mu, h->msfu)) || (rc = up2(v.mv, h->msfv))) return rc;
+  for (size_t q = 0; q < pl; ++q) { a[q] = 1.0 / h->msfu[q]; b[q] = 1.0 / h->msfv[q]; }
+  if ((rc = up2(v.rmu, a)) || (rc = up2(v.rmv, b))) return rc;
+  if ((rc = up2(v.hx, h->hx)) || (rc = up2(v.hy, h->hy))) return rc;
+
+  // 3-D static terms
+  const size_t n3 = pl * kz;
+  std::vector<double> rfw(n3), rfs(n3), wu(n3), wd(n3), wn(n3), ws(n3), we(n3), ww(n3), dz(n3);
+  for (int k = 1; k <= kz; ++k)
+    for (int i = 1; i <= ni; ++i)
+      for (int j = 1; j <= nj; ++j) {
+        const size_t q = I3(j, i, k);
+        const double f = fmz[q];
+        rfw[q] = 2.0 / (f + fmz[I3(j - 1, i, k)]);   // sound :584
+        rfs[q] = 2.0 / (f + fmz[I3(j, i - 1, k)]);   // sound :585
+        wu[q] = (dtrdz_a * f) / fmzf[I2(j, i) + pl * (size_t)(k - 1)];  // wafone :1011
+        wd[q] = (dtrdz_a * f) / fmzf[I2(j, i) + pl * (size_t)k];        // wafone :1012
+        const double fn = fmz[I3(j, i + 1, k)], fs = fmz[I3(j, i - 1, k)];
+        const double fe = fmz[I3(j + 1, i, k)], fw = fmz[I3(j - 1, i, k)];
+        const double rmvn = 1.0 / h->msfv[I2(j, i + 1)], rmvs = 1.0 / h->msfv[I2(j, i)];
+        const double mxx = h->msfx[I2(j, i)], muu = h->msfu[I2(j, i)];
+        if (P.rotllr) {
+          const double zhxvtn = (dtrdy_a * rmvn) * mxx, zhxvts = (dtrdy_a * rmvs) * mxx;  // :1120-1121
+          wn[q] = ((zhxvtn * 2.0) * f) / (f + fn);
+          ws[q] = ((zhxvts * 2.0) * f) / (f + fs);
+          const double zcostx = dtrdx_a * muu;  // :1177
+          we[q] = ((zcostx * 2.0) * f) / (f + fe);
+          ww[q] = ((zcostx * 2.0) * f) / (f + fw);
+        } else {  // :1230-1231, :1287-1288
+          wn[q] = ((dtrdy_a * 2.0) * f) / (f + fn);
+          ws[q] = ((dtrdy_a * 2.0) * f) / (f + fs);
+          we[q] = ((dtrdx_a * 2.0) * f) / (f + fe);
+          ww[q] = ((dtrdx_a * 2.0) * f) / (f + fw);
+        }
+        dz[q] = dzita / f;  // layer thickness for the column sums
+      }
+  auto up3 = [&](const T* dst, const std::vector<double>& src) { return upload_dense<T>(h, (T*)dst, src); };
+  if ((rc = up3(v.fmz, fmz)) || (rc = up3(v.fmzf, fmzf)) || (rc = up3(v.zeta, h->zeta))) return rc;
+  if ((rc = up3(v.rfw, rfw)) || (rc = up3(v.rfs, rfs)) || (rc = up3(v.wafu, wu)) || (rc = up3(v.wafd, wd)))
+    return rc;
+  if ((rc = up3(v.wafn, wn)) || (rc = up3(v.wafs, ws)) || (rc = up3(v.wafe, we)) || (rc = up3(v.wafw, ww)))
+    return rc;
+  if ((rc = up3(v.dz, dz))) return rc;
+  // w(:,:,1) = 0 (:260-262); s, deltaw zero (reset_tendencies :1313-1325 --
+  // the kernels never write s(1), deltaw(1), deltaw(kz+1), which therefore
+  // keep this zero for the whole run)
+  CUDA_TRY(cudaMemsetAsync(v.w, 0, sizeof(T) * pl, h->stream));
+  CUDA_TRY(cudaMemsetAsync(v.s, 0, sizeof(T) * pl * (kz + 1), h->stream));
+  CUDA_TRY(cudaMemsetAsync(v.deltaw, 0, sizeof(T) * pl * (kz + 1), h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return MOLOCH_OK;
+}
+
+// one phase or a whole step on the handle's stream; returns kernel count
+template <class T>
+int launch_phase(moloch_handle* h, View<T>& v, int phase) {
+  const PhaseFlags fl = flags_of(h);
+  const bool exact = h->prm.mode == MOLOCH_FP64_EXACT;
+  const T* zk = v.zeta + (size_t)v.pl * (v.kz - 1);
+  const T* zkm1 = v.zeta + (size_t)v.pl * (v.kz - 2);
+  int n = 0;
+  if constexpr (sizeof(T) == sizeof(double)) {
+    if (exact) {
+      switch (phase) {
+        case 0: n = kexact::launch_prediag<T>(v, h->stream, fl); break;
+        case 1: n = kexact::launch_sound<T>(v, h->stream, fl); break;
+        case 2: n = kexact::launch_advection<T>(v, h->stream); break;
+        case 3: n = kexact::launch_postdiag<T>(v, h->stream, fl, zk, zkm1); break;
+        case 4: n = kexact::launch_diag<T>(v, h->stream); break;
+      }
+      return n;
+    }
+  }
+  switch (phase) {
+    case 0: n = kfast::launch_prediag<T>(v, h->stream, fl); break;
+    case 1: n = kfast::launch_sound<T>(v, h->stream, fl); break;
+    case 2: n = kfast::launch_advection<T>(v, h->stream); break;
+    case 3: n = kfast::launch_postdiag<T>(v, h->stream, fl, zk, zkm1); break;
+    case 4: n = kfast::launch_diag<T>(v, h->stream); break;
+  }
+  return n;
+}
+
+template <class T>
+int launch_step(moloch_handle* h, View<T>& v) {
+  int n = launch_phase(h, v, 0);
+  for (int a = 0; a < h->prm.mo_nadv; ++a) {
+    n += launch_phase(h, v, 1);
+    n += launch_phase(h, v, 2);
+  }
+  n += launch_phase(h, v, 3);
+  return n;
+}
+
+int step_kernels(moloch_handle* h) {
+  if (h->elem == 8) return launch_step(h, h->vd);
+  return launch_step(h, h->vf);
+}
+
+int check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(MOLOCH_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return MOLOCH_OK;
+}
+
+int read_diag(moloch_handle* h, moloch_diag_t* diag) {
+  int n = h->elem == 8 ? launch_phase(h, h->vd, 4) : launch_phase(h, h->vf, 4);
+  h->kernels += n;
+  int rc;
+  if ((rc = check_launch("diag"))) return rc;
+  const double* dres = h->elem == 8 ? h->vd.dres : h->vf.dres;
+  CUDA_TRY(cudaMemcpyAsync(h->hres, dres, sizeof(double) * 9, cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  moloch_diag_t d{};
+  d.maxps = h->hres[0]; d.minps = h->hres[1];
+  d.maxu = h->hres[2]; d.minu = h->hres[3]; d.maxv = h->hres[4]; d.minv = h->hres[5];
+  d.mass = h->hres[6]; d.energy = h->hres[7];
+  d.nonfinite = (int)h->hres[8];
+  const bool bad = d.nonfinite > 0 || !std::isfinite(d.maxps) || !std::isfinite(d.minps);
+  d.status = bad ? MOLOCH_ERR_CFL : MOLOCH_OK;
+  if (diag) *diag = d;
+  if (bad) return fail(MOLOCH_ERR_CFL, "CFL VIOLATION: %d non-finite ps values", d.nonfinite);
+  return MOLOCH_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+extern "C" {
+
+const char* moloch_gpu_last_error(void) { return g_err.c_str(); }
+
+void moloch_gpu_default_params(moloch_params_t* p) {
+  if (!p) return;
+  std::memset(p, 0, sizeof *p);
+  p->dt = 30.0;
+  p->dx = 3.0 * 1000.0;
+  p->mo_ztop = 36000.0;
+  p->mo_h = 12000.0;
+  p->mo_a0 = 0.0;
+  p->mo_anu2 = 0.6;
+  p->mo_nadv = 3;
+  p->mo_nsound = 5;
+  p->mode = MOLOCH_FP64;
+  p->rotllr = 1;
+}
+
+int moloch_gpu_create(const moloch_grid_t* grid, const moloch_params_t* params, void* stream,
+                      moloch_handle_t** out) {
+  g_err.clear();
+  if (!grid || !params || !out) return fail(MOLOCH_ERR_ARG, "null argument");
+  *out = nullptr;
+  if (grid->jx < 4 || grid->iy < 4 || grid->kz < 4)
+    return fail(MOLOCH_ERR_ARG, "grid %dx%dx%d too small (need jx, iy, kz >= 4)", grid->jx, grid->iy, grid->kz);
+  if ((double)grid->jx * grid->iy * (grid->kz + 1) > 2.0e9)
+    return fail(MOLOCH_ERR_ARG, "grid too large for one handle");
+  if (params->mode < MOLOCH_FP64 || params->mode > MOLOCH_FP32_MIXED)
+    return fail(MOLOCH_ERR_ARG, "unknown mode %d", params->mode);
+  if (params->mo_nadv < 1 || params->mo_nsound < 1 || !(params->dt > 0) || !(params->dx > 0))
+    return fail(MOLOCH_ERR_ARG, "bad time parameters");
+  moloch_handle* h = new moloch_handle();
+  h->grid = *grid;
+  h->prm = *params;
+  h->elem = params->mode == MOLOCH_FP32_MIXED ? 4 : 8;
+  if (stream) {
+    h->stream = (cudaStream_t)stream;
+  } else {
+    cudaError_t e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) {
+      delete h;
+      return fail(MOLOCH_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+    }
+    h->own_stream = true;
+  }
+  size_t bytes = h->elem == 8 ? layout(h->vd, nullptr, h) : layout(h->vf, nullptr, h);
+  cudaError_t e = cudaMalloc(&h->arena, bytes);
+  if (e != cudaSuccess) {
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    delete h;
+    cudaGetLastError();
+    return fail(MOLOCH_ERR_NOMEM, "device arena of %zu bytes: %s", bytes, cudaGetErrorString(e));
+  }
+  h->arena_bytes = bytes;
+  if (h->elem == 8) layout(h->vd, (char*)h->arena, h); else layout(h->vf, (char*)h->arena, h);
+  cudaMemsetAsync(h->arena, 0, bytes, h->stream);  // getmem zero-fills (mod_memutil.F90:1249)
+  e = cudaMallocHost(&h->hres, sizeof(double) * 16);
+  if (e == cudaSuccess) {
+    h->stage_bytes = sizeof(double) * (size_t)grid->jx * grid->iy * (grid->kz + 1);
+    e = cudaMallocHost(&h->stage, h->stage_bytes);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  if (e != cudaSuccess) {
+    cudaFree(h->arena);
+    if (h->own_stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return fail(MOLOCH_ERR_CUDA, "create: %s", cudaGetErrorString(e));
+  }
+  *out = h;
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_upload(moloch_handle_t* h, int field, const double* host_base, const int* lb, const int* ub) {
+  g_err.clear();
+  if (!h || !host_base || !lb || !ub) return fail(MOLOCH_ERR_ARG, "null argument");
+  const int nj = h->nj(), ni = h->ni(), kz = h->kz();
+  FieldShape s = shape_of(field, nj, ni, kz);
+  if (s.ndim == 0) return fail(MOLOCH_ERR_ARG, "unknown field %d", field);
+  for (int d = 0; d < s.ndim; ++d)
+    if (lb[d] != s.lb[d] || ub[d] != s.ub[d])
+      return fail(MOLOCH_ERR_BOUNDS, "field %d dim %d: bounds %d:%d, expected %d:%d", field, d + 1, lb[d], ub[d],
+                  s.lb[d], s.ub[d]);
+  if (field == MOLOCH_F_ZITA || field == MOLOCH_F_ZITAH) {
+    std::vector<double>* st = static_store(h, field);
+    st->assign(host_base, host_base + (s.ub[0] - s.lb[0] + 1));
+    h->uploaded |= 1u << field;
+    return MOLOCH_OK;
+  }
+  const int nk = s.ndim >= 3 ? s.ub[2] : 1;
+  std::vector<double> dense;
+  if (field == MOLOCH_F_HT) {  // not used by the step; accepted for completeness
+    h->uploaded |= 1u << field;
+    return MOLOCH_OK;
+  }
+  if (is_static(field)) {
+    gather_interior(host_base, s, nj, ni, nk, 0, dense);
+    *static_store(h, field) = dense;
+    h->uploaded |= 1u << field;
+    if (h->initialized) h->initialized = false;  // statics changed: init again
+    return MOLOCH_OK;
+  }
+  if (field == MOLOCH_F_QX) {
+    for (int n = 0; n < 5; ++n) {
+      gather_interior(host_base, s, nj, ni, nk, n, dense);
+      int rc = h->elem == 8 ? upload_dense<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), dense)
+                            : upload_dense<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), dense);
+      if (rc) return rc;
+      h->uploaded |= 1u << (MOLOCH_F_QV + n);
+    }
+    return MOLOCH_OK;
+  }
+  gather_interior(host_base, s, nj, ni, nk, 0, dense);
+  int rc;
+  if (h->elem == 8) {
+    double* p = field_ptr(h->vd, field);
+    if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", field);
+    rc = upload_dense<double>(h, p, dense);
+  } else {
+    float* p = field_ptr(h->vf, field);
+    if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", field);
+    rc = upload_dense<float>(h, p, dense);
+  }
+  if (!rc) h->uploaded |= 1u << field;
+  return rc;
+}
+
+int moloch_gpu_init(moloch_handle_t* h) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  const int need[] = {MOLOCH_F_U, MOLOCH_F_V, MOLOCH_F_W, MOLOCH_F_PAI, MOLOCH_F_T, MOLOCH_F_QV, MOLOCH_F_QC,
+                      MOLOCH_F_QI, MOLOCH_F_QR, MOLOCH_F_QS, MOLOCH_F_ZETA, MOLOCH_F_FMZ, MOLOCH_F_FMZF,
+                      MOLOCH_F_MSFX, MOLOCH_F_MSFU, MOLOCH_F_MSFV, MOLOCH_F_HX, MOLOCH_F_HY, MOLOCH_F_ULAT,
+                      MOLOCH_F_VLAT, MOLOCH_F_ZITA, MOLOCH_F_ZITAH};
+  for (int f : need)
+    if (!(h->uploaded & (1u << f))) return fail(MOLOCH_ERR_STATE, "init before field %d was uploaded", f);
+  int rc = h->elem == 8 ? init_impl(h, h->vd) : init_impl(h, h->vf);
+  if (rc) return rc;
+  if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
+  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  h->initialized = true;
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_step(moloch_handle_t* h, int istep, int lprint, moloch_diag_t* diag) {
+  g_err.clear();
+  (void)istep;  // the reference uses istep only in its printout (:412)
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  if (!h->initialized) return fail(MOLOCH_ERR_STATE, "step before moloch_gpu_init");
+  int n = step_kernels(h);
+  h->kernels += n;
+  h->kernels_per_step = n;
+  int rc = check_launch("step");
+  if (rc) return rc;
+  if (lprint) return read_diag(h, diag);
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_run(moloch_handle_t* h, int nsteps, int use_graph) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  if (!h->initialized) return fail(MOLOCH_ERR_STATE, "run before moloch_gpu_init");
+  if (nsteps < 0) return fail(MOLOCH_ERR_ARG, "nsteps < 0");
+  if (!use_graph) {
+    for (int s = 0; s < nsteps; ++s) {
+      int n = step_kernels(h);
+      h->kernels += n;
+      h->kernels_per_step = n;
+      int rc = check_launch("run");
+      if (rc) return rc;
+    }
+    return MOLOCH_OK;
+  }
+  if (!h->gexec) {
+    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+    int n = step_kernels(h);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+    if (e != cudaSuccess) return fail(MOLOCH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    h->graph = g;
+    CUDA_TRY(cudaGraphInstantiate(&h->gexec, h->graph, 0));
+    h->kernels_per_step = n;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    CUDA_TRY(cudaGraphLaunch(h->gexec, h->stream));
+    h->kernels += h->kernels_per_step;
+  }
+  return check_launch("graph replay");
+}
+
+int moloch_gpu_phase(moloch_handle_t* h, int phase) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  if (!h->initialized) return fail(MOLOCH_ERR_STATE, "phase before moloch_gpu_init");
+  if (phase < 0 || phase > 3) return fail(MOLOCH_ERR_ARG, "phase %d", phase);
+  int n = h->elem == 8 ? launch_phase(h, h->vd, phase) : launch_phase(h, h->vf, phase);
+  h->kernels += n;
+  return check_launch("phase");
+}
+
+int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base, const int* lb, const int* ub) {
+  g_err.clear();
+  if (!h || !host_base || !lb || !ub) return fail(MOLOCH_ERR_ARG, "null argument");
+  const int nj = h->nj(), ni = h->ni(), kz = h->kz();
+  FieldShape s = shape_of(field, nj, ni, kz);
+  if (s.ndim == 0) return fail(MOLOCH_ERR_ARG, "unknown field %d", field);
+  for (int d = 0; d < s.ndim; ++d)
+    if (lb[d] != s.lb[d] || ub[d] != s.ub[d])
+      return fail(MOLOCH_ERR_BOUNDS, "field %d dim %d: bounds %d:%d, expected %d:%d", field, d + 1, lb[d], ub[d],
+                  s.lb[d], s.ub[d]);
+  if (field == MOLOCH_F_ZITA || field == MOLOCH_F_ZITAH) {
+    std::vector<double>* st = static_store(h, field);
+    if (st->empty()) return fail(MOLOCH_ERR_STATE, "field %d not uploaded", field);
+    std::memcpy(host_base, st->data(), sizeof(double) * st->size());
+    return MOLOCH_OK;
+  }
+  const int nk = s.ndim >= 3 ? s.ub[2] : 1;
+  std::vector<double> dense;
+  if (is_static(field)) {
+    std::vector<double>* st = static_store(h, field);
+    if (!st || st->empty()) return fail(MOLOCH_ERR_STATE, "field %d not available", field);
+    scatter_periodic(*st, s, nj, ni, nk, 0, host_base);
+    return MOLOCH_OK;
+  }
+  if (field == MOLOCH_F_QX) {
+    for (int n = 0; n < 5; ++n) {
+      int rc = h->elem == 8
+                   ? download_dense<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), (size_t)nj * ni * kz, dense)
+                   : download_dense<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), (size_t)nj * ni * kz, dense);
+      if (rc) return rc;
+      scatter_periodic(dense, s, nj, ni, kz, n, host_base);
+    }
+    return MOLOCH_OK;
+  }
+  const size_t n = (size_t)nj * ni * nk;
+  int rc = h->elem == 8 ? download_dense<double>(h, field_ptr(h->vd, field), n, dense)
+                        : download_dense<float>(h, field_ptr(h->vf, field), n, dense);
+  if (rc) return rc;
+  scatter_periodic(dense, s, nj, ni, nk, 0, host_base);
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_sync(moloch_handle_t* h) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return MOLOCH_OK;
+}
+
+void* moloch_gpu_stream(moloch_handle_t* h) { return h ? (void*)h->stream : nullptr; }
+
+long long moloch_gpu_kernel_count(moloch_handle_t* h) { return h ? h->kernels : -1; }
+
+static const char* const kKindNames[KK_COUNT] = {
+    "k_prediag", "k_sound_div", "k_sound_column", "k_lap_filter", "k_pai_update", "k_sound_momentum",
+    "k_stag_to_x", "k_waf_vertical", "k_waf_meridional", "k_waf_zonal", "k_stag_from_x",
+    "k_filter_increment", "k_postdiag", "k_diag"};
+
+int moloch_gpu_kernel_kinds(void) { return KK_COUNT; }
+
+const char* moloch_gpu_kernel_name(int kind) { return (kind >= 0 && kind < KK_COUNT) ? kKindNames[kind] : ""; }
+
+int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launches_by_kind, int nkinds) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  if (!h->initialized) return fail(MOLOCH_ERR_STATE, "profile before moloch_gpu_init");
+  KernelTimer* tm = new KernelTimer();
+  for (int q = 0; q < KernelTimer::kCap; ++q)
+    if (cudaEventCreate(&tm->ev[q]) != cudaSuccess) {
+      for (int r = 0; r < q; ++r) cudaEventDestroy(tm->ev[r]);
+      delete tm;
+      return fail(MOLOCH_ERR_CUDA, "event create");
+    }
+  kfast::set_timer(tm);
+  kexact::set_timer(tm);
+  int n = step_kernels(h);
+  kfast::set_timer(nullptr);
+  kexact::set_timer(nullptr);
+  h->kernels += n;
+  int rc = check_launch("profile");
+  if (!rc && cudaStreamSynchronize(h->stream) != cudaSuccess) rc = fail(MOLOCH_ERR_CUDA, "profile sync");
+  if (!rc && !tm->ok) rc = fail(MOLOCH_ERR_ARG, "too many kernels to profile one step");
+  if (!rc) {
+    for (int q = 0; q + 1 < tm->n; q += 2) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, tm->ev[q], tm->ev[q + 1]);
+      int k = tm->kind[q / 2];
+      if (k < nkinds) {
+        if (ms_by_kind) ms_by_kind[k] += ms;
+        if (launches_by_kind) launches_by_kind[k] += 1;
+      }
+    }
+  }
+  for (int q = 0; q < KernelTimer::kCap; ++q) cudaEventDestroy(tm->ev[q]);
+  delete tm;
+  return rc;
+}
+
+int moloch_internal_describe(moloch_handle_t* h, moloch_grid_t* g, moloch_params_t* p) {
+  if (!h || !g || !p) return fail(MOLOCH_ERR_ARG, "null argument");
+  *g = h->grid;
+  *p = h->prm;
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_destroy(moloch_handle_t* h) {
+  if (!h) return MOLOCH_OK;
+  cudaStreamSynchronize(h->stream);
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  if (h->graph) cudaGraphDestroy(h->graph);
+  if (h->arena) cudaFree(h->arena);
+  if (h->hres) cudaFreeHost(h->hres);
+  if (h->stage) cudaFreeHost(h->stage);
+  if (h->own_stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return MOLOCH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,24 @@
+// Declarations of the kernel launchers compiled in the kernel translation
+// units (moloch_kernels_exact.cu: FP64 without multiply-add contraction;
+// moloch_kernels_fast.cu: FP64 and FP32 with contraction).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "moloch_view.h"
+
+namespace moloch {
+#define MOLOCH_DECLARE_LAUNCHERS(NS)                                                                \
+  namespace NS {                                                                                    \
+  template <class T> int launch_prediag(const View<T>& d, cudaStream_t st, const PhaseFlags& fl);  \
+  template <class T> int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl);          \
+  template <class T> int launch_advection(View<T>& d, cudaStream_t st);                            \
+  template <class T>                                                                                \
+  int launch_postdiag(View<T>& d, cudaStream_t st, const PhaseFlags& fl, const T* zk, const T* zkm1); \
+  template <class T> int launch_diag(const View<T>& d, cudaStream_t st);                           \
+  int diag_parts(int nj, int ni);                                                                   \
+  void set_timer(KernelTimer* t);                                                                   \
+  }
+MOLOCH_DECLARE_LAUNCHERS(kexact)
+MOLOCH_DECLARE_LAUNCHERS(kfast)
+#undef MOLOCH_DECLARE_LAUNCHERS
+}  // namespace moloch

@@ -1,0 +1,143 @@
+// Device-side view of one MOLOCH domain: pointers into HBM plus the scalars
+// a step needs.  Shared by the kernel translation units and the host API.
+//
+// Layout (all 3-D fields): dense, j fastest, then i, then k -- the
+// reference's Fortran column-major order without the halo rings:
+//     idx(j, i, k) = (j-1) + nj * ((i-1) + ni * (k-1))      (1-based j, i, k)
+// Threads map to j, so every warp access is a contiguous row segment.
+// Periodic halos are not stored: stencils wrap their indices.  The three
+// places where the reference reads a halo that is OLDER than the interior
+// (nompi/mod_moloch.F90:716-735: pai filled before its update, ud/vd copied
+// after divdamp changed the interior but not the ring) are kept in small
+// edge buffers written by the kernel that owns the old values.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+
+namespace moloch {
+
+constexpr int kNumAdvected = 10;  // tetav pai ux vx wx qv qc qi qr qs (mod_moloch.F90:911-920)
+
+template <class T>
+struct View {
+  int nj, ni, kz;
+  int pl;  // nj * ni, one level
+  int rotllr;
+
+  // prognostic state
+  T* ubuf[2];
+  T* vbuf[2];
+  int cur;  // which of ubuf/vbuf holds the current u, v
+  T* w;     // kz+1 levels
+  T* pai;
+  T* tetav;
+  T* t;
+  T* q[5];  // qv qc qi qr qs
+  // diagnostics
+  T* p;
+  T* qsat;
+  T* tvirt;
+  T* rho;
+  T* ps;  // one level
+  T* qwltot;
+  T* qwitot;
+  // work
+  T* s;       // kz+1 levels
+  T* deltaw;  // kz+1 levels
+  T* zdiv2a;  // horizontal divergence (Equation 16)
+  T* zdiv2b;  // after divdamp and the vertical s term
+  double* wp;    // Thomas down-sweep values (FP64 in every mode), kz+1 levels
+  double* wwkw;  // Thomas pivot ratios (FP64 in every mode), kz+1 levels
+  T* ux;
+  T* vx;
+  T* wx;
+  T* wz;  // kNumAdvected fields
+  T* p0;  // kNumAdvected fields
+  T* pf;
+  T* tf;
+  T* fscr;  // filter output scratch
+  // edge buffers of stale halos (see header)
+  T* eu_j;  // u before divdamp at j = 1, one per (i, k)    [ud(nj+1, i)]
+  T* eu_i;  // u before divdamp at i = ni, one per (j, k)   [ud(j, 0)]
+  T* ev_j;  // v before divdamp at j = nj, per (i, k)       [vd(0, i)]
+  T* ev_i;  // v before divdamp at i = 1, per (j, k)        [vd(j, ni+1)]
+  T* ep_j;  // pai before its update at j = nj, per (i, k)  [pai(0, i)]
+  T* ep_i;  // pai before its update at i = ni, per (j, k)  [pai(j, 0)]
+
+  // static 3-D metric terms (computed once on the host in FP64)
+  const T* fmz;
+  const T* fmzf;  // kz+1 levels
+  const T* zeta;
+  const T* dz;
+  const T* rfw;   // 2 / (fmz(j) + fmz(j-1))
+  const T* rfs;   // 2 / (fmz(i) + fmz(i-1))
+  const T* wafu;  // wafone zrfmu
+  const T* wafd;  // wafone zrfmd
+  const T* wafn;  // wafone zrfmn
+  const T* wafs;  // wafone zrfms
+  const T* wafe;  // wafone zrfme
+  const T* wafw;  // wafone zrfmw
+  // static 2-D terms
+  const T* hx;
+  const T* hy;
+  const T* mx;
+  const T* mu;
+  const T* mv;
+  const T* rmu;
+  const T* rmv;
+  const T* mx2;
+  const T* coru;
+  const T* corv;
+  // 1-D level tables
+  const T* gzitak;   // kz+1
+  const T* gzitakh;  // kz
+  const T* xknu;     // kz
+  const T* cdamp;    // xknu(k) * ddamp
+  const T* ffilt;    // kz (zero in the reference)
+
+  // scalars of sound() (dts) and wafone() (dta)
+  T dts, dtrdx, dtrdy, dtrdz, zcs2, ddamp2, egdts;
+  double dts_d, dtrdz_d, zcs2_d, egdts_d;
+  T dtrdx_a, dtrdy_a, dtrdz_a;  // wafone: dta/dx, dta/dx, 0.5*dta/dzita
+  T anu2;
+
+  // diagnostics
+  double* dpart;  // per-block partial reductions
+  double* dres;   // final reduction (device)
+  int dparts;
+};
+
+// Kernel kinds, for per-kernel CUDA-event timing (moloch_gpu_profile_step).
+enum KernelKind {
+  KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE, KK_SOUND_MOMENTUM,
+  KK_STAG_TO_X, KK_WAF_VERTICAL, KK_WAF_MERIDIONAL, KK_WAF_ZONAL, KK_STAG_FROM_X,
+  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_COUNT
+};
+
+// Optional event recorder: when a launcher is given one, it records a CUDA
+// event on the launching stream before and after every kernel.
+struct KernelTimer {
+  static constexpr int kCap = 4096;
+  cudaEvent_t ev[kCap];
+  int kind[kCap / 2];
+  int n = 0;  // events recorded
+  bool ok = true;
+  void mark(int k, cudaStream_t st, bool begin) {
+    if (n >= kCap) { ok = false; return; }
+    if (begin) kind[n / 2] = k;
+    cudaEventRecord(ev[n++], st);
+  }
+};
+
+// launch counts per phase are returned by the launchers so the API can
+// account for every kernel it starts
+struct PhaseFlags {
+  int divfilter;
+  int filterpai;
+  int filtertheta;
+  int nsound;
+  int nadv;
+};
+
+}  // namespace moloch

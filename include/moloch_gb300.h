@@ -1,0 +1,203 @@
+/*
+ * moloch_gb300.h -- C ABI of the GB300-native MOLOCH dynamical-core step.
+ *
+ * This is the drop-in boundary for the reference's Fortran module
+ * `mod_moloch` (nompi/mod_moloch.F90), whose public interface is
+ *     public :: allocate_moloch , init_moloch , moloch        (:93)
+ * A replacement `mod_moloch` written with ISO_C_BINDING keeps those three
+ * names and forwards to the functions below (INTEGRATION.md shows the shim).
+ * All arrays cross the boundary as plain host pointers to the Fortran arrays
+ * (column-major, j fastest) together with their lower and upper bounds, so
+ * the library can check the layout contract of nompi/mod_atmosphere.F90:104-169
+ * and nompi/mod_moloch.F90:183-217.  No PyTorch or CUDA types appear here;
+ * the only CUDA object is an optional stream passed as `void*`.
+ *
+ * Every function returns 0 on success or one of the MOLOCH_ERR_* codes; the
+ * text of the last error of the calling thread is in moloch_gpu_last_error().
+ * A handle owns one CUDA stream and is not re-entrant (the reference is a
+ * single-threaded program).
+ */
+#ifndef MOLOCH_GB300_H
+#define MOLOCH_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes -------------------------------------------------------- */
+#define MOLOCH_OK 0
+#define MOLOCH_ERR_ARG 1      /* bad argument, size or option */
+#define MOLOCH_ERR_BOUNDS 2   /* array bounds differ from the layout contract */
+#define MOLOCH_ERR_CUDA 3     /* a CUDA call failed */
+#define MOLOCH_ERR_CFL 4      /* ps not finite: "CFL VIOLATION" (mod_moloch.F90:402-411) */
+#define MOLOCH_ERR_STATE 5    /* call out of order (e.g. step before init) */
+#define MOLOCH_ERR_TIMEOUT 6  /* a bounded device wait gave up */
+#define MOLOCH_ERR_NOMEM 7    /* device allocation failed */
+
+/* ---- arithmetic modes ---------------------------------------------------- */
+#define MOLOCH_FP64 0        /* plain FP64, multiply-add contraction allowed */
+#define MOLOCH_FP64_EXACT 1  /* FP64 in the reference's evaluation order, no FMA */
+#define MOLOCH_FP32_MIXED 2  /* FP32 storage and stencils, FP64 tridiagonal solve and column sums */
+
+/* ---- field identifiers for upload / download ------------------------------
+ * Bounds (j, i, k) with nj = jx, ni = iy follow the reference allocations:
+ *   u            (-1:nj+2, 0:ni+1, 1:kz)      mod_atmosphere.F90:107
+ *   v            (0:nj+1, -1:ni+2, 1:kz)      :108
+ *   t tetav pai  (0:nj+1, 0:ni+1, 1:kz)      :111-114
+ *   w            (1:nj, 1:ni, 1:kz+1)         :113
+ *   qx           (0:nj+1, 0:ni+1, 1:kz, 1:5)  :115   (MOLOCH_F_QX, 4-D)
+ *   qv..qs       the 3-D slices of qx         (mod_moloch.F90:247-251)
+ *   zeta         (-1:nj+2, -1:ni+2, 1:kz)     :116
+ *   p tvirt qs(qsat) rho  (1:nj, 1:ni, 1:kz)  :118-124
+ *   fmz          (0:nj+1, 0:ni+1, 1:kz)       :125
+ *   fmzf         (1:nj, 1:ni, 1:kz+1)         :126
+ *   ps           (0:nj+1, 0:ni+1)             :166
+ *   ht           (-1:nj+2, -1:ni+2)           :131
+ *   msfx         (1:nj, 1:ni)                 :140
+ *   msfu         (0:nj+1, 1:ni)               :141
+ *   msfv         (1:nj, 0:ni+1)               :142
+ *   hx           (0:nj+1, 1:ni)               :143
+ *   hy           (1:nj, 0:ni+1)               :144
+ *   ulat vlat    (1:nj, 1:ni)                 :145,147
+ *   zita         (1:kz+1)   zitah (1:kz)      mod_runparams.F90:73-74
+ *   s            (1:nj, 1:ni, 1:kz+1)         mod_moloch.F90:190 (download only)
+ * The domain is doubly periodic (one rank): halo values passed in are not
+ * used, the device recomputes them as periodic images of the interior.
+ * Downloads fill the interior; halo positions receive periodic images. */
+enum moloch_field {
+  MOLOCH_F_U = 0, MOLOCH_F_V, MOLOCH_F_W, MOLOCH_F_PAI, MOLOCH_F_T, MOLOCH_F_TETAV,
+  MOLOCH_F_QV, MOLOCH_F_QC, MOLOCH_F_QI, MOLOCH_F_QR, MOLOCH_F_QS,
+  MOLOCH_F_QX,    /* 4-D qx(:,:,:,1:5), lb[3] = 1, ub[3] = 5 */
+  MOLOCH_F_P, MOLOCH_F_TVIRT, MOLOCH_F_QSAT, MOLOCH_F_RHO, MOLOCH_F_PS,
+  MOLOCH_F_ZETA, MOLOCH_F_FMZ, MOLOCH_F_FMZF, MOLOCH_F_HT,
+  MOLOCH_F_MSFX, MOLOCH_F_MSFU, MOLOCH_F_MSFV, MOLOCH_F_HX, MOLOCH_F_HY,
+  MOLOCH_F_ULAT, MOLOCH_F_VLAT, MOLOCH_F_ZITA, MOLOCH_F_ZITAH,
+  MOLOCH_F_S, MOLOCH_F_DELTAW,
+  MOLOCH_F_COUNT
+};
+
+/* Grid sizes: namelist &dimensions (namelist.in:1-5). */
+typedef struct moloch_grid {
+  int jx, iy, kz;
+} moloch_grid_t;
+
+/* Run parameters set by param() (nompi/regcm_dynamical_core.F90:99-113) and
+ * the compile-time switches of mod_moloch (nompi/mod_moloch.F90:95-106),
+ * here runtime options with the reference defaults noted. */
+typedef struct moloch_params {
+  double dt;        /* 30 s */
+  double dx;        /* 3000 m */
+  double mo_ztop;   /* 36000 m */
+  double mo_h;      /* 12000 m */
+  double mo_a0;     /* 0 */
+  double mo_anu2;   /* 0.6 */
+  int mo_nadv;      /* 3 */
+  int mo_nsound;    /* 5 */
+  int mode;         /* MOLOCH_FP64 | MOLOCH_FP64_EXACT | MOLOCH_FP32_MIXED */
+  int mo_divfilter; /* .false. (mod_runparams.F90:55) */
+  int do_filterpai; /* .false. (mod_moloch.F90:101) */
+  int do_filtertheta; /* .false. (mod_moloch.F90:102) */
+  int rotllr;       /* 1: iproj == 'ROTLLR' (mod_dynparam.F90:39) */
+} moloch_params_t;
+
+/* Printout of moloch(istep, lprint) (nompi/mod_moloch.F90:395-419) plus
+ * the FP64 column sums kept by every mode. */
+typedef struct moloch_diag {
+  double maxps, minps;  /* Pa, over the interior */
+  double maxu, minu, maxv, minv;
+  double mass;          /* sum of rho * dz over all points (kg m^-2 summed over columns), FP64 */
+  double energy;        /* sum of rho * dz * (cvd*T + g*zeta + (u^2+v^2+w^2)/2), FP64 */
+  int status;           /* MOLOCH_OK or MOLOCH_ERR_CFL */
+  int nonfinite;        /* number of non-finite ps values */
+} moloch_diag_t;
+
+typedef struct moloch_handle moloch_handle_t;
+
+/* allocate_moloch (nompi/mod_moloch.F90:183-217): device arrays for one
+ * domain.  `stream` is a cudaStream_t or NULL (the handle then creates one). */
+int moloch_gpu_create(const moloch_grid_t* grid, const moloch_params_t* params,
+                      void* stream, moloch_handle_t** out);
+
+/* Defaults of moloch_params_t as set by the reference's param(). */
+void moloch_gpu_default_params(moloch_params_t* p);
+
+/* Copy one reference array (with its Fortran bounds) to the device.  Part of
+ * init_moloch's role (nompi/mod_moloch.F90:219-268, which aliases the module
+ * arrays with assignpnt): lb/ub hold the lower/upper bound per dimension. */
+int moloch_gpu_upload(moloch_handle_t* h, int field, const double* host_base,
+                      const int* lb, const int* ub);
+
+/* init_moloch (nompi/mod_moloch.F90:219-268): derive coru, corv, mx2, rmu,
+ * rmv, gzitak, gzitakh, xknu and the static metric terms from the uploaded
+ * arrays, set w(:,:,1) = 0.  Call after all uploads. */
+int moloch_gpu_init(moloch_handle_t* h);
+
+/* moloch(istep, lprint) (nompi/mod_moloch.F90:272-421): one dt step.
+ * With lprint != 0 the max/min of ps, u, v and the column sums are reduced
+ * on the device and returned in *diag (may be NULL when lprint == 0); a
+ * non-finite ps returns MOLOCH_ERR_CFL, like the reference's fatal() call. */
+int moloch_gpu_step(moloch_handle_t* h, int istep, int lprint, moloch_diag_t* diag);
+
+/* Run nsteps steps back to back with no host synchronisation in between
+ * (the time loop of nompi/regcm_dynamical_core.F90:49-53 without output).
+ * use_graph != 0 replays one CUDA graph of a whole step. */
+int moloch_gpu_run(moloch_handle_t* h, int nsteps, int use_graph);
+
+/* Copy a field back into a reference-layout host array. */
+int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base,
+                        const int* lb, const int* ub);
+
+/* Block until the handle's stream is idle. */
+int moloch_gpu_sync(moloch_handle_t* h);
+
+/* The stream the handle launches on (a cudaStream_t). */
+void* moloch_gpu_stream(moloch_handle_t* h);
+
+/* Number of kernels this handle has launched (graph replays count each
+ * kernel node), for launch accounting. */
+long long moloch_gpu_kernel_count(moloch_handle_t* h);
+
+/* Run one phase of the step, for per-phase parity checks:
+ * 0 = reset_tendencies + pre-diagnostics (:289-323), 1 = sound() (:483-851),
+ * 2 = advection() (:897-927), 3 = filters + post-diagnostics (:333-391). */
+int moloch_gpu_phase(moloch_handle_t* h, int phase);
+
+/* One step with a CUDA event before and after every kernel on the handle's
+ * stream; adds the milliseconds of each kernel kind to ms_by_kind[kind]
+ * (kinds 0 .. moloch_gpu_kernel_kinds()-1) and the launch counts to
+ * launches_by_kind (either array may be NULL).  For profiling and the
+ * roofline report; the reference only times the whole run
+ * (nompi/regcm_dynamical_core.F90:30,222-228). */
+int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launches_by_kind, int nkinds);
+int moloch_gpu_kernel_kinds(void);
+const char* moloch_gpu_kernel_name(int kind);
+
+/* deallocate (the reference frees its pool at exit, memory_destroy). */
+int moloch_gpu_destroy(moloch_handle_t* h);
+
+/* Text of the last error raised on the calling thread ("" if none). */
+const char* moloch_gpu_last_error(void);
+
+/* ---- idealized initial state ---------------------------------------------
+ * Host restatement of the reference driver's param() and init()
+ * (nompi/regcm_dynamical_core.F90:93-201, nompi/mod_atmosphere.F90:171-235)
+ * followed by the uploads and moloch_gpu_init(): the call sequence the
+ * Fortran program performs before its time loop.  Additions that the
+ * reference does not have: Gaussian hills in ht, a seeded theta noise
+ * t += a*(2U-1)*pai on the lowest `pert_levels` levels (splitmix64 of the
+ * linear index), and the background wind u0, v0 (reference: 1, 1). */
+typedef struct moloch_ideal {
+  int nhills;
+  double hill_h[4], hill_j[4], hill_i[4], hill_r[4]; /* m, centre (grid points), e-folding radius */
+  double pert_amp;
+  int pert_levels;
+  unsigned long long seed;
+  double u0, v0;
+} moloch_ideal_t;
+
+int moloch_gpu_setup_idealized(moloch_handle_t* h, const moloch_ideal_t* ideal);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MOLOCH_GB300_H */

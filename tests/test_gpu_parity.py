@@ -1,0 +1,180 @@
+"""Parity of the CUDA step against the CPU oracle, through the C ABI.
+
+Tolerances (floating point, FP64):
+  * initial state and static terms: bit-identical (same host code path);
+  * one phase / one step, FP64_EXACT build: relative L2 <= 1e-13 (only the
+    transcendental calls pow/exp differ between CUDA and the host libm);
+  * 100 steps at the reference defaults (100 x 100 x 30): relative L2 <= 1e-9
+    per prognostic field, for the FP64 (contracting) and FP64_EXACT builds;
+  * FP32 storage with FP64 solve: see test_gpu_mixed.py.
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+PROG = ("u", "v", "w", "pai", "t", "qv", "qc")
+DIAG = ("ps", "p", "rho", "qsat", "tvirt", "tetav")
+
+
+def pair(oracle_mod, dm, jx, iy, kz, mode="fp64_exact", hills=(), pert_amp=0.5, pert_levels=10,
+         seed=1234, u0=1.0, v0=1.0, **opts):
+    cfg_opts = {}
+    prm = {}
+    for k, v in opts.items():
+        if k == "divfilter":
+            cfg_opts["divfilter"] = v; prm["mo_divfilter"] = int(v)
+        elif k == "filterpai":
+            cfg_opts["filterpai"] = v; prm["do_filterpai"] = int(v)
+        elif k == "filtertheta":
+            cfg_opts["filtertheta"] = v; prm["do_filtertheta"] = int(v)
+        elif k == "rotllr":
+            cfg_opts["rotllr"] = v; prm["rotllr"] = int(v)
+        else:
+            raise TypeError(k)
+    o = oracle_mod.Oracle(oracle_mod.make_cfg(jx, iy, kz, hills=hills, pert_amp=pert_amp,
+                                              pert_levels=pert_levels, seed=seed, u0=u0, v0=v0, **cfg_opts))
+    g = dm.Moloch(jx, iy, kz, mode=mode, **prm)
+    g.setup_idealized(hills=hills, pert_amp=pert_amp, pert_levels=pert_levels, seed=seed, u0=u0, v0=v0)
+    return o, g
+
+
+def compare(o, g, names, tol):
+    worst = {}
+    for n in names:
+        e = rel_l2(g.get(n), o.get(n))
+        worst[n] = e
+    bad = {n: e for n, e in worst.items() if not e <= tol}
+    assert not bad, f"relative L2 above {tol}: {bad}"
+    return worst
+
+
+def test_initial_state_bit_identical(oracle_mod, gpu_lib):
+    o, g = pair(oracle_mod, gpu_lib, 17, 13, 9, hills=((400.0, 8.0, 6.0, 3.0),))
+    for n in ("u", "v", "w", "pai", "t", "qv", "fmz", "fmzf", "zeta", "hx", "hy"):
+        a, b = g.get(n), o.get(n)
+        assert np.array_equal(a, b), n
+
+
+@pytest.mark.parametrize("jx,iy,kz", [(13, 11, 7), (40, 33, 16)])
+def test_phases_exact(oracle_mod, gpu_lib, jx, iy, kz):
+    """Each phase of one step separately (odd sizes exercise the edge paths)."""
+    o, g = pair(oracle_mod, gpu_lib, jx, iy, kz)
+    o.phase(0); g.phase(0)
+    compare(o, g, ("tetav", "tvirt"), 0.0)
+    compare(o, g, ("p", "qsat"), 1e-15)
+    o.phase(1); g.phase(1)
+    compare(o, g, ("u", "v", "w", "pai", "tetav", "s", "deltaw"), 1e-13)
+    o.phase(2); g.phase(2)
+    compare(o, g, ("u", "v", "w", "pai", "tetav", "qv", "qc"), 1e-13)
+    for _ in range(2):
+        o.phase(1); g.phase(1)
+        o.phase(2); g.phase(2)
+    o.phase(3); g.phase(3)
+    compare(o, g, PROG + DIAG, 1e-13)
+
+
+@pytest.mark.parametrize("mode", ["fp64_exact", "fp64"])
+def test_steps_small(oracle_mod, gpu_lib, mode):
+    o, g = pair(oracle_mod, gpu_lib, 24, 20, 12)
+    for s in range(1, 6):
+        o.step(s)
+        g.moloch(s)
+    compare(o, g, PROG + DIAG, 1e-12)
+
+
+@pytest.mark.parametrize("opts", [
+    dict(divfilter=True),
+    dict(filterpai=True, filtertheta=True),
+    dict(rotllr=False),
+    dict(divfilter=True, filterpai=True, filtertheta=True, rotllr=False),
+])
+def test_options(oracle_mod, gpu_lib, opts):
+    o, g = pair(oracle_mod, gpu_lib, 19, 16, 10, hills=((300.0, 9.0, 8.0, 3.0),), **opts)
+    for s in range(1, 4):
+        o.step(s)
+        g.moloch(s)
+    compare(o, g, PROG + DIAG, 1e-12)
+
+
+def test_hill_and_wind(oracle_mod, gpu_lib):
+    """Gaussian hill (500 m, radius 20 gp as in the 512 x 512 x 60 workload,
+    scaled to the grid) and a 7 m/s background wind."""
+    o, g = pair(oracle_mod, gpu_lib, 48, 40, 20, hills=((500.0, 24.5, 20.5, 6.0),), u0=7.0, v0=-2.0)
+    for s in range(1, 4):
+        o.step(s)
+        g.moloch(s)
+    compare(o, g, PROG + DIAG, 1e-12)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp64_exact"])
+def test_reference_defaults_100_steps(oracle_mod, gpu_lib, mode):
+    """The reference's own defaults (namelist.in: 100 x 100 x 30) with the
+    seeded +-0.5 K theta noise on the lowest 10 levels: 100 steps."""
+    o, g = pair(oracle_mod, gpu_lib, 100, 100, 30, mode=mode)
+    diag_o = diag_g = None
+    for s in range(1, 101):
+        lp = s % 20 == 0
+        bad, diag_o = o.step(s, lp)
+        d = g.moloch(s, lp)
+        if lp:
+            diag_g = d
+            assert bad == 0 and d.status == 0
+    worst = compare(o, g, PROG + DIAG, 1e-9)
+    print(mode, {k: f"{v:.2e}" for k, v in worst.items()})
+    # lprint max/min printout (mod_moloch.F90:396-401)
+    gd = [diag_g.maxps, diag_g.minps, diag_g.maxu, diag_g.minu, diag_g.maxv, diag_g.minv]
+    assert np.allclose(gd, diag_o, rtol=1e-9, atol=0)
+
+
+def test_graph_replay_matches_stepwise(gpu_lib):
+    a = gpu_lib.Moloch(32, 24, 12)
+    b = gpu_lib.Moloch(32, 24, 12)
+    a.setup_idealized()
+    b.setup_idealized()
+    for s in range(4):
+        a.moloch(s + 1)
+    b.run(4, graph=True)
+    b.sync()
+    for n in PROG + DIAG:
+        assert np.array_equal(a.get(n), b.get(n)), n
+    assert b.kernel_count > 0
+
+
+def test_cfl_violation_is_reported(gpu_lib):
+    """A non-finite state is reported like the reference's fatal('CFL VIOLATION')."""
+    g = gpu_lib.Moloch(16, 12, 8)
+    g.setup_idealized()
+    t = g.download("t")
+    t[5, 5, 3] = np.nan
+    g.upload("t", t)
+    g.moloch(1)
+    with pytest.raises(gpu_lib.MolochError) as ei:
+        g.moloch(2, lprint=True)
+    assert ei.value.code == 4
+
+
+def test_upload_download_roundtrip_and_bounds(gpu_lib):
+    g = gpu_lib.Moloch(12, 10, 6)
+    g.setup_idealized()
+    rng = np.random.default_rng(0)
+    for name in ("u", "v", "w", "pai", "t", "qv", "qc", "qi", "qr", "qs"):
+        a = g.download(name)
+        interior = rng.standard_normal(g.get(name).shape)
+        b = a.copy()
+        (l1, _), (l2, _) = gpu_lib.field_bounds(name, 12, 10, 6)[:2]
+        b[1 - l1:1 - l1 + 12, 1 - l2:1 - l2 + 10, :] = interior.transpose(2, 1, 0)
+        g.upload(name, b)
+        assert np.array_equal(g.get(name), interior)
+        full = g.download(name)
+        # halo positions hold periodic images of the interior
+        assert np.array_equal(full[0 - l1], full[12 - l1]) if l1 <= 0 else True
+    import ctypes
+    L = gpu_lib.lib()
+    lb = (ctypes.c_int * 3)(0, 0, 1)
+    ub = (ctypes.c_int * 3)(13, 11, 6)
+    buf = np.zeros(14 * 12 * 6)
+    rc = L.moloch_gpu_upload(g.h, gpu_lib.FIELD["u"], buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), lb, ub)
+    assert rc == 2  # u has bounds (-1:nj+2, 0:ni+1, 1:kz)
