@@ -88,6 +88,8 @@ _PROTOS = {
                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_kernel_kinds": (ctypes.c_int, []),
     "moloch_gpu_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
+                                  [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
 }
 
 _lib = None
@@ -237,6 +239,10 @@ class Moloch:
         _check(self.L.moloch_gpu_download(self.h, FIELD[name], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                           lb, ub))
         return a
+
+    def get_1d(self, name):
+        """A 1-D level table (zita, zitah) as uploaded."""
+        return np.array(self.download(name))
 
     def get(self, name):
         """Interior of a field as (nk, iy, jx) float64 (or (iy, jx) for 2-D)."""

@@ -496,6 +496,9 @@ extern "C" {
 
 const char* moloch_gpu_last_error(void) { return g_err.c_str(); }
 
+// error text from the other translation units of the library
+void moloch_internal_set_error(const char* msg) { g_err = msg ? msg : ""; }
+
 void moloch_gpu_default_params(moloch_params_t* p) {
   if (!p) return;
   std::memset(p, 0, sizeof *p);

@@ -172,6 +172,30 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 int moloch_gpu_kernel_kinds(void);
 const char* moloch_gpu_kernel_name(int kind);
 
+/* WAF advection of ONE field by dt_adv seconds (the arithmetic of wafone,
+ * nompi/mod_moloch.F90:929-1311) that allocates no device memory.  It has
+ * no counterpart in the reference: it exists for callers that own all
+ * device memory themselves -- a Fortran model keeping its arrays in its own
+ * CUDA/OpenACC data regions, or a framework with its own memory pool -- and
+ * cannot let a library call cudaMalloc, which may synchronise the device,
+ * grow past the caller's pool, or fail once the caller has reserved the
+ * GPU's memory.  The caller passes device pointers in this library's dense
+ * layout (j fastest, then i, then k; s and fmzf have kz+1 levels; msfu,
+ * msfv, msfx are jx*iy periodic arrays) and pp is advected in place.
+ * The two work arrays live in one fixed __device__ array of 32 MiB that
+ * every GPU loading the library keeps until exit, so jx*iy*kz may not
+ * exceed 2097152 (2^21) points; larger sizes return MOLOCH_ERR_ARG.
+ * The first call on a device looks that array's address up once
+ * (cudaGetSymbolAddress with the device current): make the first call on
+ * each device before any stream capture.  All calls share the array, so
+ * calls that overlap on the GPU (other streams, other threads) race; each
+ * call overwrites the work arrays completely before reading them.  No
+ * cudaMalloc, cudaFree or allocating library routine is called. */
+int moloch_gpu_wafone_noalloc(double* pp, const double* s, const double* u, const double* v,
+                              const double* fmz, const double* fmzf, const double* msfu,
+                              const double* msfv, const double* msfx, int jx, int iy, int kz,
+                              double dt_adv, double dx, double dzita, int rotllr, void* stream);
+
 /* deallocate (the reference frees its pool at exit, memory_destroy). */
 int moloch_gpu_destroy(moloch_handle_t* h);
 
