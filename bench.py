@@ -45,13 +45,13 @@ SEED = 1234
 # not counted; their traffic shows up as measured traffic above algorithmic.
 ALG_WORDS = {
     "k_prediag": 13,          # r: pai t q(5) | w: p qsat tvirt qwltot qwitot tetav
-    "k_sound_div": 7,         # r: u v fmz rfw rfs | w: s zdiv2
-    "k_sound_column": 21,     # r: zdiv2 u v s fmz w fmzf tetav qv qsat pai t qc qwltot qwitot | w: u v w deltaw tetav pai
+    "k_sound_div": 7,         # r: u v fmz rfw rfs | w: s zdiv2a
+    "k_sound_damp": 8,        # r: zdiv2a u v fmz s | w: u v zdiv2b
+    "k_sound_column": 16,     # r: w fmzf qv tetav pai qsat t zdiv2b fmz qc qwltot qwitot | w: w deltaw tetav pai
     "k_sound_momentum": 7,    # r: u v deltaw tetav pai | w: u v
     "k_stag_to_x": 6,         # r: u v w | w: ux vx wx
     "k_waf_vertical": 23,     # r: 10 fields s wafu wafd | w: 10 wz
-    "k_waf_meridional": 33,   # r: 10 wz 10 pp v wafn wafs | w: 10 p0
-    "k_waf_zonal": 33,        # r: 10 p0 10 pp u wafe wafw | w: 10 pp
+    "k_waf_horizontal": 36,   # r: 10 wz 10 pp u v wafn wafs wafe wafw | w: 10 pp
     "k_stag_from_x": 6,       # r: ux vx wx | w: u v w
     "k_postdiag": 12,         # r: pai tetav q(5) | w: tvirt t p rho qsat
 }

@@ -152,8 +152,10 @@ struct moloch_handle {
   bool initialized = false;
   long long kernels = 0;
   int kernels_per_step = 0;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t gexec = nullptr;
+  // one graph per field-buffer parity at the start of a step (advection
+  // swaps the two buffer sets, so odd mo_nadv alternates between them)
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   double* hres = nullptr;  // pinned diag result
   void* stage = nullptr;   // pinned staging buffer, one 3-D field (kz+1 levels) of doubles
   size_t stage_bytes = 0;
@@ -194,16 +196,17 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   auto T2 = [&]() { return (T*)take(sizeof(T) * pl); };
   auto T1 = [&](size_t n) { return (T*)take(sizeof(T) * n); };
   v.ubuf[0] = T3(); v.ubuf[1] = T3(); v.vbuf[0] = T3(); v.vbuf[1] = T3();
-  v.w = T3p(); v.pai = T3(); v.tetav = T3(); v.t = T3();
-  for (int n = 0; n < 5; ++n) v.q[n] = T3();
+  v.w = T3p(); v.t = T3();
+  for (int set = 0; set < 2; ++set)
+    for (int n = 0; n < kNumAdvected; ++n) v.fset[set][n] = T3();
+  v.fcur = 0;
+  v.bind_fields();
   v.p = T3(); v.qsat = T3(); v.tvirt = T3(); v.rho = T3(); v.ps = T2();
   v.qwltot = T3(); v.qwitot = T3();
   v.s = T3p(); v.deltaw = T3p(); v.zdiv2a = T3(); v.zdiv2b = T3();
   v.wp = (double*)take(sizeof(double) * n3p);
   v.wwkw = (double*)take(sizeof(double) * n3p);
-  v.ux = T3(); v.vx = T3(); v.wx = T3();
   v.wz = (T*)take(sizeof(T) * n3 * kNumAdvected);
-  v.p0 = (T*)take(sizeof(T) * n3 * kNumAdvected);
   const bool filt = h->prm.do_filterpai || h->prm.do_filtertheta;
   v.pf = h->prm.do_filterpai ? T3() : nullptr;
   v.tf = h->prm.do_filtertheta ? T3() : nullptr;
@@ -633,8 +636,10 @@ int moloch_gpu_init(moloch_handle_t* h) {
     if (!(h->uploaded & (1u << f))) return fail(MOLOCH_ERR_STATE, "init before field %d was uploaded", f);
   int rc = h->elem == 8 ? init_impl(h, h->vd) : init_impl(h, h->vf);
   if (rc) return rc;
-  if (h->gexec) { cudaGraphExecDestroy(h->gexec); h->gexec = nullptr; }
-  if (h->graph) { cudaGraphDestroy(h->graph); h->graph = nullptr; }
+  for (int q = 0; q < 2; ++q) {
+    if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
+    if (h->graph[q]) { cudaGraphDestroy(h->graph[q]); h->graph[q] = nullptr; }
+  }
   h->initialized = true;
   return MOLOCH_OK;
 }
@@ -668,19 +673,36 @@ int moloch_gpu_run(moloch_handle_t* h, int nsteps, int use_graph) {
     }
     return MOLOCH_OK;
   }
-  if (!h->gexec) {
-    CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
-    int n = step_kernels(h);
-    cudaGraph_t g = nullptr;
-    cudaError_t e = cudaStreamEndCapture(h->stream, &g);
-    if (e != cudaSuccess) return fail(MOLOCH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-    h->graph = g;
-    CUDA_TRY(cudaGraphInstantiate(&h->gexec, h->graph, 0));
-    h->kernels_per_step = n;
-  }
-  for (int s = 0; s < nsteps; ++s) {
-    CUDA_TRY(cudaGraphLaunch(h->gexec, h->stream));
+  for (int st = 0; st < nsteps; ++st) {
+    const int par = h->elem == 8 ? h->vd.fcur : h->vf.fcur;
+    const int cur = h->elem == 8 ? h->vd.cur : h->vf.cur;
+    if (cur != 0) {  // after a lone sound() phase the u/v pair is swapped: no graph for this step
+      h->kernels += step_kernels(h);
+      int rc = check_launch("run");
+      if (rc) return rc;
+      continue;
+    }
+    if (!h->gexec[par]) {
+      // capture advances the host-side buffer bookkeeping like a real step;
+      // it is restored below so the replay starts from the same state
+      View<double> vd0 = h->vd;
+      View<float> vf0 = h->vf;
+      CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+      int n = step_kernels(h);
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamEndCapture(h->stream, &g);
+      h->vd = vd0;
+      h->vf = vf0;
+      if (e != cudaSuccess) return fail(MOLOCH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+      h->graph[par] = g;
+      CUDA_TRY(cudaGraphInstantiate(&h->gexec[par], h->graph[par], 0));
+      h->kernels_per_step = n;
+    }
+    CUDA_TRY(cudaGraphLaunch(h->gexec[par], h->stream));
     h->kernels += h->kernels_per_step;
+    // the same bookkeeping the captured step performed
+    if (h->elem == 8) { h->vd.fcur ^= (h->prm.mo_nadv & 1); h->vd.bind_fields(); h->vd.cur = 0; }
+    else { h->vf.fcur ^= (h->prm.mo_nadv & 1); h->vf.bind_fields(); h->vf.cur = 0; }
   }
   return check_launch("graph replay");
 }
@@ -749,8 +771,8 @@ void* moloch_gpu_stream(moloch_handle_t* h) { return h ? (void*)h->stream : null
 long long moloch_gpu_kernel_count(moloch_handle_t* h) { return h ? h->kernels : -1; }
 
 static const char* const kKindNames[KK_COUNT] = {
-    "k_prediag", "k_sound_div", "k_sound_column", "k_lap_filter", "k_pai_update", "k_sound_momentum",
-    "k_stag_to_x", "k_waf_vertical", "k_waf_meridional", "k_waf_zonal", "k_stag_from_x",
+    "k_prediag", "k_sound_div", "k_sound_damp", "k_sound_column", "k_lap_filter", "k_pai_update",
+    "k_sound_momentum", "k_stag_to_x", "k_waf_vertical", "k_waf_horizontal", "k_stag_from_x",
     "k_filter_increment", "k_postdiag", "k_diag"};
 
 int moloch_gpu_kernel_kinds(void) { return KK_COUNT; }
@@ -803,8 +825,10 @@ int moloch_internal_describe(moloch_handle_t* h, moloch_grid_t* g, moloch_params
 int moloch_gpu_destroy(moloch_handle_t* h) {
   if (!h) return MOLOCH_OK;
   cudaStreamSynchronize(h->stream);
-  if (h->gexec) cudaGraphExecDestroy(h->gexec);
-  if (h->graph) cudaGraphDestroy(h->graph);
+  for (int q = 0; q < 2; ++q) {
+    if (h->gexec[q]) cudaGraphExecDestroy(h->gexec[q]);
+    if (h->graph[q]) cudaGraphDestroy(h->graph[q]);
+  }
   if (h->arena) cudaFree(h->arena);
   if (h->hres) cudaFreeHost(h->hres);
   if (h->stage) cudaFreeHost(h->stage);

@@ -7,16 +7,15 @@
 // Kernel map (reference: nompi/mod_moloch.F90):
 //   k_prediag          :289-323  p, qsat, tvirt, qwltot, qwitot, tetav
 //   k_sound_div        :514-597  u/v halo + surface w + s (Eq. 10) + zdiv2 (Eq. 16)
-//   k_sound_column     :853-895 + :627-728  divdamp, vertical s term, implicit w
-//                      (Thomas, one thread per column), Exner/theta update,
-//                      nompi pai halo order, s completion (:843-849)
+//   k_sound_damp       :853-895 + :627-630  divdamp and the vertical s term
+//   k_sound_column     :634-728  implicit w (Thomas, one thread per column),
+//                      Exner/theta update, nompi pai halo order, s completion (:843-849)
 //   k_lap_filter       :423-440 divergence_filter (mo_divfilter)
 //   k_pai_update       :716-728 (split form used when the filter is on)
 //   k_sound_momentum   :730-837  Equations 17, 18
 //   k_stag_to_x        :1327-1341, :1389-1417  (u,v,w) -> (ux,vx,wx)
-//   k_waf_vertical     :966-1073  two vertical WAF passes, all 10 fields
-//   k_waf_meridional   :1075-1136 meridional WAF flux + update -> p0
-//   k_waf_zonal        :1138-1187 zonal WAF flux + update -> pp
+//   k_waf_vertical     :966-1073  both vertical WAF passes in registers, all 10 fields
+//   k_waf_horizontal   :1075-1187 meridional + zonal WAF of one level, p0 in shared memory
 //   k_stag_from_x      :1343-1387  (ux,vx,wx) -> (u,v,w)
 //   k_filter_increment :442-481 + :333-353 filtpai / filttheta
 //   k_postdiag         :355-391  tvirt, t, p, rho, ps, qsat
@@ -39,7 +38,6 @@ constexpr int kColBX = 32;  // column kernels: 32 j x 4 i threads
 constexpr int kColBY = 4;
 constexpr int kPtBX = 32;   // point kernels: 32 j x 8 i threads
 constexpr int kPtBY = 8;
-constexpr int kTileBI = 8;  // WAF tile rows
 
 template <class T>
 struct FieldPtrs {
@@ -69,6 +67,13 @@ template <class T> __device__ __forceinline__ T fmin2(T a, T b) { return a < b ?
 template <class T> __device__ __forceinline__ T superbee(T r) {
   return fmax2(T(0), fmin2(T(2), fmax2(r, fmin2(T(2) * r, T(1)))));
 }
+// Quotient of the WAF limiter ratio.  FP64 builds: the IEEE quotient, as
+// the reference.  FP32 storage: the fast approximate quotient (2 ulp); the
+// ratio only selects and scales the limiter, and the FP32 error is measured
+// against the FP64 step anyway.
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
+
 // sign(max(abs(z), minden), z)   (:992)
 template <class T> __device__ __forceinline__ T safeden(T z) {
   return dcopysign(fmax2(dabs(z), T(kMinden)), z);
@@ -116,137 +121,166 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_prediag(View<T> d, int filterp
 }
 
 // ---- sound: halo, surface w, s (Eq. 10), horizontal divergence (Eq. 16) ---
-// One thread per column.  Writes the pre-divdamp u/v edge values that the
-// momentum step later reads as the stale ud/vd halo ring (:730-735).
+// One thread per point.  Boundary threads also store the pre-divdamp u/v
+// edge values that the momentum step reads as the stale ud/vd halo ring
+// (:730-735); the bottom level computes w(kz+1) and s(kz+1) (:536-549).
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY) k_sound_div(View<T> d) {
-  int jj = blockIdx.x * kColBX + threadIdx.x;
-  int ii = blockIdx.y * kColBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz, pl = d.pl;
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_div(View<T> d) {
+  const int jj = blockIdx.x * kPtBX + threadIdx.x;
+  const int ii = blockIdx.y * kPtBY + threadIdx.y;
+  const int kk = blockIdx.z;
+  const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
+  const size_t pl = d.pl;
   const int jp = wp1(jj, nj), ip = wp1(ii, ni);
   const T* __restrict__ u = d.ubuf[d.cur];
   const T* __restrict__ v = d.vbuf[d.cur];
   const size_t c = (size_t)jj + (size_t)nj * ii;
   const size_t ce = (size_t)jp + (size_t)nj * ii;  // (j+1, i)
   const size_t cn = (size_t)jj + (size_t)nj * ip;  // (j, i+1)
+  const size_t o = (size_t)kk * pl;
+  const T u0 = u[c + o], u1 = u[ce + o], v0 = v[c + o], v1 = v[cn + o];
   const T hx0 = d.hx[c], hx1 = d.hx[ce], hy0 = d.hy[c], hy1 = d.hy[cn];
-  const T mxv = d.rotllr ? d.mx[c] : d.mx2[c];
-  const T rmv0 = d.rmv[c], rmv1 = d.rmv[cn];
-  const T rmu0 = d.rmu[c], rmu1 = d.rmu[ce];
-  const T dtrdx = d.dtrdx, dtrdy = d.dtrdy;
-  T u0p = T(0), u1p = T(0), v0p = T(0), v1p = T(0);
-  for (int kk = 0; kk < kz; ++kk) {
-    const size_t o = (size_t)kk * pl;
-    const T u0 = u[c + o], u1 = u[ce + o], v0 = v[c + o], v1 = v[cn + o];
-    if (kk > 0) {  // s(k), k = 2..kz  (:557-570)
-      T zuh = (u0 + u0p) * hx0 + (u1 + u1p) * hx1;
-      T zvh = (v0 + v0p) * hy0 + (v1 + v1p) * hy1;
-      d.s[c + o] = -((T(0.25) * (zuh + zvh)) * d.gzitak[kk]);
-    }
-    const T f = d.fmz[c + o];
-    const T zrfmzum = d.rfw[c + o], zrfmzup = d.rfw[ce + o];
-    const T zrfmzvm = d.rfs[c + o], zrfmzvp = d.rfs[cn + o];
-    T zum, zup, zvm, zvp;
-    if (d.rotllr) {
-      zum = (dtrdx * u0) * zrfmzum;
-      zup = (dtrdx * u1) * zrfmzup;
-      zvm = ((dtrdy * v0) * zrfmzvm) * rmv0;
-      zvp = ((dtrdy * v1) * zrfmzvp) * rmv1;
-      d.zdiv2a[c + o] = (f * mxv) * ((zup - zum) + (zvp - zvm));
-    } else {
-      zum = ((dtrdx * u0) * rmu0) * zrfmzum;
-      zup = ((dtrdx * u1) * rmu1) * zrfmzup;
-      zvm = ((dtrdy * v0) * rmv0) * zrfmzvm;
-      zvp = ((dtrdy * v1) * rmv1) * zrfmzvp;
-      d.zdiv2a[c + o] = (mxv * f) * ((zup - zum) + (zvp - zvm));
-    }
-    // stale-halo edges (values before divdamp)
-    if (jj == 0) d.eu_j[ii + (size_t)ni * kk] = u0;
-    if (ii == ni - 1) d.eu_i[jj + (size_t)nj * kk] = u0;
-    if (jj == nj - 1) d.ev_j[ii + (size_t)ni * kk] = v0;
-    if (ii == 0) d.ev_i[jj + (size_t)nj * kk] = v0;
-    u0p = u0; u1p = u1; v0p = v0; v1p = v1;
+  if (kk > 0) {  // s(k), k = 2..kz  (:557-570)
+    const T u0p = u[c + o - pl], u1p = u[ce + o - pl], v0p = v[c + o - pl], v1p = v[cn + o - pl];
+    T zuh = (u0 + u0p) * hx0 + (u1 + u1p) * hx1;
+    T zvh = (v0 + v0p) * hy0 + (v1 + v1p) * hy1;
+    d.s[c + o] = -((T(0.25) * (zuh + zvh)) * d.gzitak[kk]);
   }
-  // surface w(kz+1), s(kz+1)  (:536-549); u0p.. hold level kz
-  T zuh = u0p * hx0 + u1p * hx1;
-  T zvh = v0p * hy0 + v1p * hy1;
-  T ws = T(0.5) * (zuh + zvh);
-  d.w[c + (size_t)kz * pl] = ws;
-  d.s[c + (size_t)kz * pl] = -ws;
+  const T dtrdx = d.dtrdx, dtrdy = d.dtrdy;
+  const T f = d.fmz[c + o];
+  const T zrfmzum = d.rfw[c + o], zrfmzup = d.rfw[ce + o];
+  const T zrfmzvm = d.rfs[c + o], zrfmzvp = d.rfs[cn + o];
+  const T rmv0 = d.rmv[c], rmv1 = d.rmv[cn];
+  if (d.rotllr) {
+    const T zum = (dtrdx * u0) * zrfmzum;
+    const T zup = (dtrdx * u1) * zrfmzup;
+    const T zvm = ((dtrdy * v0) * zrfmzvm) * rmv0;
+    const T zvp = ((dtrdy * v1) * zrfmzvp) * rmv1;
+    d.zdiv2a[c + o] = (f * d.mx[c]) * ((zup - zum) + (zvp - zvm));
+  } else {
+    const T rmu0 = d.rmu[c], rmu1 = d.rmu[ce];
+    const T zum = ((dtrdx * u0) * rmu0) * zrfmzum;
+    const T zup = ((dtrdx * u1) * rmu1) * zrfmzup;
+    const T zvm = ((dtrdy * v0) * rmv0) * zrfmzvm;
+    const T zvp = ((dtrdy * v1) * rmv1) * zrfmzvp;
+    d.zdiv2a[c + o] = (d.mx2[c] * f) * ((zup - zum) + (zvp - zvm));
+  }
+  if (jj == 0) d.eu_j[ii + (size_t)ni * kk] = u0;
+  if (ii == ni - 1) d.eu_i[jj + (size_t)nj * kk] = u0;
+  if (jj == nj - 1) d.ev_j[ii + (size_t)ni * kk] = v0;
+  if (ii == 0) d.ev_i[jj + (size_t)nj * kk] = v0;
+  if (kk == kz - 1) {  // surface w(kz+1), s(kz+1)
+    T zuh = u0 * hx0 + u1 * hx1;
+    T zvh = v0 * hy0 + v1 * hy1;
+    T ws = T(0.5) * (zuh + zvh);
+    d.w[c + (size_t)kz * pl] = ws;
+    d.s[c + (size_t)kz * pl] = -ws;
+  }
 }
 
-// ---- sound: divdamp + implicit w + Exner/theta (one thread per column) ----
-// defer_pai: store the final divergence in zdiv2b and leave pai to
-// k_pai_update (used when the divergence filter runs in between).
+// ---- sound: divdamp (:853-895) and the vertical s term (:627-630) -------
+// One thread per point: damps u and v in place (their halo edges already
+// hold the pre-damping values) and writes the divergence the implicit
+// solve starts from into zdiv2b.
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY)
-    k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
-  int jj = blockIdx.x * kColBX + threadIdx.x;
-  int ii = blockIdx.y * kColBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz, pl = d.pl;
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_damp(View<T> d) {
+  const int jj = blockIdx.x * kPtBX + threadIdx.x;
+  const int ii = blockIdx.y * kPtBY + threadIdx.y;
+  const int kk = blockIdx.z;
+  const int nj = d.nj, ni = d.ni;
   if (jj >= nj || ii >= ni) return;
-  const int jm = wm1(jj, nj), jp = wp1(jj, nj), im = wm1(ii, ni), ip = wp1(ii, ni);
+  const size_t pl = d.pl;
+  const size_t o = (size_t)kk * pl;
+  const size_t c = (size_t)jj + (size_t)nj * ii;
   T* __restrict__ u = d.ubuf[d.cur];
   T* __restrict__ v = d.vbuf[d.cur];
+  const T zc = d.zdiv2a[c + o];
+  const T zw = d.zdiv2a[o + wm1(jj, nj) + (size_t)nj * ii];
+  const T ze = d.zdiv2a[o + wp1(jj, nj) + (size_t)nj * ii];
+  const T zs = d.zdiv2a[o + jj + (size_t)nj * wm1(ii, ni)];
+  const T zn = d.zdiv2a[o + jj + (size_t)nj * wp1(ii, ni)];
+  const T cd = d.cdamp[kk];
+  u[c + o] = u[c + o] + ((cd * d.mu[c]) * (zc - zw));
+  if (d.rotllr)
+    v[c + o] = v[c + o] + cd * (zc - zs);
+  else
+    v[c + o] = v[c + o] + ((cd * d.mv[c]) * (zc - zs));
+  const T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
+  T zd = zc + d.ddamp2 * p2d;
+  zd = zd + (d.fmz[c + o] * d.dtrdz) * (d.s[c + o] - d.s[c + o + pl]);
+  d.zdiv2b[c + o] = zd;
+}
+
+// Reciprocal of a Thomas pivot.  FP64 build: the IEEE quotient, as the
+// reference.  FP32-storage build: an FP32 estimate refined by one FP64
+// Newton step (relative error ~1e-14) -- the pivot stays FP64 while the
+// FP64 pipe, 1/64 of the FP32 rate on GB300, does 2 FMAs instead of a
+// full division.
+template <class T> __device__ __forceinline__ double pivot_rcp(double den);
+template <> __device__ __forceinline__ double pivot_rcp<double>(double den) { return 1.0 / den; }
+template <> __device__ __forceinline__ double pivot_rcp<float>(double den) {
+  float x = (float)den, r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  double r0 = (double)r;
+  double e = fma(-den, r0, 1.0);
+  return fma(r0, e, r0);
+}
+
+// ---- sound: implicit w (Thomas, :634-686) + Exner/theta (:690-728) -----
+// One thread per column.  Down-sweep k = kz..2 with FP64 pivots in every
+// mode, stash of the FP64 down-sweep values, then back-substitution fused
+// with the Exner/theta/pai update of the level above it.
+// defer_pai: leave zdiv2b final and pai to k_pai_update (divergence filter on).
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 5)
+    k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
+  const int jj = blockIdx.x * kColBX + threadIdx.x;
+  const int ii = blockIdx.y * kColBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni, kz = d.kz;
+  if (jj >= nj || ii >= ni) return;
+  const size_t pl = d.pl;
   const size_t c = (size_t)jj + (size_t)nj * ii;
-  const size_t cw = (size_t)jm + (size_t)nj * ii, ce = (size_t)jp + (size_t)nj * ii;
-  const size_t cs = (size_t)jj + (size_t)nj * im, cn = (size_t)jj + (size_t)nj * ip;
-  const T mu = d.mu[c], mv = d.mv[c];
-  const T ddamp2 = d.ddamp2, dtrdz = d.dtrdz;
-
-  // (a) divdamp (:853-895) and the vertical s contribution (:627-630)
-  for (int kk = 0; kk < kz; ++kk) {
-    const size_t o = (size_t)kk * pl;
-    const T zc = d.zdiv2a[c + o], zw = d.zdiv2a[cw + o], ze = d.zdiv2a[ce + o];
-    const T zs = d.zdiv2a[cs + o], zn = d.zdiv2a[cn + o];
-    const T cd = d.cdamp[kk];
-    u[c + o] = u[c + o] + ((cd * mu) * (zc - zw));
-    if (d.rotllr)
-      v[c + o] = v[c + o] + cd * (zc - zs);
-    else
-      v[c + o] = v[c + o] + ((cd * mv) * (zc - zs));
-    T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
-    T zd = zc + ddamp2 * p2d;
-    zd = zd + (d.fmz[c + o] * dtrdz) * (d.s[c + o] - d.s[c + o + pl]);
-    d.zdiv2b[c + o] = zd;
-  }
-
-  // (b) Thomas down-sweep, k = kz .. 2  (:634-678); pivots in FP64
   const T ns = T(nsound), ns1 = T(nsound - 1);
-  const T zcs2 = d.zcs2, dts = d.dts, egdts = d.egdts;
-  double wkp1 = (double)d.w[c + (size_t)kz * pl];  // w(kz+1) from k_sound_div
-  const T wsurf = d.w[c + (size_t)kz * pl];
-  double wwp1 = 0.0;                                // wwkw(kz+1) = 0
-  T zd_k = d.zdiv2b[c + (size_t)(kz - 1) * pl];
-  T tk = d.tetav[c + (size_t)(kz - 1) * pl];
-  T pk = d.pai[c + (size_t)(kz - 1) * pl];
-  T fk = d.fmz[c + (size_t)(kz - 1) * pl];
-  T qsk = d.qsat[c + (size_t)(kz - 1) * pl];
+  const T zcs2 = d.zcs2, dts = d.dts, egdts = d.egdts, dtrdz = d.dtrdz;
+
+  // (b) down-sweep
+  const T wsurf = d.w[c + (size_t)kz * pl];  // w(kz+1) from k_sound_div
+  double wkp1 = (double)wsurf;
+  double wwp1 = 0.0;  // wwkw(kz+1) = 0
+  size_t o = (size_t)(kz - 1) * pl;
+  T zd_k = d.zdiv2b[c + o];
+  T tk = d.tetav[c + o];
+  T pk = d.pai[c + o];
+  T fk = d.fmz[c + o];
+  T qsk = d.qsat[c + o];
+#pragma unroll 2
   for (int kk = kz - 1; kk >= 1; --kk) {
-    const size_t o = (size_t)kk * pl, om = (size_t)(kk - 1) * pl;
+    o = (size_t)kk * pl;
+    const size_t om = o - pl;
     const T wk = d.w[c + o];
     const T fz = d.fmzf[c + o];
+    const T qvk = d.q[0][c + o];
     const T tkm = d.tetav[c + om];
-    T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
-    zrom1w = zrom1w - (((((T(kCpd) * wk) * fz) * fz) * ns) * dtrdz) * (tkm - tk);
     const T pkm = d.pai[c + om];
     const T qskm = d.qsat[c + om];
-    if (d.q[0][c + o] > T(0.96) * qsk && wk > T(0.1)) {
-      T zqs = T(0.5) * (qsk + qskm);
-      T tm = d.t[c + om];
-      T zdth = ((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs) /
-               ((((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
-      zrom1w = zrom1w + zdth * fz;
-    }
     const T zd_km = d.zdiv2b[c + om];
-    T zwexpl = (wk - (zrom1w * dtrdz) * (pkm - pk)) - egdts;
-    zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * (pkm * zd_km - pk * zd_k);
     const T fkm = d.fmz[c + om];
     const T ff = d.ffilt[kk];
+    T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
+    zrom1w = zrom1w - (((((T(kCpd) * wk) * fz) * fz) * ns) * dtrdz) * (tkm - tk);
+    if (qvk > T(0.96) * qsk && wk > T(0.1)) {
+      const T zqs = T(0.5) * (qsk + qskm);
+      const T tm = d.t[c + om];
+      const T zdth = ((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs) /
+                     ((((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
+      zrom1w = zrom1w + zdth * fz;
+    }
+    T zwexpl = (wk - (zrom1w * dtrdz) * (pkm - pk)) - egdts;
+    zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * (pkm * zd_km - pk * zd_k);
     const double zu = (double)(((zcs2 * fkm) * zrom1w) * pkm + ff);
     const double zdd = (double)(((zcs2 * fk) * zrom1w) * pk + ff);
-    const double zrapp = 1.0 / (((1.0 + zdd) + zu) - zdd * wwp1);
+    const double zrapp = pivot_rcp<T>(((1.0 + zdd) + zu) - zdd * wwp1);
     const double wpk = zrapp * ((double)zwexpl + zdd * wkp1);
     const double wwk = zrapp * zu;
     d.wp[c + o] = wpk;
@@ -258,45 +292,44 @@ __global__ void __launch_bounds__(kColBX* kColBY)
   // (c) back-substitution (:681-686) fused with the Exner/theta update of
   // the level above (:690-728); w(1) = 0 always (init_moloch :260-262)
   const T rdrcv = T(kRdrcv);
-  T wlo = T(0);  // w(k-1) at the time level k is solved
   auto finalize = [&](int kk, T wl, T wh) {
-    const size_t o = (size_t)kk * pl;
-    T zd = d.zdiv2b[c + o];
-    zd = zd + (dtrdz * d.fmz[c + o]) * (wl - wh);
-    const T qv = d.q[0][c + o], qc = d.q[1][c + o];
+    const size_t q = c + (size_t)kk * pl;
+    T zd = d.zdiv2b[q];
+    zd = zd + (dtrdz * d.fmz[q]) * (wl - wh);
+    const T qv = d.q[0][q], qc = d.q[1][q];
     zd = (zd * ((T(1) + T(0.86) * qv) + T(3.2) * qc)) / ((T(1) + T(0.96) * qv) + T(4.8) * qc);
-    d.tetav[c + o] =
-        d.tetav[c + o] * (T(1) + (rdrcv * zd) * ((T(0.25) * qv + T(4.2) * d.qwltot[c + o]) +
-                                                 T(2.1) * d.qwitot[c + o]));
+    d.tetav[q] = d.tetav[q] * (T(1) + (rdrcv * zd) * ((T(0.25) * qv + T(4.2) * d.qwltot[q]) + T(2.1) * d.qwitot[q]));
     if (defer_pai) {
-      d.zdiv2b[c + o] = zd;
+      d.zdiv2b[q] = zd;
     } else {
-      const T pold = d.pai[c + o];
+      const T pold = d.pai[q];
       if (jj == nj - 1) d.ep_j[ii + (size_t)ni * kk] = pold;
       if (ii == ni - 1) d.ep_i[jj + (size_t)nj * kk] = pold;
-      d.pai[c + o] = pold * (T(1) - rdrcv * zd);
+      d.pai[q] = pold * (T(1) - rdrcv * zd);
     }
     if (last) {  // complete Equation 10 (:843-849)
       if (kk == 0)
-        d.s[c + o] = T(0);
+        d.s[q] = T(0);
       else
-        d.s[c + o] = (wl + d.s[c + o]) * d.fmzf[c + o];
+        d.s[q] = (wl + d.s[q]) * d.fmzf[q];
     }
   };
+  double wlo_d = 0.0;
+  T wlo = T(0);
+#pragma unroll 2
   for (int kk = 1; kk < kz; ++kk) {
-    const size_t o = (size_t)kk * pl;
-    const double wn_d = d.wp[c + o] + d.wwkw[c + o] * (double)wlo;
-    const T wn = (T)wn_d;
-    const T wold = d.w[c + o];
-    d.deltaw[c + o] = (-wold) + wn;
-    d.w[c + o] = wn;
+    const size_t q = c + (size_t)kk * pl;
+    wlo_d = d.wp[q] + d.wwkw[q] * wlo_d;
+    const T wn = (T)wlo_d;
+    const T wold = d.w[q];
+    d.deltaw[q] = (-wold) + wn;
+    d.w[q] = wn;
     finalize(kk - 1, wlo, wn);
     wlo = wn;
   }
   finalize(kz - 1, wlo, wsurf);
   if (last) d.s[c + (size_t)kz * pl] = T(0);
 }
-
 // ---- 5-point Laplacian filter of one field, out of place ----------------
 // out = a + coef(k) * (0.125*(aW+aE+aS+aN) - 0.5*a)   (:423-481)
 // coef(k) = anu2 * xknu(k) when use_xknu, else the constant c0.
@@ -353,12 +386,16 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
 }
 
 // ---- sound: momentum, Equations 17 and 18 (:737-837) --------------------
+// One thread per point; reads u, v (current buffer, damped interior + the
+// pre-damping edges) and writes the other buffer of the pair.
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY) k_sound_momentum(View<T> d) {
-  int jj = blockIdx.x * kColBX + threadIdx.x;
-  int ii = blockIdx.y * kColBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz, pl = d.pl;
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_momentum(View<T> d) {
+  const int jj = blockIdx.x * kPtBX + threadIdx.x;
+  const int ii = blockIdx.y * kPtBY + threadIdx.y;
+  const int kk = blockIdx.z;
+  const int nj = d.nj, ni = d.ni;
   if (jj >= nj || ii >= ni) return;
+  const size_t pl = d.pl;
   const int jm = wm1(jj, nj), jp = wp1(jj, nj), im = wm1(ii, ni), ip = wp1(ii, ni);
   const T* __restrict__ u = d.ubuf[d.cur];
   const T* __restrict__ v = d.vbuf[d.cur];
@@ -368,50 +405,40 @@ __global__ void __launch_bounds__(kColBX* kColBY) k_sound_momentum(View<T> d) {
   const size_t cw = (size_t)jm + (size_t)nj * ii, ce = (size_t)jp + (size_t)nj * ii;
   const size_t cs = (size_t)jj + (size_t)nj * im, cn = (size_t)jj + (size_t)nj * ip;
   const size_t cwn = (size_t)jm + (size_t)nj * ip, ces = (size_t)jp + (size_t)nj * im;
+  const size_t o = (size_t)kk * pl, o1 = o + pl;
   const T dts = d.dts, egdts = d.egdts;
-  const T zcx = d.dtrdx * d.mu[c];
-  const T zcy = d.rotllr ? d.dtrdy : d.dtrdy * d.mv[c];
-  const T hx = d.hx[c], hy = d.hy[c];
-  const T cu = (d.coru[c] * dts) * T(0.25);
-  const T cv = (d.corv[c] * dts) * T(0.25);
+  const T dw_c = d.deltaw[c + o], dw_c1 = d.deltaw[c + o1];
+  const T tc = d.tetav[c + o];
+  const T pc = d.pai[c + o];
+  const T gzh = d.gzitakh[kk];
   const T hcpd = T(0.5) * T(kCpd);
-  T dw_c = d.deltaw[c], dw_w = d.deltaw[cw], dw_s = d.deltaw[cs];  // level k
-  for (int kk = 0; kk < kz; ++kk) {
-    const size_t o = (size_t)kk * pl, o1 = (size_t)(kk + 1) * pl;
-    const T dw_c1 = d.deltaw[c + o1], dw_w1 = d.deltaw[cw + o1], dw_s1 = d.deltaw[cs + o1];
-    const T tc = d.tetav[c + o];
-    const T pc = d.pai[c + o];
-    const T gzh = d.gzitakh[kk];
-    // Equation 17
-    {
-      T zfz = egdts + T(0.25) * (((dw_w + dw_w1) + dw_c) + dw_c1);
-      T zrom1u = hcpd * (d.tetav[cw + o] + tc);
-      T vdc = v[c + o];
-      T vdw = jj == 0 ? d.ev_j[ii + (size_t)ni * kk] : v[cw + o];
-      T vdwn = jj == 0 ? d.ev_j[ip + (size_t)ni * kk]
-                       : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * kk] : v[cwn + o]);
-      T vdn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * kk] : v[cn + o];
-      T zcor1u = cu * (((vdc + vdw) + vdwn) + vdn);
-      T paw = jj == 0 ? d.ep_j[ii + (size_t)ni * kk] : d.pai[cw + o];
-      uo[c + o] = ((u[c + o] + zcor1u) - (zfz * hx) * gzh) - (zcx * zrom1u) * (pc - paw);
-    }
-    // Equation 18
-    {
-      T zfz = egdts + T(0.25) * (((dw_s + dw_s1) + dw_c) + dw_c1);
-      T zrom1v = hcpd * (d.tetav[cs + o] + tc);
-      T udc = u[c + o];
-      T uds = ii == 0 ? d.eu_i[jj + (size_t)nj * kk] : u[cs + o];
-      T ude = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * kk] : u[ce + o];
-      T udes = jj == nj - 1 ? d.eu_j[im + (size_t)ni * kk]
-                            : (ii == 0 ? d.eu_i[jp + (size_t)nj * kk] : u[ces + o]);
-      T zcor1v = cv * (((udc + uds) + ude) + udes);
-      T pas = ii == 0 ? d.ep_i[jj + (size_t)nj * kk] : d.pai[cs + o];
-      vo[c + o] = ((v[c + o] - zcor1v) - (zfz * hy) * gzh) - (zcy * zrom1v) * (pc - pas);
-    }
-    dw_c = dw_c1; dw_w = dw_w1; dw_s = dw_s1;
+  // Equation 17
+  {
+    const T zcx = d.dtrdx * d.mu[c];
+    const T zfz = egdts + T(0.25) * (((d.deltaw[cw + o] + d.deltaw[cw + o1]) + dw_c) + dw_c1);
+    const T zrom1u = hcpd * (d.tetav[cw + o] + tc);
+    const T vdc = v[c + o];
+    const T vdw = jj == 0 ? d.ev_j[ii + (size_t)ni * kk] : v[cw + o];
+    const T vdwn = jj == 0 ? d.ev_j[ip + (size_t)ni * kk] : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * kk] : v[cwn + o]);
+    const T vdn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * kk] : v[cn + o];
+    const T zcor1u = ((d.coru[c] * dts) * T(0.25)) * (((vdc + vdw) + vdwn) + vdn);
+    const T paw = jj == 0 ? d.ep_j[ii + (size_t)ni * kk] : d.pai[cw + o];
+    uo[c + o] = ((u[c + o] + zcor1u) - (zfz * d.hx[c]) * gzh) - (zcx * zrom1u) * (pc - paw);
+  }
+  // Equation 18
+  {
+    const T zcy = d.rotllr ? d.dtrdy : d.dtrdy * d.mv[c];
+    const T zfz = egdts + T(0.25) * (((d.deltaw[cs + o] + d.deltaw[cs + o1]) + dw_c) + dw_c1);
+    const T zrom1v = hcpd * (d.tetav[cs + o] + tc);
+    const T udc = u[c + o];
+    const T uds = ii == 0 ? d.eu_i[jj + (size_t)nj * kk] : u[cs + o];
+    const T ude = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * kk] : u[ce + o];
+    const T udes = jj == nj - 1 ? d.eu_j[im + (size_t)ni * kk] : (ii == 0 ? d.eu_i[jp + (size_t)nj * kk] : u[ces + o]);
+    const T zcor1v = ((d.corv[c] * dts) * T(0.25)) * (((udc + uds) + ude) + udes);
+    const T pas = ii == 0 ? d.ep_i[jj + (size_t)nj * kk] : d.pai[cs + o];
+    vo[c + o] = ((v[c + o] - zcor1v) - (zfz * d.hy[c]) * gzh) - (zcy * zrom1v) * (pc - pas);
   }
 }
-
 // ---- advection: staggered -> cross points (:1327-1341, :1389-1417) -----
 template <class T>
 __global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_to_x(View<T> d) {
@@ -442,216 +469,242 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_to_x(View<T> d) {
 }
 
 // ---- advection: vertical WAF, two passes at dt/2 (:966-1073) ------------
-// One thread per column streams k with a 4-value window.  Pass 2 works in
-// place on wz: each level is read before it is overwritten.
+// wfw(k+1) of one pass from x(max(k-1,1)), x(k), x(k+1), x(min(k+2,kz))
 template <class T>
-__device__ __forceinline__ void waf_vpass(const T* src, T* dst, const T* __restrict__ s,
-                                          const T* __restrict__ wafu, const T* __restrict__ wafd,
-                                          size_t c, size_t pl, int kz, T dtrdz) {
-  T a = src[c];
-  T b = a;
-  T cc = src[c + (kz > 1 ? pl : 0)];
-  T wfw_k = T(0);
-  T s_k = s[c];
-  for (int k = 1; k <= kz; ++k) {  // 1-based level
-    const size_t o = (size_t)(k - 1) * pl;
-    const T s_k1 = s[c + (size_t)k * pl];  // s(k+1)
-    const int k2 = k + 2 <= kz ? k + 2 : kz;
-    const T dd = src[c + (size_t)(k2 - 1) * pl];
-    T wfw_k1 = T(0);
-    if (k <= kz - 1) {
-      const T zamu = s_k1 * dtrdz;
-      T is, num;
-      if (zamu >= T(0)) {
-        is = T(1); num = cc - dd;  // k1 = k+1, k1p1 = min(k+2, kz)
-      } else {
-        is = T(-1); num = a - b;   // k1 = max(k-1, 1), k1p1 = k
-      }
-      const T zzden = safeden(b - cc);
-      const T r = num / zzden;
-      const T bb = superbee(r);
-      const T zphi = (is + zamu * bb) - is * bb;
-      wfw_k1 = (T(0.5) * s_k1) * ((T(1) + zphi) * cc + (T(1) - zphi) * b);
-    }
-    const T zrfmu = wafu[c + o], zrfmd = wafd[c + o];
-    const T zdv = (s_k * zrfmu - s_k1 * zrfmd) * b;
-    dst[c + o] = ((b - wfw_k * zrfmu) + wfw_k1 * zrfmd) + zdv;
-    a = b; b = cc; cc = dd; wfw_k = wfw_k1; s_k = s_k1;
+__device__ __forceinline__ T waf_vflux(T s_k1, T dtrdz, T xm, T x0, T x1, T x2) {
+  const T zamu = s_k1 * dtrdz;
+  T is, num;
+  if (zamu >= T(0)) {
+    is = T(1); num = x1 - x2;  // k1 = k+1, k1p1 = min(k+2, kz)
+  } else {
+    is = T(-1); num = xm - x0;  // k1 = max(k-1, 1), k1p1 = k
   }
+  const T r = qdiv(num, safeden(x0 - x1));
+  const T bb = superbee(r);
+  const T zphi = (is + zamu * bb) - is * bb;
+  return (T(0.5) * s_k1) * ((T(1) + zphi) * x1 + (T(1) - zphi) * x0);
 }
 
-
+// One thread per column and field.  Both passes stream k in registers:
+// pass 1 yields wz1(t) at step t, pass 2 consumes it two levels later, so
+// the intermediate field never leaves the SM.  The grid puts the field
+// index fastest, so the ten fields of one column tile run together and
+// share the s / metric loads through L2.
 template <class T>
 __global__ void __launch_bounds__(kColBX* kColBY) k_waf_vertical(View<T> d, FieldPtrs<T> fp) {
-  int jj = blockIdx.x * kColBX + threadIdx.x;
-  int ii = blockIdx.y * kColBY + threadIdx.y;
+  const int f = blockIdx.x % kNumAdvected;
+  const int tj = blockIdx.x / kNumAdvected;
+  const int jj = tj * kColBX + threadIdx.x;
+  const int ii = blockIdx.y * kColBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
-  const int f = blockIdx.z;
   const size_t pl = d.pl;
   const size_t c = jj + (size_t)nj * ii;
-  T* wz = d.wz + (size_t)f * pl * kz;
-  waf_vpass<T>(fp.f[f], wz, d.s, d.wafu, d.wafd, c, pl, kz, d.dtrdz_a);  // pp -> wz
-  waf_vpass<T>(wz, wz, d.s, d.wafu, d.wafd, c, pl, kz, d.dtrdz_a);        // wz -> wz
-}
-
-// ---- advection: meridional WAF (:1075-1136) -----------------------------
-// Block = 32 j x kTileBI i points of one level; the wz rows i-2..i+BI+1 and
-// the BI+1 fluxes live in shared memory; all 10 fields reuse the velocity
-// and metric terms loaded once per thread.
-template <class T>
-__global__ void __launch_bounds__(kPtBX* kTileBI) k_waf_meridional(View<T> d, FieldPtrs<T> fp) {
-  constexpr int BI = kTileBI;
-  __shared__ T wzt[BI + 4][kPtBX];
-  __shared__ T flx[BI + 1][kPtBX];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz;
-  const size_t pl = d.pl;
-  const int j0 = blockIdx.x * kPtBX, i0 = blockIdx.y * BI, kk = blockIdx.z;
-  const int jj = j0 + tx;
-  const bool jok = jj < nj;
-  const int jc = jok ? jj : nj - 1;
-  const size_t ko = (size_t)kk * pl;
-  const T* __restrict__ v = d.vbuf[d.cur];
-  const T dtrdy = d.dtrdy_a;
-  // flux rows owned by this thread: q = ty, and q = BI for ty == 0
-  T fv[2], fz[2], frm[2];
-  bool fok[2];
-  for (int n = 0; n < 2; ++n) {
-    int q = n == 0 ? ty : BI;
-    int ii = i0 + q;  // flux zpby at 1-based i = ii+1 (between ii-1 and ii)
-    fok[n] = (n == 0 || ty == 0) && ii <= ni;
-    int iv = ii < ni ? ii : ii - ni;
-    size_t cq = jc + (size_t)nj * (fok[n] ? iv : 0);
-    fv[n] = fok[n] ? v[ko + cq] : T(0);
-    frm[n] = fok[n] ? d.rmv[cq] : T(1);
-    fz[n] = d.rotllr ? fv[n] * dtrdy : (fv[n] * frm[n]) * dtrdy;
-  }
-  // output point
-  const int io = i0 + ty;
-  const bool ook = jok && io < ni;
-  const int ion = io + 1 < ni ? io + 1 : 0;
-  const size_t co = jc + (size_t)nj * (io < ni ? io : 0);
-  const size_t con = jc + (size_t)nj * (io < ni ? ion : 0);
-  const T zrfmn = d.wafn[ko + co], zrfms = d.wafs[ko + co];
-  const T vs = v[ko + co], vn = v[ko + con];
-  const T rmvs = d.rmv[co], rmvn = d.rmv[con], mx2 = d.mx2[co];
-  for (int f = 0; f < kNumAdvected; ++f) {
-    const T* __restrict__ wzf = d.wz + (size_t)f * pl * kz;
-    for (int r = ty; r < BI + 4; r += BI) wzt[r][tx] = wzf[ko + jc + (size_t)nj * wrapn(i0 - 2 + r, ni)];
-    __syncthreads();
-    for (int n = 0; n < 2; ++n) {
-      if (!fok[n]) continue;
-      const int q = n == 0 ? ty : BI;
-      const int r = q + 2;
-      const T zamu = fz[n];
-      T is, num;
-      if (zamu > T(0)) {
-        is = T(1); num = wzt[r - 1][tx] - wzt[r - 2][tx];   // ih = i-1, ihm1 = i-2
-      } else {
-        is = T(-1); num = wzt[r + 1][tx] - wzt[r][tx];      // ih = i+1, ihm1 = i
-      }
-      const T zzden = safeden(wzt[r][tx] - wzt[r - 1][tx]);
-      const T rr = num / zzden;
-      const T bb = superbee(rr);
-      const T zphi = (is + zamu * bb) - is * bb;
-      const T fl = (T(1) + zphi) * wzt[r - 1][tx] + (T(1) - zphi) * wzt[r][tx];
-      flx[q][tx] = d.rotllr ? (T(0.5) * fv[n]) * fl : ((T(0.5) * fv[n]) * frm[n]) * fl;
+  const T* __restrict__ src = fp.f[f];
+  T* __restrict__ wz = d.wz + (size_t)f * pl * kz;
+  const T* __restrict__ s = d.s;
+  const T* __restrict__ wafu = d.wafu;
+  const T* __restrict__ wafd = d.wafd;
+  const T dtrdz = d.dtrdz_a;
+  T xa = src[c], xb = xa, xc = src[c + pl];  // pass-1 window x(t-1), x(t), x(t+1)
+  T wfw1 = T(0), wfw2 = T(0);                // wfw1(t), wfw2(m)
+  T y0 = T(0), y1 = T(0), y2 = T(0), y3 = T(0);  // wz1(t-3 .. t)
+  T sA = T(0), sB = T(0), sC = s[c], sD;    // s(t-2 .. t+1)
+  T uA = T(0), uB = T(0), dA = T(0), dB = T(0);  // wafu/wafd at t-2, t-1
+  for (int t = 1; t <= kz + 2; ++t) {
+    T w1 = y3, uC = T(0), dC = T(0);
+    sD = T(0);
+    if (t <= kz) {
+      const size_t o = (size_t)(t - 1) * pl;
+      sD = s[c + (size_t)t * pl];
+      const int t2 = t + 2 <= kz ? t + 2 : kz;
+      const T xd = src[c + (size_t)(t2 - 1) * pl];
+      uC = wafu[c + o];
+      dC = wafd[c + o];
+      const T wfw1n = t <= kz - 1 ? waf_vflux(sD, dtrdz, xa, xb, xc, xd) : T(0);
+      w1 = ((xb - wfw1 * uC) + wfw1n * dC) + (sC * uC - sD * dC) * xb;
+      xa = xb; xb = xc; xc = xd; wfw1 = wfw1n;
     }
-    __syncthreads();
-    if (ook) {
-      T* __restrict__ ppf = fp.f[f];
-      const T pp = ppf[ko + co];
-      T p0;
-      if (d.rotllr) {
-        const T zdv = (vn * zrfmn - vs * zrfms) * pp;
-        p0 = ((wzt[ty + 2][tx] + flx[ty][tx] * zrfms) - flx[ty + 1][tx] * zrfmn) + zdv;
-      } else {
-        const T zdv = ((vn * rmvn) * zrfmn - (vs * rmvs) * zrfms) * pp;
-        p0 = wzt[ty + 2][tx] + mx2 * (((flx[ty][tx] * zrfms) - flx[ty + 1][tx] * zrfmn) + zdv);
-      }
-      d.p0[(size_t)f * pl * kz + ko + co] = p0;
+    y0 = y1; y1 = y2; y2 = y3; y3 = w1;  // for t > kz, wz1 stays clamped at wz1(kz)
+    const int m = t - 2;
+    if (m >= 1) {
+      const T ym = m == 1 ? y1 : y0;
+      const T wfw2n = m <= kz - 1 ? waf_vflux(sB, dtrdz, ym, y1, y2, y3) : T(0);
+      wz[c + (size_t)(m - 1) * pl] = ((y1 - wfw2 * uA) + wfw2n * dA) + (sA * uA - sB * dA) * y1;
+      wfw2 = wfw2n;
     }
-    __syncthreads();
+    sA = sB; sB = sC; sC = sD;
+    uA = uB; uB = uC; dA = dB; dB = dC;
   }
 }
 
-// ---- advection: zonal WAF (:1138-1187), update of pp in place -----------
+// ---- advection: meridional + zonal WAF of one level (:1075-1187) -------
+// Block = 32 (j) x 8 (i) output points of one level, ten fields in turn.
+// Per field: the wz tile with a 2-point halo in both directions and the pp
+// tile go to shared memory; the meridional fluxes and p0 are formed for the
+// 36-wide strip the zonal step needs, then the zonal fluxes and the new pp.
+// p0 never leaves the SM.  The result is written to the other field buffer
+// (dst): neighbouring blocks still read the old pp at their halo columns.
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kTileBI) k_waf_zonal(View<T> d, FieldPtrs<T> fp) {
-  constexpr int BI = kTileBI;
-  constexpr int BX = kPtBX;
-  __shared__ T p0t[BI][BX + 4];
-  __shared__ T flx[BI][BX + 1];
-  const int tx = threadIdx.x, ty = threadIdx.y;
+__global__ void __launch_bounds__(256) k_waf_horizontal(View<T> d, FieldPtrs<T> src, FieldPtrs<T> dst) {
+  constexpr int TJ = 32, TI = 8, HJ = TJ + 4, HI = TI + 4;
+  constexpr int NW = HI * HJ, NP = TI * HJ, NM = (TI + 1) * HJ, NZ = TI * (TJ + 1);
+  __shared__ T sw[2][HI][HJ];    // wz, rows i0-2.., cols j0-2.. (two fields in flight)
+  __shared__ T sp[2][TI][HJ];    // pp (old), rows i0.., cols j0-2..
+  __shared__ T smf[TI + 1][HJ];  // meridional fluxes at rows i0..i0+TI
+  __shared__ T sp0[TI][HJ];      // p0
+  __shared__ T szf[TI][TJ + 1];  // zonal fluxes at cols j0..j0+TJ
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   const size_t pl = d.pl;
-  const int j0 = blockIdx.x * BX, i0 = blockIdx.y * BI, kk = blockIdx.z;
-  const int ii = i0 + ty;
-  const bool iok = ii < ni;
-  const int ic = iok ? ii : ni - 1;
+  const int j0 = blockIdx.x * TJ, i0 = blockIdx.y * TI, kk = blockIdx.z;
   const size_t ko = (size_t)kk * pl;
-  const size_t row = (size_t)nj * ic;
   const T* __restrict__ u = d.ubuf[d.cur];
-  const T dtrdx = d.dtrdx_a;
-  T fu[2], fz[2], frm[2];
-  bool fok[2];
+  const T* __restrict__ v = d.vbuf[d.cur];
+  const T dtrdx = d.dtrdx_a, dtrdy = d.dtrdy_a;
+  const int rot = d.rotllr;
+
+  // field-independent terms of the points this thread owns
+  T mz[2], mfac[2];  // meridional flux points: zamu and the factor of fl
   for (int n = 0; n < 2; ++n) {
-    int q = n == 0 ? tx : BX;
-    int jq = j0 + q;  // flux zpbw at 1-based j = jq+1
-    fok[n] = (n == 0 || tx == 0) && jq <= nj;
-    int ju = jq < nj ? jq : jq - nj;
-    size_t cq = (fok[n] ? ju : 0) + row;
-    fu[n] = fok[n] ? u[ko + cq] : T(0);
-    T m = fok[n] ? (d.rotllr ? d.mu[cq] : d.rmu[cq]) : T(1);
-    frm[n] = m;
-    fz[n] = (fu[n] * m) * dtrdx;
+    const int q = tid + 256 * n;
+    mz[n] = T(0); mfac[n] = T(0);
+    if (q < NM) {
+      const int r = q / HJ, x = q % HJ;
+      const size_t cq = wrapn(j0 - 2 + x, nj) + (size_t)nj * wrapn(i0 + r, ni);
+      const T vv = v[ko + cq];
+      const T rm = d.rmv[cq];
+      mz[n] = rot ? vv * dtrdy : (vv * rm) * dtrdy;
+      mfac[n] = rot ? T(0.5) * vv : (T(0.5) * vv) * rm;
+    }
   }
-  const int jo = j0 + tx;
-  const bool ook = iok && jo < nj;
-  const int joe = jo + 1 < nj ? jo + 1 : 0;
-  const size_t co = (jo < nj ? jo : 0) + row;
-  const size_t coe = (jo < nj ? joe : 0) + row;
-  const T zrfme = d.wafe[ko + co], zrfmw = d.wafw[ko + co];
-  const T uw = u[ko + co], ue = u[ko + coe];
-  const T rmuw = d.rmu[co], rmue = d.rmu[coe], mx2 = d.mx2[co];
-  for (int f = 0; f < kNumAdvected; ++f) {
-    const T* __restrict__ p0f = d.p0 + (size_t)f * pl * kz;
-    for (int x = tx; x < BX + 4; x += BX) p0t[ty][x] = p0f[ko + row + wrapn(j0 - 2 + x, nj)];
-    __syncthreads();
+  T pn[2], ps_[2], pdv[2], pmx[2];  // p0 points: zrfmn, zrfms, velocity-divergence factor, mx2
+  for (int n = 0; n < 2; ++n) {
+    const int q = tid + 256 * n;
+    pn[n] = ps_[n] = pdv[n] = pmx[n] = T(0);
+    if (q < NP) {
+      const int r = q / HJ, x = q % HJ;
+      const int jq = wrapn(j0 - 2 + x, nj), iq = wrapn(i0 + r, ni), iqn = wp1(iq, ni);
+      const size_t cq = jq + (size_t)nj * iq, cqn = jq + (size_t)nj * iqn;
+      const T zrfmn = d.wafn[ko + cq], zrfms = d.wafs[ko + cq];
+      const T vs = v[ko + cq], vn = v[ko + cqn];
+      pn[n] = zrfmn; ps_[n] = zrfms;
+      pdv[n] = rot ? (vn * zrfmn - vs * zrfms) : ((vn * d.rmv[cqn]) * zrfmn - (vs * d.rmv[cq]) * zrfms);
+      pmx[n] = d.mx2[cq];
+    }
+  }
+  T zz[2], zfac[2];  // zonal flux points
+  for (int n = 0; n < 2; ++n) {
+    const int q = tid + 256 * n;
+    zz[n] = T(0); zfac[n] = T(0);
+    if (q < NZ) {
+      const int r = q / (TJ + 1), x = q % (TJ + 1);
+      const size_t cq = wrapn(j0 + x, nj) + (size_t)nj * wrapn(i0 + r, ni);
+      const T uu = u[ko + cq];
+      const T m = rot ? d.mu[cq] : d.rmu[cq];
+      zz[n] = (uu * m) * dtrdx;
+      zfac[n] = rot ? T(0.5) * uu : (T(0.5) * uu) * m;
+    }
+  }
+  const int jo = j0 + tx, io = i0 + ty;
+  const bool ook = jo < nj && io < ni;
+  T oe = T(0), ow = T(0), odv = T(0), omx = T(0);
+  size_t co = 0;
+  if (ook) {
+    co = jo + (size_t)nj * io;
+    const size_t coe = wp1(jo, nj) + (size_t)nj * io;
+    oe = d.wafe[ko + co]; ow = d.wafw[ko + co];
+    const T uw = u[ko + co], ue = u[ko + coe];
+    odv = rot ? (ue * oe - uw * ow) : ((ue * d.rmu[coe]) * oe - (uw * d.rmu[co]) * ow);
+    omx = d.mx2[co];
+  }
+
+  // wrapped tile offsets are the same for every field: compute them once
+  int woff[2], poff[2];
+  for (int n = 0; n < 2; ++n) {
+    const int q = tid + 256 * n;
+    woff[n] = q < NW ? wrapn(j0 - 2 + q % HJ, nj) + nj * wrapn(i0 - 2 + q / HJ, ni) : 0;
+    poff[n] = q < NP ? wrapn(j0 - 2 + q % HJ, nj) + nj * wrapn(i0 + q / HJ, ni) : 0;
+  }
+  // double-buffered tiles; the next field's values travel in registers
+  // while the current field is computed
+  T rw[2], rp[2];
+  auto fetch = [&](int f) {
+    const T* __restrict__ wzf = d.wz + (size_t)f * pl * kz + ko;
+    const T* __restrict__ ppf = src.f[f] + ko;
     for (int n = 0; n < 2; ++n) {
-      if (!fok[n]) continue;
-      const int q = n == 0 ? tx : BX;
-      const int x = q + 2;
-      const T zamu = fz[n];
-      T is, num;
-      if (zamu > T(0)) {
-        is = T(1); num = p0t[ty][x - 1] - p0t[ty][x - 2];
-      } else {
-        is = T(-1); num = p0t[ty][x + 1] - p0t[ty][x];
+      const int q = tid + 256 * n;
+      rw[n] = q < NW ? wzf[woff[n]] : T(0);
+      rp[n] = q < NP ? ppf[poff[n]] : T(0);
+    }
+  };
+  auto stash = [&](int b) {
+    for (int n = 0; n < 2; ++n) {
+      const int q = tid + 256 * n;
+      if (q < NW) sw[b][q / HJ][q % HJ] = rw[n];
+      if (q < NP) sp[b][q / HJ][q % HJ] = rp[n];
+    }
+  };
+  fetch(0);
+  stash(0);
+  __syncthreads();
+  for (int f = 0; f < kNumAdvected; ++f) {
+    const int b = f & 1;
+    if (f + 1 < kNumAdvected) fetch(f + 1);
+    for (int n = 0; n < 2; ++n) {  // zpby, flux between rows r+1 and r+2 of sw
+      const int q = tid + 256 * n;
+      if (q < NM) {
+        const int r = q / HJ, x = q % HJ;
+        const T zamu = mz[n];
+        T is, num;
+        if (zamu > T(0)) {
+          is = T(1); num = sw[b][r + 1][x] - sw[b][r][x];      // ih = i-1, ihm1 = i-2
+        } else {
+          is = T(-1); num = sw[b][r + 3][x] - sw[b][r + 2][x];  // ih = i+1, ihm1 = i
+        }
+        const T rr = qdiv(num, safeden(sw[b][r + 2][x] - sw[b][r + 1][x]));
+        const T bb = superbee(rr);
+        const T zphi = (is + zamu * bb) - is * bb;
+        smf[r][x] = mfac[n] * ((T(1) + zphi) * sw[b][r + 1][x] + (T(1) - zphi) * sw[b][r + 2][x]);
       }
-      const T zzden = safeden(p0t[ty][x] - p0t[ty][x - 1]);
-      const T rr = num / zzden;
-      const T bb = superbee(rr);
-      const T zphi = (is + zamu * bb) - is * bb;
-      const T fl = (T(1) + zphi) * p0t[ty][x - 1] + (T(1) - zphi) * p0t[ty][x];
-      flx[ty][q] = d.rotllr ? (T(0.5) * fu[n]) * fl : ((T(0.5) * fu[n]) * frm[n]) * fl;
     }
     __syncthreads();
-    if (ook) {
-      T* __restrict__ ppf = fp.f[f];
-      const T pp = ppf[ko + co];
-      const T p0 = p0t[ty][tx + 2];
-      T out;
-      if (d.rotllr) {
-        const T zdv = (ue * zrfme - uw * zrfmw) * pp;
-        out = ((p0 + flx[ty][tx] * zrfmw) - flx[ty][tx + 1] * zrfme) + zdv;
-      } else {
-        const T zdv = ((ue * rmue) * zrfme - (uw * rmuw) * zrfmw) * pp;
-        out = p0 + mx2 * (((flx[ty][tx] * zrfmw) - flx[ty][tx + 1] * zrfme) + zdv);
+    for (int n = 0; n < 2; ++n) {  // p0 (:1113-1131, :1222-1240)
+      const int q = tid + 256 * n;
+      if (q < NP) {
+        const int r = q / HJ, x = q % HJ;
+        const T zdv = pdv[n] * sp[b][r][x];
+        sp0[r][x] = rot ? ((sw[b][r + 2][x] + smf[r][x] * ps_[n]) - smf[r + 1][x] * pn[n]) + zdv
+                        : sw[b][r + 2][x] + pmx[n] * (((smf[r][x] * ps_[n]) - smf[r + 1][x] * pn[n]) + zdv);
       }
-      ppf[ko + co] = out;
     }
+    __syncthreads();
+    for (int n = 0; n < 2; ++n) {  // zpbw, flux between cols x+1 and x+2 of sp0
+      const int q = tid + 256 * n;
+      if (q < NZ) {
+        const int r = q / (TJ + 1), x = q % (TJ + 1);
+        const T zamu = zz[n];
+        T is, num;
+        if (zamu > T(0)) {
+          is = T(1); num = sp0[r][x + 1] - sp0[r][x];
+        } else {
+          is = T(-1); num = sp0[r][x + 3] - sp0[r][x + 2];
+        }
+        const T rr = qdiv(num, safeden(sp0[r][x + 2] - sp0[r][x + 1]));
+        const T bb = superbee(rr);
+        const T zphi = (is + zamu * bb) - is * bb;
+        szf[r][x] = zfac[n] * ((T(1) + zphi) * sp0[r][x + 1] + (T(1) - zphi) * sp0[r][x + 2]);
+      }
+    }
+    __syncthreads();
+    if (ook) {  // new pp (:1173-1187, :1283-1297)
+      const T p0 = sp0[ty][tx + 2];
+      const T zdv = odv * sp[b][ty][tx + 2];
+      const T out = rot ? ((p0 + szf[ty][tx] * ow) - szf[ty][tx + 1] * oe) + zdv
+                        : p0 + omx * (((szf[ty][tx] * ow) - szf[ty][tx + 1] * oe) + zdv);
+      dst.f[f][ko + co] = out;
+    }
+    if (f + 1 < kNumAdvected) stash(b ^ 1);  // the other buffer was last read two fields ago
     __syncthreads();
   }
 }
@@ -807,10 +860,9 @@ void set_timer(KernelTimer* t) { g_timer = t; }
     if (g_timer) g_timer->mark((KIND), (STREAM), false);        \
   } while (0)
 template <class T>
-inline FieldPtrs<T> advected(const View<T>& d) {
+inline FieldPtrs<T> field_set(const View<T>& d, int set) {
   FieldPtrs<T> fp;
-  fp.f[0] = d.tetav; fp.f[1] = d.pai; fp.f[2] = d.ux; fp.f[3] = d.vx; fp.f[4] = d.wx;
-  for (int n = 0; n < 5; ++n) fp.f[5 + n] = d.q[n];
+  for (int n = 0; n < kNumAdvected; ++n) fp.f[n] = d.fset[set][n];
   return fp;
 }
 
@@ -819,9 +871,6 @@ inline dim3 col_grid(int nj, int ni, int z = 1) {
 }
 inline dim3 pt_grid(int nj, int ni, int nz) {
   return dim3((nj + kPtBX - 1) / kPtBX, (ni + kPtBY - 1) / kPtBY, nz);
-}
-inline dim3 tile_grid(int nj, int ni, int nz) {
-  return dim3((nj + kPtBX - 1) / kPtBX, (ni + kTileBI - 1) / kTileBI, nz);
 }
 
 template <class T>
@@ -838,8 +887,9 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
   for (int ns = 1; ns <= fl.nsound; ++ns) {
     const int last = ns == fl.nsound;
-    MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div<T><<<cg, cb, 0, st>>>(d));
-    ++n;
+    MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div<T><<<pg, pb, 0, st>>>(d));
+    MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp<T><<<pg, pb, 0, st>>>(d));
+    n += 2;
     if (fl.divfilter) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 1));
       MOLOCH_LAUNCH(KK_LAP_FILTER, st, k_lap_filter<T><<<pg, pb, 0, st>>>(d, d.zdiv2b, d.zdiv2a, 1, T(0)));
@@ -849,23 +899,28 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
-    MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum<T><<<cg, cb, 0, st>>>(d));
+    MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum<T><<<pg, pb, 0, st>>>(d));
     ++n;
     d.cur ^= 1;
   }
   return n;
 }
 
+// one advection() call; the advected fields move to the other buffer set
 template <class T>
 int launch_advection(View<T>& d, cudaStream_t st) {
-  const FieldPtrs<T> fp = advected(d);
-  MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pt_grid(d.nj, d.ni, d.kz), dim3(kPtBX, kPtBY), 0, st>>>(d));
-  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<col_grid(d.nj, d.ni, kNumAdvected), dim3(kColBX, kColBY), 0, st>>>(d, fp));
-  MOLOCH_LAUNCH(KK_WAF_MERIDIONAL, st, k_waf_meridional<T><<<tile_grid(d.nj, d.ni, d.kz), dim3(kPtBX, kTileBI), 0, st>>>(d, fp));
-  MOLOCH_LAUNCH(KK_WAF_ZONAL, st, k_waf_zonal<T><<<tile_grid(d.nj, d.ni, d.kz), dim3(kPtBX, kTileBI), 0, st>>>(d, fp));
-  MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pt_grid(d.nj, d.ni, d.kz), dim3(kPtBX, kPtBY), 0, st>>>(d));
+  const FieldPtrs<T> src = field_set(d, d.fcur), dst = field_set(d, d.fcur ^ 1);
+  const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
+  const dim3 vg(((d.nj + kColBX - 1) / kColBX) * kNumAdvected, (d.ni + kColBY - 1) / kColBY);
+  const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, d.kz);
+  MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pg, pb, 0, st>>>(d));
+  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<vg, dim3(kColBX, kColBY), 0, st>>>(d, src));
+  MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_horizontal<T><<<hg, dim3(32, 8), 0, st>>>(d, src, dst));
+  d.fcur ^= 1;
+  d.bind_fields();
+  MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pg, pb, 0, st>>>(d));
   d.cur = 0;
-  return 5;
+  return 4;
 }
 
 template <class T>

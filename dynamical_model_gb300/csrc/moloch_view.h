@@ -52,8 +52,11 @@ struct View {
   T* ux;
   T* vx;
   T* wx;
-  T* wz;  // kNumAdvected fields
-  T* p0;  // kNumAdvected fields
+  T* wz;  // kNumAdvected fields (vertical WAF result)
+  // the ten advected fields live in two buffer sets; the horizontal WAF
+  // step writes the other set (fset[fcur ^ 1]) and the sets swap roles
+  T* fset[2][kNumAdvected];
+  int fcur;
   T* pf;
   T* tf;
   T* fscr;  // filter output scratch
@@ -106,12 +109,22 @@ struct View {
   double* dpart;  // per-block partial reductions
   double* dres;   // final reduction (device)
   int dparts;
+
+  // point the named field pointers at the current buffer set
+  void bind_fields() {
+    tetav = fset[fcur][0];
+    pai = fset[fcur][1];
+    ux = fset[fcur][2];
+    vx = fset[fcur][3];
+    wx = fset[fcur][4];
+    for (int n = 0; n < 5; ++n) q[n] = fset[fcur][5 + n];
+  }
 };
 
 // Kernel kinds, for per-kernel CUDA-event timing (moloch_gpu_profile_step).
 enum KernelKind {
-  KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE, KK_SOUND_MOMENTUM,
-  KK_STAG_TO_X, KK_WAF_VERTICAL, KK_WAF_MERIDIONAL, KK_WAF_ZONAL, KK_STAG_FROM_X,
+  KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_DAMP, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE,
+  KK_SOUND_MOMENTUM, KK_STAG_TO_X, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
   KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_COUNT
 };
 
