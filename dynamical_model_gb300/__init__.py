@@ -88,6 +88,10 @@ _PROTOS = {
                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_kernel_kinds": (ctypes.c_int, []),
     "moloch_gpu_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
+    "moloch_gpu_tuning_count": (ctypes.c_int, []),
+    "moloch_gpu_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "moloch_gpu_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
                                   [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
 }
@@ -220,6 +224,19 @@ class Moloch:
         cnt = (ctypes.c_int * n)()
         _check(self.L.moloch_gpu_profile_step(self.h, ms, cnt, n))
         return {self.L.moloch_gpu_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n) if cnt[k]}
+
+    def autotune(self):
+        """Time the tunable launch shapes on this handle (advances the state)
+        and keep the fastest; returns the chosen values."""
+        n = self.L.moloch_gpu_tuning_count()
+        ch = (ctypes.c_int * n)()
+        ms = (ctypes.c_double * n)()
+        _check(self.L.moloch_gpu_autotune(self.h, ch, ms, n))
+        return list(ch)
+
+    def set_tuning(self, choice):
+        arr = (ctypes.c_int * len(choice))(*choice)
+        _check(self.L.moloch_gpu_set_tuning(self.h, arr, len(choice)))
 
     @property
     def stream(self):

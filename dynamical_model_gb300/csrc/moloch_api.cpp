@@ -224,6 +224,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.dparts = parts;
   v.nj = h->nj(); v.ni = h->ni(); v.kz = h->kz(); v.pl = (int)pl; v.rotllr = h->prm.rotllr;
   v.cur = 0;
+  v.hz_levels = 1;
   return off + 256;
 }
 
@@ -813,6 +814,66 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
   for (int q = 0; q < KernelTimer::kCap; ++q) cudaEventDestroy(tm->ev[q]);
   delete tm;
   return rc;
+}
+
+// ---- autotuner --------------------------------------------------------------
+// Tunable launch shapes, in order: [0] levels per k_waf_horizontal block.
+static const int kTuneCandidates[][4] = {{1, 2, 4, 8}};
+static const int kTuneCount = 1;
+
+int moloch_gpu_tuning_count(void) { return kTuneCount; }
+
+int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
+  g_err.clear();
+  if (!h || (n > 0 && !choice)) return fail(MOLOCH_ERR_ARG, "null argument");
+  if (n > 0) {
+    if (choice[0] < 1 || choice[0] > 64) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
+    h->vd.hz_levels = choice[0];
+    h->vf.hz_levels = choice[0];
+  }
+  for (int q = 0; q < 2; ++q) {  // launch shapes are baked into captured graphs
+    if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
+    if (h->graph[q]) { cudaGraphDestroy(h->graph[q]); h->graph[q] = nullptr; }
+  }
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n) {
+  g_err.clear();
+  if (!h || !choice || n < kTuneCount) return fail(MOLOCH_ERR_ARG, "need %d choice slots", kTuneCount);
+  if (!h->initialized) return fail(MOLOCH_ERR_STATE, "autotune before moloch_gpu_init");
+  // time advection() (the tuned kernel's phase) on a copy of the view: the
+  // state is advanced but the step the caller sees is unchanged in shape
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best = 1e30;
+  int pick = h->elem == 8 ? h->vd.hz_levels : h->vf.hz_levels;
+  for (int c = 0; c < 4; ++c) {
+    const int cand = kTuneCandidates[0][c];
+    if (cand > h->kz()) continue;
+    h->vd.hz_levels = cand;
+    h->vf.hz_levels = cand;
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {  // first repeat warms up
+      cudaEventRecord(e0, h->stream);
+      int nk = h->elem == 8 ? launch_phase(h, h->vd, 2) : launch_phase(h, h->vf, 2);
+      h->kernels += nk;
+      cudaEventRecord(e1, h->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best) { best = tot; pick = cand; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  choice[0] = pick;
+  if (best_ms) best_ms[0] = best / 2.0;
+  return moloch_gpu_set_tuning(h, choice, kTuneCount);
 }
 
 int moloch_internal_describe(moloch_handle_t* h, moloch_grid_t* g, moloch_params_t* p) {

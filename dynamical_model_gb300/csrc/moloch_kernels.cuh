@@ -23,6 +23,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <type_traits>
 
 #include "moloch_constants.h"
 #include "moloch_view.h"
@@ -233,7 +234,7 @@ template <> __device__ __forceinline__ double pivot_rcp<float>(double den) {
 // with the Exner/theta/pai update of the level above it.
 // defer_pai: leave zdiv2b final and pai to k_pai_update (divergence filter on).
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 5)
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
     k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
   const int jj = blockIdx.x * kColBX + threadIdx.x;
   const int ii = blockIdx.y * kColBY + threadIdx.y;
@@ -241,95 +242,137 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 5)
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
   const size_t c = (size_t)jj + (size_t)nj * ii;
+  // one restrict-qualified pointer per array, offset to this column, so the
+  // loads of the next level can be issued ahead of the current level's
+  // stores and FP64 work
+  T* __restrict__ W = d.w + c;
+  const T* __restrict__ FMZF = d.fmzf + c;
+  const T* __restrict__ QV = d.q[0] + c;
+  const T* __restrict__ QC = d.q[1] + c;
+  T* __restrict__ TET = d.tetav + c;
+  T* __restrict__ PAI = d.pai + c;
+  const T* __restrict__ QSAT = d.qsat + c;
+  const T* __restrict__ TT = d.t + c;
+  T* __restrict__ ZD = d.zdiv2b + c;
+  const T* __restrict__ FMZ = d.fmz + c;
+  const T* __restrict__ QWL = d.qwltot + c;
+  const T* __restrict__ QWI = d.qwitot + c;
+  T* __restrict__ S = d.s + c;
+  T* __restrict__ DW = d.deltaw + c;
+  const T* __restrict__ FF = d.ffilt;
   const T ns = T(nsound), ns1 = T(nsound - 1);
   const T zcs2 = d.zcs2, dts = d.dts, egdts = d.egdts, dtrdz = d.dtrdz;
 
-  // (b) down-sweep
-  const T wsurf = d.w[c + (size_t)kz * pl];  // w(kz+1) from k_sound_div
-  double wkp1 = (double)wsurf;
+  // (b) down-sweep k = kz .. 2, loads of the next level issued one level ahead.
+  // The pivots (den, its reciprocal zrapp and the ratio wwkw) are FP64 in
+  // every mode.  FP64 storage: the right-hand-side sweep and the stash are
+  // FP64 too (the reference's arithmetic).  FP32 storage: the right-hand
+  // side and the stash are FP32, which keeps the FP64 pipe -- 1/64 of the
+  // FP32 rate on GB300 -- to the pivot recurrence.
+  constexpr bool kF32 = sizeof(T) == 4;
+  using ST = typename std::conditional<kF32, float, double>::type;  // stash / RHS type
+  ST* __restrict__ WPs = reinterpret_cast<ST*>(d.wp) + c;
+  ST* __restrict__ WWs = reinterpret_cast<ST*>(d.wwkw) + c;
+  const T wsurf = W[(size_t)kz * pl];  // w(kz+1) from k_sound_div
+  ST wkp1 = (ST)wsurf;
   double wwp1 = 0.0;  // wwkw(kz+1) = 0
   size_t o = (size_t)(kz - 1) * pl;
-  T zd_k = d.zdiv2b[c + o];
-  T tk = d.tetav[c + o];
-  T pk = d.pai[c + o];
-  T fk = d.fmz[c + o];
-  T qsk = d.qsat[c + o];
-#pragma unroll 2
+  T zd_k = ZD[o], tk = TET[o], pk = PAI[o], fk = FMZ[o], qsk = QSAT[o];
+  T n_wk = W[o], n_fz = FMZF[o], n_qv = QV[o], n_ff = FF[kz - 1];
+  T n_tkm = TET[o - pl], n_pkm = PAI[o - pl], n_qskm = QSAT[o - pl], n_zdkm = ZD[o - pl];
+  T n_fkm = FMZ[o - pl], n_tm = TT[o - pl];
   for (int kk = kz - 1; kk >= 1; --kk) {
     o = (size_t)kk * pl;
-    const size_t om = o - pl;
-    const T wk = d.w[c + o];
-    const T fz = d.fmzf[c + o];
-    const T qvk = d.q[0][c + o];
-    const T tkm = d.tetav[c + om];
-    const T pkm = d.pai[c + om];
-    const T qskm = d.qsat[c + om];
-    const T zd_km = d.zdiv2b[c + om];
-    const T fkm = d.fmz[c + om];
-    const T ff = d.ffilt[kk];
+    const T wk = n_wk, fz = n_fz, qvk = n_qv, ff = n_ff, tkm = n_tkm, pkm = n_pkm;
+    const T qskm = n_qskm, zd_km = n_zdkm, fkm = n_fkm, tm = n_tm;
+    if (kk > 1) {
+      const size_t on = o - pl, onm = on - pl;
+      n_wk = W[on]; n_fz = FMZF[on]; n_qv = QV[on]; n_ff = FF[kk - 1];
+      n_tkm = TET[onm]; n_pkm = PAI[onm]; n_qskm = QSAT[onm]; n_zdkm = ZD[onm];
+      n_fkm = FMZ[onm]; n_tm = TT[onm];
+    }
     T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
     zrom1w = zrom1w - (((((T(kCpd) * wk) * fz) * fz) * ns) * dtrdz) * (tkm - tk);
     if (qvk > T(0.96) * qsk && wk > T(0.1)) {
       const T zqs = T(0.5) * (qsk + qskm);
-      const T tm = d.t[c + om];
       const T zdth = ((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs) /
                      ((((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
       zrom1w = zrom1w + zdth * fz;
     }
     T zwexpl = (wk - (zrom1w * dtrdz) * (pkm - pk)) - egdts;
     zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * (pkm * zd_km - pk * zd_k);
-    const double zu = (double)(((zcs2 * fkm) * zrom1w) * pkm + ff);
-    const double zdd = (double)(((zcs2 * fk) * zrom1w) * pk + ff);
+    const T zu_t = ((zcs2 * fkm) * zrom1w) * pkm + ff;
+    const T zd_t = ((zcs2 * fk) * zrom1w) * pk + ff;
+    const double zu = (double)zu_t;
+    const double zdd = (double)zd_t;
     const double zrapp = pivot_rcp<T>(((1.0 + zdd) + zu) - zdd * wwp1);
-    const double wpk = zrapp * ((double)zwexpl + zdd * wkp1);
     const double wwk = zrapp * zu;
-    d.wp[c + o] = wpk;
-    d.wwkw[c + o] = wwk;
+    ST wpk;
+    if constexpr (kF32)
+      wpk = (float)zrapp * (zwexpl + zd_t * wkp1);
+    else
+      wpk = zrapp * ((double)zwexpl + zdd * wkp1);
+    WPs[o] = wpk;
+    WWs[o] = (ST)wwk;
     wkp1 = wpk; wwp1 = wwk;
     zd_k = zd_km; tk = tkm; pk = pkm; fk = fkm; qsk = qskm;
   }
 
   // (c) back-substitution (:681-686) fused with the Exner/theta update of
-  // the level above (:690-728); w(1) = 0 always (init_moloch :260-262)
+  // the level above (:690-728); w(1) = 0 always (init_moloch :260-262).
+  // Level kk is solved while level kk-1 is finalized; loads run one ahead.
   const T rdrcv = T(kRdrcv);
-  auto finalize = [&](int kk, T wl, T wh) {
-    const size_t q = c + (size_t)kk * pl;
-    T zd = d.zdiv2b[q];
-    zd = zd + (dtrdz * d.fmz[q]) * (wl - wh);
-    const T qv = d.q[0][q], qc = d.q[1][q];
-    zd = (zd * ((T(1) + T(0.86) * qv) + T(3.2) * qc)) / ((T(1) + T(0.96) * qv) + T(4.8) * qc);
-    d.tetav[q] = d.tetav[q] * (T(1) + (rdrcv * zd) * ((T(0.25) * qv + T(4.2) * d.qwltot[q]) + T(2.1) * d.qwitot[q]));
-    if (defer_pai) {
-      d.zdiv2b[q] = zd;
-    } else {
-      const T pold = d.pai[q];
-      if (jj == nj - 1) d.ep_j[ii + (size_t)ni * kk] = pold;
-      if (ii == ni - 1) d.ep_i[jj + (size_t)nj * kk] = pold;
-      d.pai[q] = pold * (T(1) - rdrcv * zd);
-    }
-    if (last) {  // complete Equation 10 (:843-849)
-      if (kk == 0)
-        d.s[q] = T(0);
-      else
-        d.s[q] = (wl + d.s[q]) * d.fmzf[q];
-    }
-  };
-  double wlo_d = 0.0;
+  ST wlo_d = 0;
   T wlo = T(0);
-#pragma unroll 2
+  // finalize inputs of level m
+  struct Fin { T zd, fmz, qv, qc, tet, qwl, qwi, pai, s, fmzf; };
+  auto load_fin = [&](int m) {
+    const size_t q = (size_t)m * pl;
+    Fin f;
+    f.zd = ZD[q]; f.fmz = FMZ[q]; f.qv = QV[q]; f.qc = QC[q]; f.tet = TET[q];
+    f.qwl = QWL[q]; f.qwi = QWI[q]; f.pai = PAI[q];
+    f.s = last ? S[q] : T(0);
+    f.fmzf = last ? FMZF[q] : T(0);
+    return f;
+  };
+  auto finalize = [&](int m, const Fin& f, T wl, T wh) {
+    const size_t q = (size_t)m * pl;
+    T zd = f.zd;
+    zd = zd + (dtrdz * f.fmz) * (wl - wh);
+    zd = (zd * ((T(1) + T(0.86) * f.qv) + T(3.2) * f.qc)) / ((T(1) + T(0.96) * f.qv) + T(4.8) * f.qc);
+    TET[q] = f.tet * (T(1) + (rdrcv * zd) * ((T(0.25) * f.qv + T(4.2) * f.qwl) + T(2.1) * f.qwi));
+    if (defer_pai) {
+      ZD[q] = zd;
+    } else {
+      if (jj == nj - 1) d.ep_j[ii + (size_t)ni * m] = f.pai;
+      if (ii == ni - 1) d.ep_i[jj + (size_t)nj * m] = f.pai;
+      PAI[q] = f.pai * (T(1) - rdrcv * zd);
+    }
+    if (last) S[q] = m == 0 ? T(0) : (wl + f.s) * f.fmzf;  // complete Equation 10 (:843-849)
+  };
+  Fin fin = load_fin(0);
+  ST n_wp = WPs[pl], n_ww = WWs[pl];
+  T n_wold = W[pl];
   for (int kk = 1; kk < kz; ++kk) {
-    const size_t q = c + (size_t)kk * pl;
-    wlo_d = d.wp[q] + d.wwkw[q] * wlo_d;
+    const size_t q = (size_t)kk * pl;
+    const ST wpk = n_wp, wwk = n_ww;
+    const T wold = n_wold;
+    const Fin cur = fin;
+    fin = load_fin(kk);  // level kk is finalized in the next iteration
+    if (kk + 1 < kz) {
+      n_wp = WPs[q + pl]; n_ww = WWs[q + pl]; n_wold = W[q + pl];
+    }
+    wlo_d = wpk + wwk * wlo_d;
     const T wn = (T)wlo_d;
-    const T wold = d.w[q];
-    d.deltaw[q] = (-wold) + wn;
-    d.w[q] = wn;
-    finalize(kk - 1, wlo, wn);
+    DW[q] = (-wold) + wn;
+    W[q] = wn;
+    finalize(kk - 1, cur, wlo, wn);
     wlo = wn;
   }
-  finalize(kz - 1, wlo, wsurf);
-  if (last) d.s[c + (size_t)kz * pl] = T(0);
+  finalize(kz - 1, fin, wlo, wsurf);
+  if (last) S[(size_t)kz * pl] = T(0);
 }
+
 // ---- 5-point Laplacian filter of one field, out of place ----------------
 // out = a + coef(k) * (0.125*(aW+aE+aS+aN) - 0.5*a)   (:423-481)
 // coef(k) = anu2 * xknu(k) when use_xknu, else the constant c0.
@@ -538,100 +581,93 @@ __global__ void __launch_bounds__(kColBX* kColBY) k_waf_vertical(View<T> d, Fiel
   }
 }
 
-// ---- advection: meridional + zonal WAF of one level (:1075-1187) -------
-// Block = 32 (j) x 8 (i) output points of one level, ten fields in turn.
-// Per field: the wz tile with a 2-point halo in both directions and the pp
-// tile go to shared memory; the meridional fluxes and p0 are formed for the
-// 36-wide strip the zonal step needs, then the zonal fluxes and the new pp.
-// p0 never leaves the SM.  The result is written to the other field buffer
-// (dst): neighbouring blocks still read the old pp at their halo columns.
+// ---- advection: meridional + zonal WAF (:1075-1187) ----------------------
+// Block = 32 (j) x 8 (i) output points of kHzLevels consecutive levels, ten
+// fields per level.  Per field: the wz tile with a 2-point halo in both
+// directions and the pp tile go to shared memory; the meridional fluxes and
+// p0 are formed for the 36-wide strip the zonal step needs, then the zonal
+// fluxes and the new pp.  p0 never leaves the SM.  The next field's tiles
+// travel in registers while the current one is computed.  The result goes to
+// the other field buffer (dst): neighbouring blocks still read the old pp at
+// their halo columns.  The wrapped (periodic) tile offsets are computed once
+// per block and reused for every level and field; d.hz_levels (levels per
+// block) is picked by the autotuner (moloch_gpu_autotune).
+
+// WAF flux between cells m1 and x0 (limiter from m2, p1), the reference's
+// expression (:1091-1106, :1148-1163)
 template <class T>
-__global__ void __launch_bounds__(256) k_waf_horizontal(View<T> d, FieldPtrs<T> src, FieldPtrs<T> dst) {
+__device__ __forceinline__ T waf_hflux(T zamu, T m2, T m1, T x0, T p1) {
+  T is, num;
+  if (zamu > T(0)) {
+    is = T(1); num = m1 - m2;   // ih = i-1, ihm1 = i-2
+  } else {
+    is = T(-1); num = p1 - x0;  // ih = i+1, ihm1 = i
+  }
+  const T rr = qdiv(num, safeden(x0 - m1));
+  const T bb = superbee(rr);
+  const T zphi = (is + zamu * bb) - is * bb;
+  return (T(1) + zphi) * m1 + (T(1) - zphi) * x0;
+}
+
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(View<T> d, FieldPtrs<T> src, FieldPtrs<T> dst) {
   constexpr int TJ = 32, TI = 8, HJ = TJ + 4, HI = TI + 4;
   constexpr int NW = HI * HJ, NP = TI * HJ, NM = (TI + 1) * HJ, NZ = TI * (TJ + 1);
-  __shared__ T sw[2][HI][HJ];    // wz, rows i0-2.., cols j0-2.. (two fields in flight)
-  __shared__ T sp[2][TI][HJ];    // pp (old), rows i0.., cols j0-2..
-  __shared__ T smf[TI + 1][HJ];  // meridional fluxes at rows i0..i0+TI
-  __shared__ T sp0[TI][HJ];      // p0
-  __shared__ T szf[TI][TJ + 1];  // zonal fluxes at cols j0..j0+TJ
+  // flat row-major tiles: a work item's linear number q is its own index
+  __shared__ T sw[2][NW];  // wz, rows i0-2 .. i0+TI+1, cols j0-2 .. j0+TJ+1
+  __shared__ T sp[2][NP];  // pp (old), rows i0 .., cols j0-2 ..
+  __shared__ T smf[NM];    // meridional fluxes at rows i0 .. i0+TI
+  __shared__ T sp0[NP];    // p0
+  __shared__ T szf[NZ];    // zonal fluxes at cols j0 .. j0+TJ
   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
-  const int nj = d.nj, ni = d.ni, kz = d.kz;
-  const size_t pl = d.pl;
-  const int j0 = blockIdx.x * TJ, i0 = blockIdx.y * TI, kk = blockIdx.z;
-  const size_t ko = (size_t)kk * pl;
+  const int nj = d.nj, ni = d.ni, kz = d.kz, pl = d.pl;
+  const int j0 = blockIdx.x * TJ, i0 = blockIdx.y * TI;
+  const int k0 = blockIdx.z * d.hz_levels;
+  const int k1 = min(k0 + d.hz_levels, kz);
   const T* __restrict__ u = d.ubuf[d.cur];
   const T* __restrict__ v = d.vbuf[d.cur];
   const T dtrdx = d.dtrdx_a, dtrdy = d.dtrdy_a;
   const int rot = d.rotllr;
 
-  // field-independent terms of the points this thread owns
-  T mz[2], mfac[2];  // meridional flux points: zamu and the factor of fl
+  // ---- per block: wrapped offsets (valid for every level) and map factors
+  int woff[2], poff[2], pnoff[2], zoffg[2], zoff[2];
+  T mrm[2], prs[2], prn[2], pmx[2], zm[2];
   for (int n = 0; n < 2; ++n) {
     const int q = tid + 256 * n;
-    mz[n] = T(0); mfac[n] = T(0);
-    if (q < NM) {
-      const int r = q / HJ, x = q % HJ;
-      const size_t cq = wrapn(j0 - 2 + x, nj) + (size_t)nj * wrapn(i0 + r, ni);
-      const T vv = v[ko + cq];
-      const T rm = d.rmv[cq];
-      mz[n] = rot ? vv * dtrdy : (vv * rm) * dtrdy;
-      mfac[n] = rot ? T(0.5) * vv : (T(0.5) * vv) * rm;
-    }
-  }
-  T pn[2], ps_[2], pdv[2], pmx[2];  // p0 points: zrfmn, zrfms, velocity-divergence factor, mx2
-  for (int n = 0; n < 2; ++n) {
-    const int q = tid + 256 * n;
-    pn[n] = ps_[n] = pdv[n] = pmx[n] = T(0);
-    if (q < NP) {
-      const int r = q / HJ, x = q % HJ;
-      const int jq = wrapn(j0 - 2 + x, nj), iq = wrapn(i0 + r, ni), iqn = wp1(iq, ni);
-      const size_t cq = jq + (size_t)nj * iq, cqn = jq + (size_t)nj * iqn;
-      const T zrfmn = d.wafn[ko + cq], zrfms = d.wafs[ko + cq];
-      const T vs = v[ko + cq], vn = v[ko + cqn];
-      pn[n] = zrfmn; ps_[n] = zrfms;
-      pdv[n] = rot ? (vn * zrfmn - vs * zrfms) : ((vn * d.rmv[cqn]) * zrfmn - (vs * d.rmv[cq]) * zrfms);
-      pmx[n] = d.mx2[cq];
-    }
-  }
-  T zz[2], zfac[2];  // zonal flux points
-  for (int n = 0; n < 2; ++n) {
-    const int q = tid + 256 * n;
-    zz[n] = T(0); zfac[n] = T(0);
-    if (q < NZ) {
-      const int r = q / (TJ + 1), x = q % (TJ + 1);
-      const size_t cq = wrapn(j0 + x, nj) + (size_t)nj * wrapn(i0 + r, ni);
-      const T uu = u[ko + cq];
-      const T m = rot ? d.mu[cq] : d.rmu[cq];
-      zz[n] = (uu * m) * dtrdx;
-      zfac[n] = rot ? T(0.5) * uu : (T(0.5) * uu) * m;
-    }
+    const int jq = wrapn(j0 - 2 + q % HJ, nj);
+    woff[n] = q < NW ? jq + nj * wrapn(i0 - 2 + q / HJ, ni) : 0;
+    const int iq = wrapn(i0 + q / HJ, ni);  // meridional flux rows and p0 rows
+    poff[n] = q < NM ? jq + nj * iq : 0;
+    pnoff[n] = q < NP ? jq + nj * wp1(iq, ni) : 0;
+    const int r = q / (TJ + 1), x = q % (TJ + 1);
+    zoff[n] = q < NZ ? r * HJ + x : 0;
+    zoffg[n] = q < NZ ? wrapn(j0 + x, nj) + nj * wrapn(i0 + r, ni) : 0;
   }
   const int jo = j0 + tx, io = i0 + ty;
   const bool ook = jo < nj && io < ni;
-  T oe = T(0), ow = T(0), odv = T(0), omx = T(0);
-  size_t co = 0;
-  if (ook) {
-    co = jo + (size_t)nj * io;
-    const size_t coe = wp1(jo, nj) + (size_t)nj * io;
-    oe = d.wafe[ko + co]; ow = d.wafw[ko + co];
-    const T uw = u[ko + co], ue = u[ko + coe];
-    odv = rot ? (ue * oe - uw * ow) : ((ue * d.rmu[coe]) * oe - (uw * d.rmu[co]) * ow);
-    omx = d.mx2[co];
-  }
+  const int co = ook ? jo + nj * io : 0;
+  const int coe = ook ? wp1(jo, nj) + nj * io : 0;
+  const int op0 = ty * HJ + tx + 2, ozf = ty * (TJ + 1) + tx;
 
-  // wrapped tile offsets are the same for every field: compute them once
-  int woff[2], poff[2];
-  for (int n = 0; n < 2; ++n) {
-    const int q = tid + 256 * n;
-    woff[n] = q < NW ? wrapn(j0 - 2 + q % HJ, nj) + nj * wrapn(i0 - 2 + q / HJ, ni) : 0;
-    poff[n] = q < NP ? wrapn(j0 - 2 + q % HJ, nj) + nj * wrapn(i0 + q / HJ, ni) : 0;
-  }
-  // double-buffered tiles; the next field's values travel in registers
-  // while the current field is computed
+  // raw per-level inputs (velocities, metric factors), loaded one level ahead
+  T rv[2], rwn[2], rws[2], rvn[2], ru[2], rwe = T(0), rww = T(0), ruw = T(0), rue = T(0);
+  auto fetch_level = [&](int k) {
+    const size_t ko = (size_t)k * pl;
+    for (int n = 0; n < 2; ++n) {
+      const int q = tid + 256 * n;
+      rv[n] = q < NM ? v[ko + poff[n]] : T(0);
+      rwn[n] = q < NP ? d.wafn[ko + poff[n]] : T(0);
+      rws[n] = q < NP ? d.wafs[ko + poff[n]] : T(0);
+      rvn[n] = q < NP ? v[ko + pnoff[n]] : T(0);
+      ru[n] = q < NZ ? u[ko + zoffg[n]] : T(0);
+    }
+    rwe = d.wafe[ko + co]; rww = d.wafw[ko + co];
+    ruw = u[ko + co]; rue = u[ko + coe];
+  };
   T rw[2], rp[2];
-  auto fetch = [&](int f) {
-    const T* __restrict__ wzf = d.wz + (size_t)f * pl * kz + ko;
-    const T* __restrict__ ppf = src.f[f] + ko;
+  auto fetch = [&](int k, int f) {
+    const T* __restrict__ wzf = d.wz + ((size_t)f * kz + k) * pl;
+    const T* __restrict__ ppf = src.f[f] + (size_t)k * pl;
     for (int n = 0; n < 2; ++n) {
       const int q = tid + 256 * n;
       rw[n] = q < NW ? wzf[woff[n]] : T(0);
@@ -641,71 +677,85 @@ __global__ void __launch_bounds__(256) k_waf_horizontal(View<T> d, FieldPtrs<T> 
   auto stash = [&](int b) {
     for (int n = 0; n < 2; ++n) {
       const int q = tid + 256 * n;
-      if (q < NW) sw[b][q / HJ][q % HJ] = rw[n];
-      if (q < NP) sp[b][q / HJ][q % HJ] = rp[n];
+      if (q < NW) sw[b][q] = rw[n];
+      if (q < NP) sp[b][q] = rp[n];
     }
   };
-  fetch(0);
+  fetch_level(k0);
+  fetch(k0, 0);
+  for (int n = 0; n < 2; ++n) {
+    const int q = tid + 256 * n;
+    mrm[n] = q < NM ? d.rmv[poff[n]] : T(1);
+    prs[n] = q < NP ? d.rmv[poff[n]] : T(1);
+    prn[n] = q < NP ? d.rmv[pnoff[n]] : T(1);
+    pmx[n] = q < NP ? d.mx2[poff[n]] : T(0);
+    zm[n] = q < NZ ? (rot ? d.mu[zoffg[n]] : d.rmu[zoffg[n]]) : T(0);
+  }
+  const T ormw = d.rmu[co], orme = d.rmu[coe], omx = d.mx2[co];
   stash(0);
   __syncthreads();
-  for (int f = 0; f < kNumAdvected; ++f) {
-    const int b = f & 1;
-    if (f + 1 < kNumAdvected) fetch(f + 1);
-    for (int n = 0; n < 2; ++n) {  // zpby, flux between rows r+1 and r+2 of sw
-      const int q = tid + 256 * n;
-      if (q < NM) {
-        const int r = q / HJ, x = q % HJ;
-        const T zamu = mz[n];
-        T is, num;
-        if (zamu > T(0)) {
-          is = T(1); num = sw[b][r + 1][x] - sw[b][r][x];      // ih = i-1, ihm1 = i-2
-        } else {
-          is = T(-1); num = sw[b][r + 3][x] - sw[b][r + 2][x];  // ih = i+1, ihm1 = i
+  int b = 0;
+  for (int k = k0; k < k1; ++k) {
+    const size_t ko = (size_t)k * pl;
+    T mz[2], mfac[2], pn[2], ps_[2], pdv[2], zz[2], zfac[2];
+    for (int n = 0; n < 2; ++n) {
+      const T vv = rv[n];
+      mz[n] = rot ? vv * dtrdy : (vv * mrm[n]) * dtrdy;
+      mfac[n] = rot ? T(0.5) * vv : (T(0.5) * vv) * mrm[n];
+      const T zrfmn = rwn[n], zrfms = rws[n], vs = rv[n], vn = rvn[n];
+      pn[n] = zrfmn; ps_[n] = zrfms;
+      pdv[n] = rot ? (vn * zrfmn - vs * zrfms) : ((vn * prn[n]) * zrfmn - (vs * prs[n]) * zrfms);
+      const T uu = ru[n];
+      zz[n] = (uu * zm[n]) * dtrdx;
+      zfac[n] = rot ? T(0.5) * uu : (T(0.5) * uu) * zm[n];
+    }
+    const T oe = rwe, ow = rww;
+    const T odv = rot ? (rue * oe - ruw * ow) : ((rue * orme) * oe - (ruw * ormw) * ow);
+    for (int f = 0; f < kNumAdvected; ++f) {
+      const T* __restrict__ W = sw[b];
+      const T* __restrict__ P = sp[b];
+      const bool next_field = f + 1 < kNumAdvected;
+      const bool next_level = !next_field && k + 1 < k1;
+      if (next_field) fetch(k, f + 1);
+      if (next_level) {
+        fetch(k + 1, 0);
+        fetch_level(k + 1);
+      }
+      for (int n = 0; n < 2; ++n) {  // zpby between tile rows r+1 and r+2 (flat: q+HJ, q+2HJ)
+        const int q = tid + 256 * n;
+        if (q < NM)
+          smf[q] = mfac[n] * waf_hflux(mz[n], W[q], W[q + HJ], W[q + 2 * HJ], W[q + 3 * HJ]);
+      }
+      __syncthreads();
+      for (int n = 0; n < 2; ++n) {  // p0 (:1113-1131, :1222-1240)
+        const int q = tid + 256 * n;
+        if (q < NP) {
+          const T zdv = pdv[n] * P[q];
+          const T wc = W[q + 2 * HJ];
+          sp0[q] = rot ? ((wc + smf[q] * ps_[n]) - smf[q + HJ] * pn[n]) + zdv
+                       : wc + pmx[n] * (((smf[q] * ps_[n]) - smf[q + HJ] * pn[n]) + zdv);
         }
-        const T rr = qdiv(num, safeden(sw[b][r + 2][x] - sw[b][r + 1][x]));
-        const T bb = superbee(rr);
-        const T zphi = (is + zamu * bb) - is * bb;
-        smf[r][x] = mfac[n] * ((T(1) + zphi) * sw[b][r + 1][x] + (T(1) - zphi) * sw[b][r + 2][x]);
       }
-    }
-    __syncthreads();
-    for (int n = 0; n < 2; ++n) {  // p0 (:1113-1131, :1222-1240)
-      const int q = tid + 256 * n;
-      if (q < NP) {
-        const int r = q / HJ, x = q % HJ;
-        const T zdv = pdv[n] * sp[b][r][x];
-        sp0[r][x] = rot ? ((sw[b][r + 2][x] + smf[r][x] * ps_[n]) - smf[r + 1][x] * pn[n]) + zdv
-                        : sw[b][r + 2][x] + pmx[n] * (((smf[r][x] * ps_[n]) - smf[r + 1][x] * pn[n]) + zdv);
-      }
-    }
-    __syncthreads();
-    for (int n = 0; n < 2; ++n) {  // zpbw, flux between cols x+1 and x+2 of sp0
-      const int q = tid + 256 * n;
-      if (q < NZ) {
-        const int r = q / (TJ + 1), x = q % (TJ + 1);
-        const T zamu = zz[n];
-        T is, num;
-        if (zamu > T(0)) {
-          is = T(1); num = sp0[r][x + 1] - sp0[r][x];
-        } else {
-          is = T(-1); num = sp0[r][x + 3] - sp0[r][x + 2];
+      __syncthreads();
+      for (int n = 0; n < 2; ++n) {  // zpbw between sp0 cols x+1 and x+2
+        const int q = tid + 256 * n;
+        if (q < NZ) {
+          const int z0 = zoff[n];
+          szf[q] = zfac[n] * waf_hflux(zz[n], sp0[z0], sp0[z0 + 1], sp0[z0 + 2], sp0[z0 + 3]);
         }
-        const T rr = qdiv(num, safeden(sp0[r][x + 2] - sp0[r][x + 1]));
-        const T bb = superbee(rr);
-        const T zphi = (is + zamu * bb) - is * bb;
-        szf[r][x] = zfac[n] * ((T(1) + zphi) * sp0[r][x + 1] + (T(1) - zphi) * sp0[r][x + 2]);
       }
+      __syncthreads();
+      if (ook) {  // new pp (:1173-1187, :1283-1297)
+        const T p0 = sp0[op0];
+        const T zdv = odv * P[op0];
+        const T out = rot ? ((p0 + szf[ozf] * ow) - szf[ozf + 1] * oe) + zdv
+                          : p0 + omx * (((szf[ozf] * ow) - szf[ozf + 1] * oe) + zdv);
+        dst.f[f][ko + co] = out;
+      }
+      if (next_field || next_level) stash(b ^ 1);  // the other buffer was last read two fields ago
+      b ^= 1;
+      __syncthreads();
     }
-    __syncthreads();
-    if (ook) {  // new pp (:1173-1187, :1283-1297)
-      const T p0 = sp0[ty][tx + 2];
-      const T zdv = odv * sp[b][ty][tx + 2];
-      const T out = rot ? ((p0 + szf[ty][tx] * ow) - szf[ty][tx + 1] * oe) + zdv
-                        : p0 + omx * (((szf[ty][tx] * ow) - szf[ty][tx + 1] * oe) + zdv);
-      dst.f[f][ko + co] = out;
-    }
-    if (f + 1 < kNumAdvected) stash(b ^ 1);  // the other buffer was last read two fields ago
-    __syncthreads();
   }
 }
 
@@ -912,7 +962,7 @@ int launch_advection(View<T>& d, cudaStream_t st) {
   const FieldPtrs<T> src = field_set(d, d.fcur), dst = field_set(d, d.fcur ^ 1);
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
   const dim3 vg(((d.nj + kColBX - 1) / kColBX) * kNumAdvected, (d.ni + kColBY - 1) / kColBY);
-  const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, d.kz);
+  const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, (d.kz + d.hz_levels - 1) / d.hz_levels);
   MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pg, pb, 0, st>>>(d));
   MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<vg, dim3(kColBX, kColBY), 0, st>>>(d, src));
   MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_horizontal<T><<<hg, dim3(32, 8), 0, st>>>(d, src, dst));

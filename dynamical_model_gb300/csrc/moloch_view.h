@@ -105,6 +105,9 @@ struct View {
   T dtrdx_a, dtrdy_a, dtrdz_a;  // wafone: dta/dx, dta/dx, 0.5*dta/dzita
   T anu2;
 
+  // launch shape chosen by the autotuner: levels per k_waf_horizontal block
+  int hz_levels;
+
   // diagnostics
   double* dpart;  // per-block partial reductions
   double* dres;   // final reduction (device)

@@ -172,6 +172,18 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 int moloch_gpu_kernel_kinds(void);
 const char* moloch_gpu_kernel_name(int kind);
 
+/* Project-written autotuner.  Launch shapes that depend on the grid are
+ * timed with CUDA events on the handle's stream and the fastest is kept:
+ * choice[0] = levels per block of the horizontal WAF kernel (1, 2, 4, 8).
+ * moloch_gpu_autotune runs advection() once per candidate and repeat, so it
+ * advances the model state: call it on a scratch handle or before the
+ * initial state is uploaded again.  The chosen values can be cached by the
+ * caller and applied to new handles with moloch_gpu_set_tuning.  No
+ * reference counterpart (the reference has no GPU launch shapes). */
+int moloch_gpu_tuning_count(void);
+int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int nchoice);
+int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int nchoice);
+
 /* WAF advection of ONE field by dt_adv seconds (the arithmetic of wafone,
  * nompi/mod_moloch.F90:929-1311) that allocates no device memory.  It has
  * no counterpart in the reference: it exists for callers that own all
