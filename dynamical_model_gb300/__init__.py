@@ -14,7 +14,7 @@ import numpy as np
 
 from .build import LIB as _LIB_PATH, build as _build
 
-__all__ = ["Moloch", "MolochError", "Params", "Grid", "Diag", "Ideal", "lib", "FIELD",
+__all__ = ["Moloch", "Ensemble", "MolochError", "Params", "Grid", "Diag", "Ideal", "lib", "FIELD",
            "FP64", "FP64_EXACT", "FP32_MIXED", "field_bounds"]
 
 FP64, FP64_EXACT, FP32_MIXED = 0, 1, 2
@@ -92,6 +92,14 @@ _PROTOS = {
     "moloch_gpu_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
                                            ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "moloch_gpu_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+    "moloch_gpu_ensemble_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p),
+                                                  ctypes.POINTER(ctypes.c_void_p)]),
+    "moloch_gpu_ensemble_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
+    "moloch_gpu_ensemble_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                                                    ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
+    "moloch_gpu_ensemble_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
+    "moloch_gpu_ensemble_kernel_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "moloch_gpu_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
                                   [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
 }
@@ -287,3 +295,45 @@ class Moloch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Ensemble:
+    """Members (Moloch handles on one stream) advanced together: one batched
+    launch per kernel over all members, one CUDA graph per ensemble step."""
+
+    def __init__(self, members):
+        self.L = lib()
+        self.members = list(members)
+        arr = (ctypes.c_void_p * len(self.members))(*[m.h.value for m in self.members])
+        h = ctypes.c_void_p()
+        _check(self.L.moloch_gpu_ensemble_create(len(self.members), arr, ctypes.byref(h)))
+        self.h = h
+
+    def run(self, nsteps, graph=True):
+        _check(self.L.moloch_gpu_ensemble_run(self.h, nsteps, int(graph)))
+
+    def autotune(self):
+        n = self.L.moloch_gpu_tuning_count()
+        ch = (ctypes.c_int * n)()
+        ms = (ctypes.c_double * n)()
+        _check(self.L.moloch_gpu_ensemble_autotune(self.h, ch, ms, n))
+        return list(ch)
+
+    def set_tuning(self, choice):
+        arr = (ctypes.c_int * len(choice))(*choice)
+        _check(self.L.moloch_gpu_ensemble_set_tuning(self.h, arr, len(choice)))
+
+    @property
+    def kernel_count(self):
+        return self.L.moloch_gpu_ensemble_kernel_count(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.moloch_gpu_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

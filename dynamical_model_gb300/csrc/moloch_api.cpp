@@ -876,6 +876,246 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   return moloch_gpu_set_tuning(h, choice, kTuneCount);
 }
 
+// ---- ensembles --------------------------------------------------------------
+}  // extern "C"
+
+struct moloch_ensemble {
+  std::vector<moloch_handle*> m;
+  int elem = 4;
+  cudaStream_t stream = nullptr;
+  void* dev = nullptr;  // views + tile tables
+  Batch<double> bd{};
+  Batch<float> bf{};
+  std::vector<int4> tiles[TK_COUNT];
+  cudaGraph_t graph[2] = {nullptr, nullptr};
+  cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+  int hz_levels = 4;
+  int cur = 0, fcur = 0;
+  long long kernels = 0;
+  int kernels_per_step = 0;
+  PhaseFlags fl{};
+};
+
+namespace {
+
+void ens_drop_graphs(moloch_ensemble* e) {
+  for (int q = 0; q < 2; ++q) {
+    if (e->gexec[q]) { cudaGraphExecDestroy(e->gexec[q]); e->gexec[q] = nullptr; }
+    if (e->graph[q]) { cudaGraphDestroy(e->graph[q]); e->graph[q] = nullptr; }
+  }
+}
+
+// Tile tables of every kernel kind over all members.  Column-like tiles are
+// ordered by decreasing work (kz, then member) so the longest blocks start
+// first and the tail of each launch stays short.
+void ens_tiles(moloch_ensemble* e) {
+  for (int t = 0; t < TK_COUNT; ++t) e->tiles[t].clear();
+  const int n = (int)e->m.size();
+  std::vector<int> order(n);
+  for (int q = 0; q < n; ++q) order[q] = q;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return e->m[a]->kz() > e->m[b]->kz(); });
+  for (int q : order) {
+    const int nj = e->m[q]->nj(), ni = e->m[q]->ni(), kz = e->m[q]->kz();
+    const int tj = (nj + 31) / 32;
+    for (int z = 0; z < kz; ++z)
+      for (int y = 0; y < (ni + 7) / 8; ++y)
+        for (int x = 0; x < tj; ++x) e->tiles[TK_POINT].push_back(make_int4(q, x, y, z));
+    for (int y = 0; y < (ni + 3) / 4; ++y)
+      for (int x = 0; x < tj; ++x) e->tiles[TK_COLUMN].push_back(make_int4(q, x, y, 0));
+    for (int y = 0; y < (ni + 3) / 4; ++y)
+      for (int x = 0; x < tj * kNumAdvected; ++x) e->tiles[TK_VERTICAL].push_back(make_int4(q, x, y, 0));
+    const int hz = std::min(e->hz_levels, kz);
+    for (int z = 0; z < (kz + hz - 1) / hz; ++z)
+      for (int y = 0; y < (ni + 7) / 8; ++y)
+        for (int x = 0; x < tj; ++x) e->tiles[TK_HORIZONTAL].push_back(make_int4(q, x, y, z));
+  }
+}
+
+// upload views (4 parities x members) and tile tables into one device block
+template <class T>
+int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
+  const int n = (int)e->m.size();
+  size_t bytes = 4 * n * sizeof(View<T>);
+  for (int t = 0; t < TK_COUNT; ++t) bytes += ((e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255));
+  if (e->dev) cudaFree(e->dev);
+  e->dev = nullptr;
+  CUDA_TRY(cudaMalloc(&e->dev, bytes + 1024));
+  std::vector<View<T>> hv(4 * (size_t)n);
+  for (int cur = 0; cur < 2; ++cur)
+    for (int fc = 0; fc < 2; ++fc)
+      for (int q = 0; q < n; ++q) {
+        View<T> v = e->m[q]->*vm;
+        v.cur = cur;
+        v.fcur = fc;
+        v.hz_levels = std::min(e->hz_levels, v.kz);
+        v.bind_fields();
+        hv[(size_t)(cur * 2 + fc) * n + q] = v;
+      }
+  char* p = (char*)e->dev;
+  CUDA_TRY(cudaMemcpy(p, hv.data(), hv.size() * sizeof(View<T>), cudaMemcpyHostToDevice));
+  for (int cur = 0; cur < 2; ++cur)
+    for (int fc = 0; fc < 2; ++fc) b.views[cur][fc] = (const View<T>*)(p + (size_t)(cur * 2 + fc) * n * sizeof(View<T>));
+  size_t off = ((4 * n * sizeof(View<T>)) + 255) & ~size_t(255);
+  for (int t = 0; t < TK_COUNT; ++t) {
+    CUDA_TRY(cudaMemcpy(p + off, e->tiles[t].data(), e->tiles[t].size() * sizeof(int4), cudaMemcpyHostToDevice));
+    b.tiles[t] = (const int4*)(p + off);
+    b.ntiles[t] = (int)e->tiles[t].size();
+    off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
+  }
+  return MOLOCH_OK;
+}
+
+int ens_build(moloch_ensemble* e) {
+  ens_drop_graphs(e);
+  ens_tiles(e);
+  return e->elem == 8 ? ens_upload(e, e->bd, &moloch_handle::vd) : ens_upload(e, e->bf, &moloch_handle::vf);
+}
+
+int ens_step_kernels(moloch_ensemble* e) {
+  return e->elem == 8 ? kfast::blaunch_step(e->bd, e->stream, e->fl, e->cur, e->fcur)
+                      : kfast::blaunch_step(e->bf, e->stream, e->fl, e->cur, e->fcur);
+}
+
+// members' own handles see the state the ensemble left them in
+void ens_sync_members(moloch_ensemble* e) {
+  for (auto* h : e->m) {
+    if (h->elem == 8) { h->vd.cur = e->cur; h->vd.fcur = e->fcur; h->vd.bind_fields(); }
+    else { h->vf.cur = e->cur; h->vf.fcur = e->fcur; h->vf.bind_fields(); }
+    for (int q = 0; q < 2; ++q) {  // member graphs captured for the other parity stay valid
+      (void)q;
+    }
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int moloch_gpu_ensemble_create(int n, moloch_handle_t* const* members, moloch_ensemble_t** out) {
+  g_err.clear();
+  if (n < 1 || !members || !out) return fail(MOLOCH_ERR_ARG, "need members");
+  *out = nullptr;
+  moloch_handle* h0 = members[0];
+  for (int q = 0; q < n; ++q) {
+    moloch_handle* h = members[q];
+    if (!h || !h->initialized) return fail(MOLOCH_ERR_STATE, "member %d not initialized", q);
+    if (h->prm.mode == MOLOCH_FP64_EXACT) return fail(MOLOCH_ERR_ARG, "ensembles run the FP64 or FP32-storage builds");
+    if (h->elem != h0->elem || h->prm.mo_nadv != h0->prm.mo_nadv || h->prm.mo_nsound != h0->prm.mo_nsound ||
+        h->prm.mo_divfilter != h0->prm.mo_divfilter || h->prm.do_filterpai || h->prm.do_filtertheta ||
+        h->stream != h0->stream)
+      return fail(MOLOCH_ERR_ARG, "member %d: mode, nadv, nsound, filters and stream must match (pai/theta filters unsupported)", q);
+    const int cur = h->elem == 8 ? h->vd.cur : h->vf.cur;
+    const int fc = h->elem == 8 ? h->vd.fcur : h->vf.fcur;
+    const int fc0 = h0->elem == 8 ? h0->vd.fcur : h0->vf.fcur;
+    if (cur != 0 || fc != fc0) return fail(MOLOCH_ERR_STATE, "member %d is at a different buffer parity", q);
+  }
+  moloch_ensemble* e = new moloch_ensemble();
+  e->m.assign(members, members + n);
+  e->elem = h0->elem;
+  e->stream = h0->stream;
+  e->fl = flags_of(h0);
+  e->fcur = h0->elem == 8 ? h0->vd.fcur : h0->vf.fcur;
+  int rc = ens_build(e);
+  if (rc) {
+    if (e->dev) cudaFree(e->dev);
+    delete e;
+    return rc;
+  }
+  *out = e;
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_ensemble_run(moloch_ensemble_t* e, int nsteps, int use_graph) {
+  g_err.clear();
+  if (!e) return fail(MOLOCH_ERR_ARG, "null ensemble");
+  for (int st = 0; st < nsteps; ++st) {
+    if (!use_graph) {
+      int n = ens_step_kernels(e);
+      e->kernels += n;
+      e->kernels_per_step = n;
+    } else {
+      const int par = e->fcur;
+      if (!e->gexec[par]) {
+        const int c0 = e->cur, f0 = e->fcur;
+        CUDA_TRY(cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        int n = ens_step_kernels(e);
+        cudaGraph_t g = nullptr;
+        cudaError_t err = cudaStreamEndCapture(e->stream, &g);
+        e->cur = c0; e->fcur = f0;
+        if (err != cudaSuccess) return fail(MOLOCH_ERR_CUDA, "ensemble capture: %s", cudaGetErrorString(err));
+        e->graph[par] = g;
+        CUDA_TRY(cudaGraphInstantiate(&e->gexec[par], g, 0));
+        e->kernels_per_step = n;
+      }
+      CUDA_TRY(cudaGraphLaunch(e->gexec[par], e->stream));
+      e->kernels += e->kernels_per_step;
+      e->fcur ^= (e->fl.nadv & 1);
+      e->cur = 0;
+    }
+    int rc = check_launch("ensemble step");
+    if (rc) return rc;
+  }
+  ens_sync_members(e);
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best_ms, int nchoice) {
+  g_err.clear();
+  if (!e || !choice || nchoice < kTuneCount) return fail(MOLOCH_ERR_ARG, "need %d choice slots", kTuneCount);
+  cudaEvent_t e0, e1;
+  CUDA_TRY(cudaEventCreate(&e0));
+  CUDA_TRY(cudaEventCreate(&e1));
+  double best = 1e30;
+  int pick = e->hz_levels;
+  for (int c = 0; c < 4; ++c) {
+    e->hz_levels = kTuneCandidates[0][c];
+    int rc = ens_build(e);
+    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, e->stream);
+      e->kernels += e->elem == 8 ? kfast::blaunch_advection(e->bd, e->stream, e->cur, e->fcur)
+                                 : kfast::blaunch_advection(e->bf, e->stream, e->cur, e->fcur);
+      cudaEventRecord(e1, e->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "ensemble autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best) { best = tot; pick = e->hz_levels; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  e->hz_levels = pick;
+  choice[0] = pick;
+  if (best_ms) best_ms[0] = best / 2.0;
+  ens_sync_members(e);
+  return ens_build(e);
+}
+
+int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int nchoice) {
+  g_err.clear();
+  if (!e || (nchoice > 0 && !choice)) return fail(MOLOCH_ERR_ARG, "null argument");
+  if (nchoice > 0) {
+    if (choice[0] < 1 || choice[0] > 64) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
+    e->hz_levels = choice[0];
+  }
+  return ens_build(e);
+}
+
+long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e) { return e ? e->kernels : -1; }
+
+int moloch_gpu_ensemble_destroy(moloch_ensemble_t* e) {
+  if (!e) return MOLOCH_OK;
+  cudaStreamSynchronize(e->stream);
+  ens_drop_graphs(e);
+  if (e->dev) cudaFree(e->dev);
+  delete e;
+  return MOLOCH_OK;
+}
+
 int moloch_internal_describe(moloch_handle_t* h, moloch_grid_t* g, moloch_params_t* p) {
   if (!h || !g || !p) return fail(MOLOCH_ERR_ARG, "null argument");
   *g = h->grid;

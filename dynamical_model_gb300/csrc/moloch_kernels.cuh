@@ -45,6 +45,16 @@ struct FieldPtrs {
   T* f[kNumAdvected];
 };
 
+// block-cooperative copy of a member's view into shared memory (batched kernels)
+template <class V>
+__device__ __forceinline__ void copy_view(V* dst, const V* __restrict__ src) {
+  static_assert(sizeof(V) % 4 == 0, "view size");
+  const int n = (int)(sizeof(V) / 4);
+  const int nt = blockDim.x * blockDim.y;
+  for (int q = threadIdx.x + blockDim.x * threadIdx.y; q < n; q += nt)
+    reinterpret_cast<int*>(dst)[q] = reinterpret_cast<const int*>(src)[q];
+}
+
 // ---- small device helpers ---------------------------------------------
 __device__ __forceinline__ int wm1(int x, int n) { return x == 0 ? n - 1 : x - 1; }
 __device__ __forceinline__ int wp1(int x, int n) { return x == n - 1 ? 0 : x + 1; }
@@ -101,11 +111,11 @@ __device__ __forceinline__ T pfwsat(T t, T p) {
 
 // ---- pre-diagnostics (:289-323) ----------------------------------------
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_prediag(View<T> d, int filterpai, int filtertheta) {
-  int jj = blockIdx.x * kPtBX + threadIdx.x;
-  int ii = blockIdx.y * kPtBY + threadIdx.y;
+__device__ __forceinline__ void b_prediag(const View<T>& d, const int bx, const int by, const int bz, int filterpai, int filtertheta) {
+  int jj = bx * kPtBX + threadIdx.x;
+  int ii = by * kPtBY + threadIdx.y;
   if (jj >= d.nj || ii >= d.ni) return;
-  size_t c = (size_t)jj + (size_t)d.nj * ii + (size_t)blockIdx.z * d.pl;
+  size_t c = (size_t)jj + (size_t)d.nj * ii + (size_t)bz * d.pl;
   T pai = d.pai[c], t = d.t[c];
   T qv = d.q[0][c], qc = d.q[1][c], qi = d.q[2][c], qr = d.q[3][c], qs = d.q[4][c];
   T p = dpow(pai, T(kCpovr)) * T(kP00);
@@ -121,15 +131,31 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_prediag(View<T> d, int filterp
   if (filtertheta) d.tf[c] = tet;
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_prediag(View<T> d, int filterpai, int filtertheta) {
+  b_prediag<T>(d, blockIdx.x, blockIdx.y, blockIdx.z, filterpai, filtertheta);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_prediag(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int filterpai, int filtertheta) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_prediag<T>(sv, t.y, t.z, t.w, filterpai, filtertheta);
+}
+
+
 // ---- sound: halo, surface w, s (Eq. 10), horizontal divergence (Eq. 16) ---
 // One thread per point.  Boundary threads also store the pre-divdamp u/v
 // edge values that the momentum step reads as the stale ud/vd halo ring
 // (:730-735); the bottom level computes w(kz+1) and s(kz+1) (:536-549).
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_div(View<T> d) {
-  const int jj = blockIdx.x * kPtBX + threadIdx.x;
-  const int ii = blockIdx.y * kPtBY + threadIdx.y;
-  const int kk = blockIdx.z;
+__device__ __forceinline__ void b_sound_div(const View<T>& d, const int bx, const int by, const int bz) {
+  const int jj = bx * kPtBX + threadIdx.x;
+  const int ii = by * kPtBY + threadIdx.y;
+  const int kk = bz;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
@@ -180,15 +206,31 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_div(View<T> d) {
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_div(View<T> d) {
+  b_sound_div<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_sound_div(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_sound_div<T>(sv, t.y, t.z, t.w);
+}
+
+
 // ---- sound: divdamp (:853-895) and the vertical s term (:627-630) -------
 // One thread per point: damps u and v in place (their halo edges already
 // hold the pre-damping values) and writes the divergence the implicit
 // solve starts from into zdiv2b.
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_damp(View<T> d) {
-  const int jj = blockIdx.x * kPtBX + threadIdx.x;
-  const int ii = blockIdx.y * kPtBY + threadIdx.y;
-  const int kk = blockIdx.z;
+__device__ __forceinline__ void b_sound_damp(const View<T>& d, const int bx, const int by, const int bz) {
+  const int jj = bx * kPtBX + threadIdx.x;
+  const int ii = by * kPtBY + threadIdx.y;
+  const int kk = bz;
   const int nj = d.nj, ni = d.ni;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
@@ -213,6 +255,22 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_damp(View<T> d) {
   d.zdiv2b[c + o] = zd;
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_damp(View<T> d) {
+  b_sound_damp<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_sound_damp(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_sound_damp<T>(sv, t.y, t.z, t.w);
+}
+
+
 // Reciprocal of a Thomas pivot.  FP64 build: the IEEE quotient, as the
 // reference.  FP32-storage build: an FP32 estimate refined by one FP64
 // Newton step (relative error ~1e-14) -- the pivot stays FP64 while the
@@ -234,10 +292,9 @@ template <> __device__ __forceinline__ double pivot_rcp<float>(double den) {
 // with the Exner/theta/pai update of the level above it.
 // defer_pai: leave zdiv2b final and pai to k_pai_update (divergence filter on).
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
-    k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
-  const int jj = blockIdx.x * kColBX + threadIdx.x;
-  const int ii = blockIdx.y * kColBY + threadIdx.y;
+__device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, const int by, const int bz, int nsound, int last, int defer_pai) {
+  const int jj = bx * kColBX + threadIdx.x;
+  const int ii = by * kColBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
@@ -373,32 +430,66 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
   if (last) S[(size_t)kz * pl] = T(0);
 }
 
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4) k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
+  b_sound_column<T>(d, blockIdx.x, blockIdx.y, blockIdx.z, nsound, last, defer_pai);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
+    kb_sound_column(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int nsound, int last, int defer_pai) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_sound_column<T>(sv, t.y, t.z, t.w, nsound, last, defer_pai);
+}
+
+
 // ---- 5-point Laplacian filter of one field, out of place ----------------
 // out = a + coef(k) * (0.125*(aW+aE+aS+aN) - 0.5*a)   (:423-481)
 // coef(k) = anu2 * xknu(k) when use_xknu, else the constant c0.
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY)
-    k_lap_filter(View<T> d, const T* __restrict__ a, T* __restrict__ out, int use_xknu, T c0) {
-  int jj = blockIdx.x * kPtBX + threadIdx.x;
-  int ii = blockIdx.y * kPtBY + threadIdx.y;
+__device__ __forceinline__ void b_lap_filter(const View<T>& d, const int bx, const int by, const int bz) {  const T* __restrict__ a = d.zdiv2b;
+  T* __restrict__ out = d.zdiv2a;
+
+  int jj = bx * kPtBX + threadIdx.x;
+  int ii = by * kPtBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni;
   if (jj >= nj || ii >= ni) return;
-  const size_t o = (size_t)blockIdx.z * d.pl;
+  const size_t o = (size_t)bz * d.pl;
   const size_t c = jj + (size_t)nj * ii;
   T aw = a[o + wm1(jj, nj) + (size_t)nj * ii], ae = a[o + wp1(jj, nj) + (size_t)nj * ii];
   T as = a[o + jj + (size_t)nj * wm1(ii, ni)], an = a[o + jj + (size_t)nj * wp1(ii, ni)];
   T ac = a[o + c];
   T p2d = T(0.125) * (((aw + ae) + as) + an) - T(0.5) * ac;
-  T coef = use_xknu ? d.anu2 * d.xknu[blockIdx.z] : c0;
+  const T coef = d.anu2 * d.xknu[bz];
   out[o + c] = ac + coef * p2d;
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_lap_filter(View<T> d) {
+  b_lap_filter<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_lap_filter(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_lap_filter<T>(sv, t.y, t.z, t.w);
+}
+
+
 // pai update with the nompi halo order (:716-728), split form
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_pai_update(View<T> d, const T* __restrict__ zd) {
-  int jj = blockIdx.x * kPtBX + threadIdx.x;
-  int ii = blockIdx.y * kPtBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kk = blockIdx.z;
+__device__ __forceinline__ void b_pai_update(const View<T>& d, const int bx, const int by, const int bz) {  const T* __restrict__ zd = d.zdiv2a;
+
+  int jj = bx * kPtBX + threadIdx.x;
+  int ii = by * kPtBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni, kk = bz;
   if (jj >= nj || ii >= ni) return;
   const size_t c = jj + (size_t)nj * ii + (size_t)kk * d.pl;
   const T pold = d.pai[c];
@@ -407,16 +498,34 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_pai_update(View<T> d, const T*
   d.pai[c] = pold * (T(1) - T(kRdrcv) * zd[c]);
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_pai_update(View<T> d) {
+  b_pai_update<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_pai_update(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_pai_update<T>(sv, t.y, t.z, t.w);
+}
+
+
 // filtpai / filttheta on the step increment (:333-353, :442-481):
 // x = a - ref; a = ((x + nupaitq * lap(x)) + ref), written to out
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY)
-    k_filter_increment(View<T> d, const T* __restrict__ a, const T* __restrict__ ref, T* __restrict__ out) {
-  int jj = blockIdx.x * kPtBX + threadIdx.x;
-  int ii = blockIdx.y * kPtBY + threadIdx.y;
+__device__ __forceinline__ void b_filter_increment(const View<T>& d, const int bx, const int by, const int bz, int which) {  const T* __restrict__ a = which ? d.tetav : d.pai;
+  const T* __restrict__ ref = which ? d.tf : d.pf;
+  T* __restrict__ out = d.fscr;
+
+  int jj = bx * kPtBX + threadIdx.x;
+  int ii = by * kPtBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni;
   if (jj >= nj || ii >= ni) return;
-  const size_t o = (size_t)blockIdx.z * d.pl;
+  const size_t o = (size_t)bz * d.pl;
   auto X = [&](int j, int i) {
     size_t q = o + j + (size_t)nj * i;
     return a[q] - ref[q];
@@ -428,14 +537,30 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
   out[c] = (xc + T(kNupaitq) * p2d) + ref[c];
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_filter_increment(View<T> d, int which) {
+  b_filter_increment<T>(d, blockIdx.x, blockIdx.y, blockIdx.z, which);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_filter_increment(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int which) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_filter_increment<T>(sv, t.y, t.z, t.w, which);
+}
+
+
 // ---- sound: momentum, Equations 17 and 18 (:737-837) --------------------
 // One thread per point; reads u, v (current buffer, damped interior + the
 // pre-damping edges) and writes the other buffer of the pair.
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_momentum(View<T> d) {
-  const int jj = blockIdx.x * kPtBX + threadIdx.x;
-  const int ii = blockIdx.y * kPtBY + threadIdx.y;
-  const int kk = blockIdx.z;
+__device__ __forceinline__ void b_sound_momentum(const View<T>& d, const int bx, const int by, const int bz) {
+  const int jj = bx * kPtBX + threadIdx.x;
+  const int ii = by * kPtBY + threadIdx.y;
+  const int kk = bz;
   const int nj = d.nj, ni = d.ni;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
@@ -482,12 +607,28 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_momentum(View<T> d) {
     vo[c + o] = ((v[c + o] - zcor1v) - (zfz * d.hy[c]) * gzh) - (zcy * zrom1v) * (pc - pas);
   }
 }
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_sound_momentum(View<T> d) {
+  b_sound_momentum<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_sound_momentum(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_sound_momentum<T>(sv, t.y, t.z, t.w);
+}
+
 // ---- advection: staggered -> cross points (:1327-1341, :1389-1417) -----
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_to_x(View<T> d) {
-  int jj = blockIdx.x * kPtBX + threadIdx.x;
-  int ii = blockIdx.y * kPtBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz, kk = blockIdx.z;
+__device__ __forceinline__ void b_stag_to_x(const View<T>& d, const int bx, const int by, const int bz) {
+  int jj = bx * kPtBX + threadIdx.x;
+  int ii = by * kPtBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni, kz = d.kz, kk = bz;
   if (jj >= nj || ii >= ni) return;
   const T* __restrict__ u = d.ubuf[d.cur];
   const T* __restrict__ v = d.vbuf[d.cur];
@@ -510,6 +651,22 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_to_x(View<T> d) {
           T(0.0625) * (w[c + (kk + 2) * pl] + w[c + (kk - 1) * pl]);
   d.wx[o + c] = wxv;
 }
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_to_x(View<T> d) {
+  b_stag_to_x<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_stag_to_x(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_stag_to_x<T>(sv, t.y, t.z, t.w);
+}
+
 
 // ---- advection: vertical WAF, two passes at dt/2 (:966-1073) ------------
 // wfw(k+1) of one pass from x(max(k-1,1)), x(k), x(k+1), x(min(k+2,kz))
@@ -534,16 +691,16 @@ __device__ __forceinline__ T waf_vflux(T s_k1, T dtrdz, T xm, T x0, T x1, T x2) 
 // index fastest, so the ten fields of one column tile run together and
 // share the s / metric loads through L2.
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY) k_waf_vertical(View<T> d, FieldPtrs<T> fp) {
-  const int f = blockIdx.x % kNumAdvected;
-  const int tj = blockIdx.x / kNumAdvected;
+__device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, const int by, const int bz) {
+  const int f = bx % kNumAdvected;
+  const int tj = bx / kNumAdvected;
   const int jj = tj * kColBX + threadIdx.x;
-  const int ii = blockIdx.y * kColBY + threadIdx.y;
+  const int ii = by * kColBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
   const size_t c = jj + (size_t)nj * ii;
-  const T* __restrict__ src = fp.f[f];
+  const T* __restrict__ src = d.fset[d.fcur][f];
   T* __restrict__ wz = d.wz + (size_t)f * pl * kz;
   const T* __restrict__ s = d.s;
   const T* __restrict__ wafu = d.wafu;
@@ -581,6 +738,22 @@ __global__ void __launch_bounds__(kColBX* kColBY) k_waf_vertical(View<T> d, Fiel
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY) k_waf_vertical(View<T> d) {
+  b_waf_vertical<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY)
+    kb_waf_vertical(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_waf_vertical<T>(sv, t.y, t.z, t.w);
+}
+
+
 // ---- advection: meridional + zonal WAF (:1075-1187) ----------------------
 // Block = 32 (j) x 8 (i) output points of kHzLevels consecutive levels, ten
 // fields per level.  Per field: the wz tile with a 2-point halo in both
@@ -610,7 +783,7 @@ __device__ __forceinline__ T waf_hflux(T zamu, T m2, T m1, T x0, T p1) {
 }
 
 template <class T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(View<T> d, FieldPtrs<T> src, FieldPtrs<T> dst) {
+__device__ __forceinline__ void b_waf_horizontal(const View<T>& d, const int bx, const int by, const int bz) {
   constexpr int TJ = 32, TI = 8, HJ = TJ + 4, HI = TI + 4;
   constexpr int NW = HI * HJ, NP = TI * HJ, NM = (TI + 1) * HJ, NZ = TI * (TJ + 1);
   // flat row-major tiles: a work item's linear number q is its own index
@@ -621,8 +794,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(
   __shared__ T szf[NZ];    // zonal fluxes at cols j0 .. j0+TJ
   const int tx = threadIdx.x, ty = threadIdx.y, tid = tx + 32 * ty;
   const int nj = d.nj, ni = d.ni, kz = d.kz, pl = d.pl;
-  const int j0 = blockIdx.x * TJ, i0 = blockIdx.y * TI;
-  const int k0 = blockIdx.z * d.hz_levels;
+  const int j0 = bx * TJ, i0 = by * TI;
+  const int k0 = bz * d.hz_levels;
   const int k1 = min(k0 + d.hz_levels, kz);
   const T* __restrict__ u = d.ubuf[d.cur];
   const T* __restrict__ v = d.vbuf[d.cur];
@@ -667,7 +840,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(
   T rw[2], rp[2];
   auto fetch = [&](int k, int f) {
     const T* __restrict__ wzf = d.wz + ((size_t)f * kz + k) * pl;
-    const T* __restrict__ ppf = src.f[f] + (size_t)k * pl;
+    const T* __restrict__ ppf = d.fset[d.fcur][f] + (size_t)k * pl;
     for (int n = 0; n < 2; ++n) {
       const int q = tid + 256 * n;
       rw[n] = q < NW ? wzf[woff[n]] : T(0);
@@ -750,7 +923,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(
         const T zdv = odv * P[op0];
         const T out = rot ? ((p0 + szf[ozf] * ow) - szf[ozf + 1] * oe) + zdv
                           : p0 + omx * (((szf[ozf] * ow) - szf[ozf + 1] * oe) + zdv);
-        dst.f[f][ko + co] = out;
+        d.fset[d.fcur ^ 1][f][ko + co] = out;
       }
       if (next_field || next_level) stash(b ^ 1);  // the other buffer was last read two fields ago
       b ^= 1;
@@ -759,13 +932,29 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_waf_horizontal(View<T> d) {
+  b_waf_horizontal<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
+    kb_waf_horizontal(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_waf_horizontal<T>(sv, t.y, t.z, t.w);
+}
+
+
 // ---- advection: cross points -> staggered (:1343-1387) ------------------
 // Writes u, v into buffer 0 so every step replays the same pointers.
 template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_from_x(View<T> d) {
-  int jj = blockIdx.x * kPtBX + threadIdx.x;
-  int ii = blockIdx.y * kPtBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz, kk = blockIdx.z;
+__device__ __forceinline__ void b_stag_from_x(const View<T>& d, const int bx, const int by, const int bz) {
+  int jj = bx * kPtBX + threadIdx.x;
+  int ii = by * kPtBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni, kz = d.kz, kk = bz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
   const size_t o = (size_t)kk * pl;
@@ -792,12 +981,29 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_from_x(View<T> d) {
   }
 }
 
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_from_x(View<T> d) {
+  b_stag_from_x<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kPtBX* kPtBY)
+    kb_stag_from_x(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_stag_from_x<T>(sv, t.y, t.z, t.w);
+}
+
+
 // ---- post-diagnostics (:355-391), one thread per column ----------------
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY) k_postdiag(View<T> d, const T* __restrict__ zk,
-                                                            const T* __restrict__ zkm1) {
-  int jj = blockIdx.x * kColBX + threadIdx.x;
-  int ii = blockIdx.y * kColBY + threadIdx.y;
+__device__ __forceinline__ void b_postdiag(const View<T>& d, const int bx, const int by, const int bz) {  const T* __restrict__ zk = d.zeta + (size_t)d.pl * (d.kz - 1);
+  const T* __restrict__ zkm1 = d.zeta + (size_t)d.pl * (d.kz - 2);
+
+  int jj = bx * kColBX + threadIdx.x;
+  int ii = by * kColBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
@@ -824,6 +1030,22 @@ __global__ void __launch_bounds__(kColBX* kColBY) k_postdiag(View<T> d, const T*
   const T tv = tv_k - (T(0.5) * z) * lrt;
   d.ps[c] = p_k * dexp(zdgz / (T(kRgas) * tv));
 }
+
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY) k_postdiag(View<T> d) {
+  b_postdiag<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kColBX* kColBY)
+    kb_postdiag(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_postdiag<T>(sv, t.y, t.z, t.w);
+}
+
 
 // ---- diagnostics: max/min ps, u, v (:395-411) and FP64 column sums ------
 // partial record per block: maxps minps maxu minu maxv minv mass energy nonfinite
@@ -942,8 +1164,8 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
     n += 2;
     if (fl.divfilter) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 1));
-      MOLOCH_LAUNCH(KK_LAP_FILTER, st, k_lap_filter<T><<<pg, pb, 0, st>>>(d, d.zdiv2b, d.zdiv2a, 1, T(0)));
-      MOLOCH_LAUNCH(KK_PAI_UPDATE, st, k_pai_update<T><<<pg, pb, 0, st>>>(d, d.zdiv2a));
+      MOLOCH_LAUNCH(KK_LAP_FILTER, st, k_lap_filter<T><<<pg, pb, 0, st>>>(d));
+      MOLOCH_LAUNCH(KK_PAI_UPDATE, st, k_pai_update<T><<<pg, pb, 0, st>>>(d));
       n += 3;
     } else {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
@@ -959,13 +1181,12 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
 // one advection() call; the advected fields move to the other buffer set
 template <class T>
 int launch_advection(View<T>& d, cudaStream_t st) {
-  const FieldPtrs<T> src = field_set(d, d.fcur), dst = field_set(d, d.fcur ^ 1);
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
   const dim3 vg(((d.nj + kColBX - 1) / kColBX) * kNumAdvected, (d.ni + kColBY - 1) / kColBY);
   const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, (d.kz + d.hz_levels - 1) / d.hz_levels);
   MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pg, pb, 0, st>>>(d));
-  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<vg, dim3(kColBX, kColBY), 0, st>>>(d, src));
-  MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_horizontal<T><<<hg, dim3(32, 8), 0, st>>>(d, src, dst));
+  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<vg, dim3(kColBX, kColBY), 0, st>>>(d));
+  MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_horizontal<T><<<hg, dim3(32, 8), 0, st>>>(d));
   d.fcur ^= 1;
   d.bind_fields();
   MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pg, pb, 0, st>>>(d));
@@ -979,16 +1200,16 @@ int launch_postdiag(View<T>& d, cudaStream_t st, const PhaseFlags& fl, const T* 
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
   const size_t bytes = sizeof(T) * (size_t)d.pl * d.kz;
   if (fl.filterpai) {
-    MOLOCH_LAUNCH(KK_FILTER_INCREMENT, st, k_filter_increment<T><<<pg, pb, 0, st>>>(d, d.pai, d.pf, d.fscr));
+    MOLOCH_LAUNCH(KK_FILTER_INCREMENT, st, k_filter_increment<T><<<pg, pb, 0, st>>>(d, 0));
     cudaMemcpyAsync(d.pai, d.fscr, bytes, cudaMemcpyDeviceToDevice, st);
     ++n;
   }
   if (fl.filtertheta) {
-    MOLOCH_LAUNCH(KK_FILTER_INCREMENT, st, k_filter_increment<T><<<pg, pb, 0, st>>>(d, d.tetav, d.tf, d.fscr));
+    MOLOCH_LAUNCH(KK_FILTER_INCREMENT, st, k_filter_increment<T><<<pg, pb, 0, st>>>(d, 1));
     cudaMemcpyAsync(d.tetav, d.fscr, bytes, cudaMemcpyDeviceToDevice, st);
     ++n;
   }
-  MOLOCH_LAUNCH(KK_POSTDIAG, st, k_postdiag<T><<<col_grid(d.nj, d.ni), dim3(kColBX, kColBY), 0, st>>>(d, zk, zkm1));
+  MOLOCH_LAUNCH(KK_POSTDIAG, st, k_postdiag<T><<<col_grid(d.nj, d.ni), dim3(kColBX, kColBY), 0, st>>>(d));
   return n + 1;
 }
 
@@ -998,6 +1219,64 @@ int launch_diag(const View<T>& d, cudaStream_t st) {
   MOLOCH_LAUNCH(KK_DIAG, st, k_diag_partial<T><<<g, dim3(kColBX, kColBY), 0, st>>>(d));
   MOLOCH_LAUNCH(KK_DIAG, st, k_diag_final<<<1, 256, 0, st>>>(d.dpart, (int)(g.x * g.y), d.dres));
   return 2;
+}
+
+// ---- batched launchers (ensembles) --------------------------------------
+// One launch per phase covers every member; cur / fcur track the u/v buffer
+// and field-set parities exactly as the single-domain launchers do.
+template <class T>
+int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& cur, int& fcur) {
+  int n = 0;
+  const dim3 pb(kPtBX, kPtBY), cb(kColBX, kColBY), hb(32, 8);
+  auto V = [&]() { return b.views[cur][fcur]; };
+  const int4* PT = b.tiles[TK_POINT];
+  const int4* CO = b.tiles[TK_COLUMN];
+  const int4* VE = b.tiles[TK_VERTICAL];
+  const int4* HZ = b.tiles[TK_HORIZONTAL];
+  const int npt = b.ntiles[TK_POINT], nco = b.ntiles[TK_COLUMN];
+  const int nve = b.ntiles[TK_VERTICAL], nhz = b.ntiles[TK_HORIZONTAL];
+  MOLOCH_LAUNCH(KK_PREDIAG, st, kb_prediag<T><<<npt, pb, 0, st>>>(V(), PT, fl.filterpai, fl.filtertheta));
+  ++n;
+  for (int a = 0; a < fl.nadv; ++a) {
+    for (int ns = 1; ns <= fl.nsound; ++ns) {
+      const int last = ns == fl.nsound;
+      MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div<T><<<npt, pb, 0, st>>>(V(), PT));
+      MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp<T><<<npt, pb, 0, st>>>(V(), PT));
+      if (fl.divfilter) {
+        MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 1));
+        MOLOCH_LAUNCH(KK_LAP_FILTER, st, kb_lap_filter<T><<<npt, pb, 0, st>>>(V(), PT));
+        MOLOCH_LAUNCH(KK_PAI_UPDATE, st, kb_pai_update<T><<<npt, pb, 0, st>>>(V(), PT));
+        n += 2;
+      } else {
+        MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 0));
+      }
+      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum<T><<<npt, pb, 0, st>>>(V(), PT));
+      n += 4;
+      cur ^= 1;
+    }
+    MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<npt, pb, 0, st>>>(V(), PT));
+    MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T><<<nve, cb, 0, st>>>(V(), VE));
+    MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_horizontal<T><<<nhz, hb, 0, st>>>(V(), HZ));
+    fcur ^= 1;
+    MOLOCH_LAUNCH(KK_STAG_FROM_X, st, kb_stag_from_x<T><<<npt, pb, 0, st>>>(V(), PT));
+    cur = 0;
+    n += 4;
+  }
+  MOLOCH_LAUNCH(KK_POSTDIAG, st, kb_postdiag<T><<<nco, cb, 0, st>>>(V(), CO));
+  return n + 1;
+}
+
+// the advection phase alone, for the ensemble autotuner
+template <class T>
+int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur) {
+  const dim3 pb(kPtBX, kPtBY), cb(kColBX, kColBY), hb(32, 8);
+  MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
+  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T><<<b.ntiles[TK_VERTICAL], cb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_VERTICAL]));
+  MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_horizontal<T><<<b.ntiles[TK_HORIZONTAL], hb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_HORIZONTAL]));
+  fcur ^= 1;
+  MOLOCH_LAUNCH(KK_STAG_FROM_X, st, kb_stag_from_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
+  cur = 0;
+  return 4;
 }
 
 int diag_parts(int nj, int ni) {

@@ -20,5 +20,9 @@ namespace moloch {
   }
 MOLOCH_DECLARE_LAUNCHERS(kexact)
 MOLOCH_DECLARE_LAUNCHERS(kfast)
+namespace kfast {
+template <class T> int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& cur, int& fcur);
+template <class T> int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur);
+}
 #undef MOLOCH_DECLARE_LAUNCHERS
 }  // namespace moloch

@@ -146,6 +146,18 @@ struct KernelTimer {
   }
 };
 
+// Batched launch over the members of an ensemble.  Every batched kernel
+// takes a 1-D grid that walks a tile table of (member, bx, by, bz) entries
+// and reads the member's view from views[cur][fcur] (the u/v buffer and
+// field-set parities the step is at when the kernel runs).
+enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_COUNT };
+template <class T>
+struct Batch {
+  const View<T>* views[2][2];   // device arrays, one view per member
+  const int4* tiles[TK_COUNT];  // device tile tables
+  int ntiles[TK_COUNT];
+};
+
 // launch counts per phase are returned by the launchers so the API can
 // account for every kernel it starts
 struct PhaseFlags {

@@ -184,6 +184,28 @@ int moloch_gpu_tuning_count(void);
 int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int nchoice);
 int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int nchoice);
 
+/* ---- ensembles --------------------------------------------------------------
+ * Many domains of uneven size (jx, iy, kz may all differ) advanced together:
+ * each kernel of the step is ONE launch whose 1-D grid walks a table of
+ * (member, tile) entries over all members, heaviest column tiles first, and
+ * one step of the whole ensemble is one CUDA graph.  Members are ordinary
+ * handles created by the caller on the same stream with the same mode,
+ * mo_nadv, mo_nsound and filter switches (the theta/pai filters are not
+ * supported in ensembles), each initialized (setup_idealized or uploads +
+ * moloch_gpu_init).  After moloch_gpu_ensemble_run every member handle holds
+ * its advanced state (download, lprint via moloch_gpu_step, etc. work as for
+ * a single domain).  The reference runs one domain per process; these calls
+ * have no reference counterpart. */
+typedef struct moloch_ensemble moloch_ensemble_t;
+int moloch_gpu_ensemble_create(int nmembers, moloch_handle_t* const* members, moloch_ensemble_t** out);
+int moloch_gpu_ensemble_run(moloch_ensemble_t* e, int nsteps, int use_graph);
+/* event-timed choice of the launch shapes over the whole ensemble (advances
+ * the members' state); choice[0] = levels per horizontal WAF tile */
+int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best_ms, int nchoice);
+int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int nchoice);
+long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);
+int moloch_gpu_ensemble_destroy(moloch_ensemble_t* e);
+
 /* WAF advection of ONE field by dt_adv seconds (the arithmetic of wafone,
  * nompi/mod_moloch.F90:929-1311) that allocates no device memory.  It has
  * no counterpart in the reference: it exists for callers that own all
