@@ -100,6 +100,11 @@ _PROTOS = {
     "moloch_gpu_ensemble_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_ensemble_kernel_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "moloch_gpu_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_tc_gemm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_void_p]),
+    "moloch_tc_status": (ctypes.c_int, []),
     "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
                                   [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
 }

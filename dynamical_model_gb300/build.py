@@ -1,9 +1,10 @@
 """Build libmoloch_gb300.so in-tree for sm_103a.
 
-Five translation units compiled in parallel:
+Six translation units compiled in parallel:
   csrc/moloch_kernels_exact.cu  nvcc, FP64, --fmad=false (reference evaluation order)
   csrc/moloch_kernels_fast.cu   nvcc, FP64 + FP32, multiply-add contraction allowed
   csrc/moloch_noalloc.cu        nvcc, FP64, --fmad=false (allocation-free WAF entry point)
+  csrc/moloch_mlp.cu            nvcc, tcgen05 GEMM and the surrogate MLP kernels
   csrc/moloch_api.cpp           host C ABI, -ffp-contract=off
   csrc/moloch_ideal.cpp         host idealized-state generator, -ffp-contract=off
 """
@@ -59,6 +60,7 @@ def build(force=False, verbose=False):
                      "-o", os.path.join(BUILD, "kfast.o")],
         nv_common + ["--fmad=false", "-c", os.path.join(CSRC, "moloch_noalloc.cu"),
                      "-o", os.path.join(BUILD, "noalloc.o")],
+        nv_common + ["-c", os.path.join(CSRC, "moloch_mlp.cu"), "-o", os.path.join(BUILD, "mlp.o")],
         ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math"] + inc +
         ["-c", os.path.join(CSRC, "moloch_api.cpp"), "-o", os.path.join(BUILD, "api.o")],
         ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math"] + inc +
@@ -77,7 +79,7 @@ def build(force=False, verbose=False):
         raise RuntimeError("build failed:\n" + msg)
     tmp = LIB + ".tmp"
     link = [nvcc, ARCH, "-shared", "-o", tmp] + [os.path.join(BUILD, o) for o in
-                                                 ("kexact.o", "kfast.o", "noalloc.o", "api.o", "ideal.o")] + ["-lcudart"]
+                                                 ("kexact.o", "kfast.o", "noalloc.o", "mlp.o", "api.o", "ideal.o")] + ["-lcudart"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

@@ -206,6 +206,18 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
 long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);
 int moloch_gpu_ensemble_destroy(moloch_ensemble_t* e);
 
+/* ---- tensor-core GEMM (tcgen05) used by the acoustic-cycle surrogate --------
+ * C = act(A * B^T + bias) on device buffers: A [M][K] and B [N][K] BF16
+ * row-major (K contiguous), C [M][N] FP32 (ldc) and/or Cb BF16 (ldcb, holds
+ * act(...)); act 0 = identity, 1 = SiLU; bias may be NULL.  Requires
+ * N % 16 == 0, K % 64 == 0 and 16-byte aligned rows.  Accumulation is FP32
+ * in tensor memory.  No reference counterpart. */
+int moloch_tc_gemm(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
+                   const float* bias, int M, int N, int K, int act, void* stream);
+/* MOLOCH_ERR_TIMEOUT if a bounded tensor-core wait gave up since the last
+ * call (synchronises the device and clears the flag), else MOLOCH_OK. */
+int moloch_tc_status(void);
+
 /* WAF advection of ONE field by dt_adv seconds (the arithmetic of wafone,
  * nompi/mod_moloch.F90:929-1311) that allocates no device memory.  It has
  * no counterpart in the reference: it exists for callers that own all

@@ -1,0 +1,39 @@
+"""tcgen05 GEMM (BF16 operands, FP32 accumulation in tensor memory) against
+the FP32 product of the same BF16 values.  Tolerance: relative error of the
+whole matrix <= 1e-5 (only the summation order differs)."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 16, 64), (256, 256, 128), (300, 208, 1856), (1000, 256, 256),
+                                   (130, 512, 64)])
+@pytest.mark.parametrize("act", [0, 1])
+def test_tc_gemm(gpu_lib, M, N, K, act):
+    torch = pytest.importorskip("torch")
+    L = gpu_lib.lib()
+    g = torch.Generator(device="cpu").manual_seed(M + N + K)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    bias = torch.randn(N, generator=g).cuda()
+    C = torch.zeros(M, N, device="cuda")
+    Cb = torch.zeros(M, N, device="cuda", dtype=torch.bfloat16)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    rc = L.moloch_tc_gemm(P(A), K, P(B), K, P(C), N, P(Cb), N, P(bias), M, N, K, act, None)
+    assert rc == 0, L.moloch_gpu_last_error()
+    assert L.moloch_tc_status() == 0
+    ref = A.float() @ B.float().T + bias
+    err = (C - ref).norm() / ref.norm()
+    assert err.item() <= 1e-5, err.item()
+    refb = torch.nn.functional.silu(ref) if act == 1 else ref
+    errb = (Cb.float() - refb).norm() / refb.norm()
+    assert errb.item() <= 1e-2, errb.item()
+
+
+def test_tc_gemm_rejects_bad_shapes(gpu_lib):
+    L = gpu_lib.lib()
+    dummy = ctypes.c_void_p(16)
+    assert L.moloch_tc_gemm(dummy, 72, dummy, 72, dummy, 24, None, 0, None, 128, 24, 72, 0, None) == 1
