@@ -107,6 +107,25 @@ _PROTOS = {
     "moloch_tc_status": (ctypes.c_int, []),
     "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
                                   [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
+    "moloch_sur_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "moloch_sur_collect": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                          ctypes.c_ulonglong]),
+    "moloch_sur_pairs": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_sur_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_ulonglong]),
+    "moloch_sur_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong,
+                                        ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
+    "moloch_sur_attach": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float]),
+    "moloch_sur_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
+                                         ctypes.POINTER(ctypes.c_longlong)]),
+    "moloch_sur_param": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
+    "moloch_sur_gradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                            ctypes.POINTER(ctypes.c_float), ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_void_p]),
+    "moloch_sur_dims": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
+    "moloch_sur_stats": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_int]),
+    "moloch_sur_destroy": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
 _lib = None
@@ -336,6 +355,108 @@ class Ensemble:
         if getattr(self, "h", None):
             self.L.moloch_gpu_ensemble_destroy(self.h)
             self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Surrogate:
+    """Learned acoustic-cycle surrogate (per-column MLP on tcgen05): collect
+    training pairs from plain steps of an FP32-storage handle, train, attach.
+    While attached, every sound() call runs the MLP first and falls back to
+    the plain acoustic substeps when the on-device check rejects it."""
+
+    def __init__(self, kz, capacity=65536, batch=256, seed=1):
+        self.L = lib()
+        h = ctypes.c_void_p()
+        _check(self.L.moloch_sur_create(kz, capacity, batch, seed, ctypes.byref(h)))
+        self.h = h
+        self.attached = None
+
+    def dims(self):
+        d = (ctypes.c_int * 9)()
+        _check(self.L.moloch_sur_dims(self.h, d))
+        keys = ("kz", "nin", "kin", "nout", "nop", "hidden", "batch", "pairs", "ntrain")
+        return dict(zip(keys, list(d)))
+
+    def collect(self, model, nsteps, cols_per_cycle=512, seed=3):
+        _check(self.L.moloch_sur_collect(self.h, model.h, nsteps, cols_per_cycle, seed))
+        return self.L.moloch_sur_pairs(self.h)
+
+    def prepare(self, val_fraction=0.1, seed=5):
+        _check(self.L.moloch_sur_prepare(self.h, val_fraction, seed))
+
+    def train(self, iters, lr=1e-3, seed=7):
+        tl, vl = ctypes.c_float(), ctypes.c_float()
+        _check(self.L.moloch_sur_train(self.h, iters, lr, seed, ctypes.byref(tl), ctypes.byref(vl)))
+        return tl.value, vl.value
+
+    def attach(self, model, threshold=8.0):
+        _check(self.L.moloch_sur_attach(model.h, self.h, threshold))
+        self.attached = model
+
+    def detach(self):
+        if self.attached is not None and getattr(self.attached, "h", None):
+            _check(self.L.moloch_sur_attach(self.attached.h, None, 0.0))
+        self.attached = None
+
+    def counts(self):
+        c, f = ctypes.c_longlong(), ctypes.c_longlong()
+        _check(self.L.moloch_sur_counts(self.h, ctypes.byref(c), ctypes.byref(f)))
+        return c.value, f.value
+
+    def param(self, layer):
+        io = (ctypes.c_int * 2)()
+        _check(self.L.moloch_sur_param(self.h, layer, None, None, 0, io))
+        W = np.empty((io[1], io[0]), np.float32)
+        b = np.empty(io[1], np.float32)
+        _check(self.L.moloch_sur_param(self.h, layer, W.ctypes.data, b.ctypes.data, 0, io))
+        return W, b
+
+    def set_param(self, layer, W, b):
+        W = np.ascontiguousarray(W, np.float32)
+        b = np.ascontiguousarray(b, np.float32)
+        io = (ctypes.c_int * 2)()
+        _check(self.L.moloch_sur_param(self.h, layer, None, None, 0, io))
+        if W.shape != (io[1], io[0]) or b.shape != (io[1],):
+            raise ValueError(f"layer {layer} is {io[1]}x{io[0]}")
+        _check(self.L.moloch_sur_param(self.h, layer, W.ctypes.data, b.ctypes.data, 1, io))
+
+    def stats(self):
+        """(xmean, xstd, ymean, ystd), each [5, kz] (u, v, w, pai, tetav)."""
+        kz = self.dims()["kz"]
+        a = [np.empty((5, kz), np.float32) for _ in range(4)]
+        _check(self.L.moloch_sur_stats(self.h, *[x.ctypes.data for x in a], 0))
+        return tuple(a)
+
+    def set_stats(self, xmean, xstd, ymean, ystd):
+        kz = self.dims()["kz"]
+        a = [np.ascontiguousarray(np.broadcast_to(np.asarray(x, np.float32), (5, kz))) for x in
+             (xmean, xstd, ymean, ystd)]
+        _check(self.L.moloch_sur_stats(self.h, *[x.ctypes.data for x in a], 1))
+
+    def gradients(self, X, T, layer):
+        """(summed squared error, dW, db) of one forward+backward pass."""
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        W, _ = self.param(layer)
+        gW = np.empty_like(W)
+        gb = np.empty(W.shape[0], np.float32)
+        loss = ctypes.c_float()
+        _check(self.L.moloch_sur_gradients(self.h, X.ctypes.data, T.ctypes.data, X.shape[0], ctypes.byref(loss),
+                                           layer, gW.ctypes.data, gb.ctypes.data))
+        return loss.value, gW, gb
+
+    def close(self):
+        if getattr(self, "h", None):
+            try:
+                self.detach()
+            finally:
+                self.L.moloch_sur_destroy(self.h)
+                self.h = None
 
     def __del__(self):
         try:

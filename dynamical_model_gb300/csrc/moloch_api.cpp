@@ -23,6 +23,7 @@
 #include "../../include/moloch_gb300.h"
 #include "moloch_constants.h"
 #include "moloch_launch.h"
+#include "moloch_sur.h"
 #include "moloch_view.h"
 
 using namespace moloch;
@@ -162,6 +163,9 @@ struct moloch_handle {
   // host copies of the static inputs (dense interiors)
   std::vector<double> zeta, fmz, fmzf, msfx, msfu, msfv, hx, hy, ulat, vlat, zita, zitah;
   unsigned uploaded = 0;  // bit per field id
+  // attached acoustic-cycle surrogate (FP32 storage only): each sound()
+  // call first runs the surrogate; the plain substeps skip on acceptance
+  moloch::mlp::Surrogate* sur = nullptr;
   int nj() const { return grid.jx; }
   int ni() const { return grid.iy; }
   int kz() const { return grid.kz; }
@@ -225,6 +229,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.nj = h->nj(); v.ni = h->ni(); v.kz = h->kz(); v.pl = (int)pl; v.rotllr = h->prm.rotllr;
   v.cur = 0;
   v.hz_levels = 1;
+  v.sur_skip = nullptr;
   return off + 256;
 }
 
@@ -441,9 +446,12 @@ int launch_phase(moloch_handle* h, View<T>& v, int phase) {
       return n;
     }
   }
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (phase == 1 && h->sur) n += moloch::mlp::sur_cycle(h->sur, v, h->stream, fl.nsound);
+  }
   switch (phase) {
     case 0: n = kfast::launch_prediag<T>(v, h->stream, fl); break;
-    case 1: n = kfast::launch_sound<T>(v, h->stream, fl); break;
+    case 1: n += kfast::launch_sound<T>(v, h->stream, fl); break;
     case 2: n = kfast::launch_advection<T>(v, h->stream); break;
     case 3: n = kfast::launch_postdiag<T>(v, h->stream, fl, zk, zkm1); break;
     case 4: n = kfast::launch_diag<T>(v, h->stream); break;
@@ -465,6 +473,13 @@ int launch_step(moloch_handle* h, View<T>& v) {
 int step_kernels(moloch_handle* h) {
   if (h->elem == 8) return launch_step(h, h->vd);
   return launch_step(h, h->vf);
+}
+
+void drop_graphs(moloch_handle* h) {
+  for (int q = 0; q < 2; ++q) {
+    if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
+    if (h->graph[q]) { cudaGraphDestroy(h->graph[q]); h->graph[q] = nullptr; }
+  }
 }
 
 int check_launch(const char* what) {
@@ -1115,6 +1130,29 @@ int moloch_gpu_ensemble_destroy(moloch_ensemble_t* e) {
   delete e;
   return MOLOCH_OK;
 }
+
+}  // extern "C"
+
+// accessors for the surrogate translation unit (moloch_mlp.cu)
+moloch::View<float>* moloch_internal_viewf(moloch_handle_t* h) {
+  return (h && h->elem == 4 && h->initialized) ? &h->vf : nullptr;
+}
+cudaStream_t moloch_internal_stream(moloch_handle_t* h) { return h->stream; }
+int moloch_internal_nadv(moloch_handle_t* h) { return h->prm.mo_nadv; }
+int moloch_internal_nsound(moloch_handle_t* h) { return h->prm.mo_nsound; }
+// attach (s != nullptr) or detach; the plain kernels read the skip flag
+// through the view, and captured graphs are rebuilt on the next step
+int moloch_internal_attach(moloch_handle_t* h, moloch::mlp::Surrogate* s) {
+  if (h->elem != 4) return fail(MOLOCH_ERR_ARG, "the surrogate needs FP32 storage (MOLOCH_FP32_MIXED)");
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  h->sur = s;
+  h->vf.sur_skip = s ? s->flag : nullptr;
+  if (s) CUDA_TRY(cudaMemsetAsync(s->flag, 0, sizeof(int), h->stream));
+  drop_graphs(h);
+  return MOLOCH_OK;
+}
+
+extern "C" {
 
 int moloch_internal_describe(moloch_handle_t* h, moloch_grid_t* g, moloch_params_t* p) {
   if (!h || !g || !p) return fail(MOLOCH_ERR_ARG, "null argument");

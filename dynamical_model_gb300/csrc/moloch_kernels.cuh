@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
 // (:730-735); the bottom level computes w(kz+1) and s(kz+1) (:536-549).
 template <class T>
 __device__ __forceinline__ void b_sound_div(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int jj = bx * kPtBX + threadIdx.x;
   const int ii = by * kPtBY + threadIdx.y;
   const int kk = bz;
@@ -228,6 +229,7 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
 // solve starts from into zdiv2b.
 template <class T>
 __device__ __forceinline__ void b_sound_damp(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int jj = bx * kPtBX + threadIdx.x;
   const int ii = by * kPtBY + threadIdx.y;
   const int kk = bz;
@@ -293,6 +295,7 @@ template <> __device__ __forceinline__ double pivot_rcp<float>(double den) {
 // defer_pai: leave zdiv2b final and pai to k_pai_update (divergence filter on).
 template <class T>
 __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, const int by, const int bz, int nsound, int last, int defer_pai) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int jj = bx * kColBX + threadIdx.x;
   const int ii = by * kColBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
@@ -450,7 +453,9 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
 // out = a + coef(k) * (0.125*(aW+aE+aS+aN) - 0.5*a)   (:423-481)
 // coef(k) = anu2 * xknu(k) when use_xknu, else the constant c0.
 template <class T>
-__device__ __forceinline__ void b_lap_filter(const View<T>& d, const int bx, const int by, const int bz) {  const T* __restrict__ a = d.zdiv2b;
+__device__ __forceinline__ void b_lap_filter(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const T* __restrict__ a = d.zdiv2b;
   T* __restrict__ out = d.zdiv2a;
 
   int jj = bx * kPtBX + threadIdx.x;
@@ -485,7 +490,9 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
 
 // pai update with the nompi halo order (:716-728), split form
 template <class T>
-__device__ __forceinline__ void b_pai_update(const View<T>& d, const int bx, const int by, const int bz) {  const T* __restrict__ zd = d.zdiv2a;
+__device__ __forceinline__ void b_pai_update(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const T* __restrict__ zd = d.zdiv2a;
 
   int jj = bx * kPtBX + threadIdx.x;
   int ii = by * kPtBY + threadIdx.y;
@@ -558,6 +565,7 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
 // pre-damping edges) and writes the other buffer of the pair.
 template <class T>
 __device__ __forceinline__ void b_sound_momentum(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int jj = bx * kPtBX + threadIdx.x;
   const int ii = by * kPtBY + threadIdx.y;
   const int kk = bz;

@@ -108,6 +108,11 @@ struct View {
   // launch shape chosen by the autotuner: levels per k_waf_horizontal block
   int hz_levels;
 
+  // set when a learned surrogate stands in for sound(): the plain sound
+  // kernels return at once while *sur_skip == 1 (the surrogate's cycle was
+  // accepted); nullptr when no surrogate is attached
+  const int* sur_skip;
+
   // diagnostics
   double* dpart;  // per-block partial reductions
   double* dres;   // final reduction (device)

@@ -218,6 +218,54 @@ int moloch_tc_gemm(const void* A, int lda, const void* B, int ldb, float* C, int
  * call (synchronises the device and clears the flag), else MOLOCH_OK. */
 int moloch_tc_status(void);
 
+/* ---- learned acoustic-cycle surrogate ---------------------------------------
+ * A per-column MLP that replaces one sound() call (the mo_nsound acoustic
+ * substeps, nompi/mod_moloch.F90:483-851) on FP32-storage handles.  Input:
+ * u, v, w (levels 2..kz+1), pai, tetav of the column and its 8 neighbours
+ * (45*kz features, normalised per field and level); output: the increments
+ * of the same five fields of the centre column over the whole cycle.
+ * Layers: 45kz -> 256 -> 256 -> 256 -> 5kz, SiLU, BF16 operands and FP32
+ * accumulation on tcgen05 for training and inference.  When attached, each
+ * sound() first runs the MLP over every column and checks every increment
+ * (finite and |normalised| <= threshold); on acceptance the increments are
+ * committed and the plain substeps return immediately, otherwise the plain
+ * sound loop runs unchanged (the fallback; decided on the device, so the
+ * step stays one captured graph).  No reference counterpart.
+ *   create:   kz, dataset capacity (pairs), batch rows (multiple of 64)
+ *   collect:  advance the handle nsteps plain steps, recording
+ *             cols_per_cycle random columns per sound() call as pairs
+ *   prepare:  normalisation statistics, shuffle, validation split
+ *   train:    iters Adam steps (cosine decay from lr); returns the mean
+ *             squared error in normalised units on training rows and on
+ *             the validation split
+ *   attach:   s == NULL detaches; the surrogate must outlive the attachment
+ *   counts:   sound() calls seen while attached and how many fell back
+ *   param:    layer weights [out][in] and bias, read (set 0) or written
+ *   gradients: one forward+backward pass on n == batch rows of normalised
+ *             features X [n][kin] and targets T [n][nop]: summed squared
+ *             error and one layer's gradients (for gradient checks)
+ *   dims:     kz, nin, kin, nout, nop, hidden, batch, pairs, training rows
+ *   stats:    the normalisation statistics */
+typedef struct moloch_surrogate moloch_surrogate_t;
+int moloch_sur_create(int kz, int capacity, int batch, unsigned long long seed, moloch_surrogate_t** out);
+int moloch_sur_collect(moloch_surrogate_t* s, moloch_handle_t* h, int nsteps, int cols_per_cycle,
+                       unsigned long long seed);
+int moloch_sur_pairs(moloch_surrogate_t* s);
+int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long long seed);
+int moloch_sur_train(moloch_surrogate_t* s, int iters, float lr, unsigned long long seed, float* train_loss,
+                     float* val_loss);
+int moloch_sur_attach(moloch_handle_t* h, moloch_surrogate_t* s, float threshold);
+int moloch_sur_counts(moloch_surrogate_t* s, long long* cycles, long long* fallbacks);
+int moloch_sur_param(moloch_surrogate_t* s, int layer, float* W, float* b, int set, int* in_out);
+int moloch_sur_gradients(moloch_surrogate_t* s, const float* X, const float* T, int n, float* loss, int layer,
+                         float* gW, float* gb);
+int moloch_sur_dims(moloch_surrogate_t* s, int* dims);
+/* normalisation statistics, 5*kz each (field-major: u, v, w, pai, tetav):
+ * read (set 0) or write (set != 0, which also makes the surrogate
+ * attachable without moloch_sur_prepare) */
+int moloch_sur_stats(moloch_surrogate_t* s, float* xmean, float* xstd, float* ymean, float* ystd, int set);
+int moloch_sur_destroy(moloch_surrogate_t* s);
+
 /* WAF advection of ONE field by dt_adv seconds (the arithmetic of wafone,
  * nompi/mod_moloch.F90:929-1311) that allocates no device memory.  It has
  * no counterpart in the reference: it exists for callers that own all

@@ -1,0 +1,159 @@
+"""The learned acoustic-cycle surrogate on the GPU, through the C ABI.
+
+* gradients: one forward+backward pass of the tcgen05 MLP against the NumPy
+  oracle with the same BF16 roundings -- relative L2 <= 5e-3 per gradient
+  (only the FP32 summation order differs, which can move a stored BF16
+  activation by one unit in the last place);
+* inference + commit: one sound() call replaced by the surrogate, every
+  committed field and s against the oracle -- relative L2 of the increment
+  <= 5e-3;
+* fallback: a surrogate whose check rejects every cycle leaves the step
+  bit-identical to the plain FP32 step (graph and stepwise);
+* training: collect, prepare, train on a small hilly domain; the validation
+  loss falls and the surrogate run stays within a stated error of the FP64
+  run (see the test for the bound).
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+STATE = ("u", "v", "w", "pai", "tetav")
+
+
+def _random_params(sur, rng, scale=1.0):
+    P = []
+    for l in range(4):
+        W, b = sur.param(l)
+        fan = W.shape[1]
+        W = rng.normal(0, scale / np.sqrt(fan), W.shape).astype(np.float32)
+        b = rng.normal(0, 0.1, b.shape).astype(np.float32)
+        sur.set_param(l, W, b)
+        P.append((W.astype(np.float64), b.astype(np.float64)))
+    return P
+
+
+def test_sur_gradients_match_oracle(gpu_lib):
+    from oracle import mlp_oracle as mo
+    kz, B = 8, 128
+    sur = gpu_lib.Surrogate(kz, capacity=256, batch=B, seed=3)
+    d = sur.dims()
+    rng = np.random.default_rng(11)
+    P = _random_params(sur, rng, scale=1.5)
+    X = np.zeros((B, d["kin"]), np.float32)
+    X[:, :d["nin"]] = rng.normal(size=(B, d["nin"]))
+    T = np.zeros((B, d["nop"]), np.float32)
+    T[:, :d["nout"]] = rng.normal(size=(B, d["nout"]))
+    loss_ref, grads = mo.backward(P, X, T, d["nout"])
+    for l in range(4):
+        loss, gW, gb = sur.gradients(X, T, l)
+        assert abs(loss - loss_ref) <= 1e-4 * loss_ref, (loss, loss_ref)
+        assert rel_l2(gW, grads[l][0]) <= 5e-3, (l, rel_l2(gW, grads[l][0]))
+        assert rel_l2(gb, grads[l][1]) <= 5e-3, (l, rel_l2(gb, grads[l][1]))
+    sur.close()
+
+
+def _state(g):
+    return {f: g.get(f) for f in STATE}
+
+
+@pytest.mark.parametrize("jx,iy,kz", [(24, 20, 8), (37, 29, 12)])
+def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz):
+    from oracle import mlp_oracle as mo
+    g = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    g.setup_idealized(hills=((400.0, jx / 2, iy / 2, 3.0),), u0=5.0, v0=-3.0)
+    g.phase(0)
+    pre = _state(g)
+    sur = gpu_lib.Surrogate(kz, capacity=256, batch=128, seed=5)
+    d = sur.dims()
+    rng = np.random.default_rng(jx)
+    P = _random_params(sur, rng)
+    feats = mo.features(pre)
+    x5 = feats.reshape(-1, 9, 5, kz)
+    xmean = x5.mean(axis=(0, 1)).astype(np.float32)
+    xstd = (x5.std(axis=(0, 1)) + 1e-3).astype(np.float32)
+    ymean = rng.normal(0, 0.05, (5, kz)).astype(np.float32)
+    ystd = rng.uniform(0.2, 0.5, (5, kz)).astype(np.float32)
+    sur.set_stats(xmean, xstd, ymean, ystd)
+    sur.attach(g, threshold=1e30)
+    g.phase(1)
+    assert sur.counts() == (1, 0)
+    post = _state(g)
+    post["s"] = g.get("s")
+    Xn = mo.normalise(feats, xmean.astype(np.float64), xstd.astype(np.float64), d["kin"])
+    Y, _, _ = mo.forward(P, Xn.astype(np.float32))
+    inc = Y[:, :5 * kz].reshape(-1, 5, kz) * ystd + ymean
+    inc = inc.transpose(1, 2, 0).reshape(5, kz, iy, jx)
+    zita = g.get_1d("zita")
+    gz = mo.gzita(zita, g.params.mo_ztop, g.params.mo_a0)
+    want = mo.apply(pre, inc, g.params.mo_nsound, g.get("hx"), g.get("hy"), gz, g.get("fmzf"))
+    for f in STATE:
+        e = rel_l2(post[f] - pre[f], want[f] - pre[f])
+        assert e <= 5e-3, (f, e)
+    assert rel_l2(post["s"], want["s"]) <= 5e-3, rel_l2(post["s"], want["s"])
+    sur.close()
+    g.close()
+
+
+def test_sur_fallback_is_bit_identical(gpu_lib):
+    jx, iy, kz = 32, 24, 10
+    a = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    b = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    for g in (a, b):
+        g.setup_idealized(hills=((300.0, 16.0, 12.0, 3.0),), u0=4.0)
+    sur = gpu_lib.Surrogate(kz, capacity=256, batch=128)
+    _random_params(sur, np.random.default_rng(2))
+    sur.set_stats(np.zeros((5, kz)), np.ones((5, kz)), np.zeros((5, kz)), np.ones((5, kz)))
+    sur.attach(b, threshold=0.0)  # nothing passes: every cycle falls back
+    for s in range(1, 3):
+        a.moloch(s)
+        b.moloch(s)
+    a.run(2, graph=True)
+    b.run(2, graph=True)
+    nadv = a.params.mo_nadv
+    assert sur.counts() == (4 * nadv, 4 * nadv)
+    for f in ("u", "v", "w", "pai", "t", "qv", "ps", "s"):
+        assert np.array_equal(a.get(f), b.get(f)), f
+    sur.close()
+    a.close()
+    b.close()
+
+
+def test_sur_train_and_run(gpu_lib):
+    """Train on 6 plain steps of a 64 x 64 x 12 hilly domain, then run 6
+    steps with the surrogate from the same initial state.  Error measure:
+    RMS difference of tetav from the FP64 run.  Bound: the surrogate run
+    stays within 0.05 K of FP64 after 6 steps, and the validation loss
+    drops below 0.5 of its untrained value."""
+    jx, iy, kz = 64, 64, 12
+    setup = dict(hills=((500.0, 32.0, 32.0, 5.0),), u0=6.0, v0=2.0, pert_amp=0.5, pert_levels=6)
+    col = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    col.setup_idealized(**setup)
+    sur = gpu_lib.Surrogate(kz, capacity=16384, batch=256, seed=1)
+    n = sur.collect(col, 6, cols_per_cycle=512)
+    assert n == 6 * col.params.mo_nadv * 512
+    sur.prepare(0.1)
+    _, v0 = sur.train(0)
+    tl, vl = sur.train(2000, lr=1e-3)
+    print(f"surrogate: val loss {v0:.4g} -> {vl:.4g} (train {tl:.4g})")
+    assert np.isfinite(vl) and vl < 0.5 * v0
+    ref = gpu_lib.Moloch(jx, iy, kz, mode="fp64")
+    pl = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    run = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    for g in (ref, pl, run):
+        g.setup_idealized(**setup)
+    sur.attach(run, threshold=8.0)
+    for g in (ref, pl, run):
+        g.run(6, graph=True)
+    cyc, fb = sur.counts()
+    e_pl = np.sqrt(np.mean((pl.get("tetav") - ref.get("tetav")) ** 2))
+    e_sur = np.sqrt(np.mean((run.get("tetav") - ref.get("tetav")) ** 2))
+    print(f"surrogate: cycles {cyc}, fallbacks {fb}, tetav rms vs fp64: plain fp32 {e_pl:.3g}, "
+          f"surrogate {e_sur:.3g}")
+    assert cyc == 6 * run.params.mo_nadv
+    assert np.isfinite(e_sur) and e_sur <= 0.05
+    sur.close()
+    for g in (col, ref, pl, run):
+        g.close()
