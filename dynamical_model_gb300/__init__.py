@@ -115,9 +115,10 @@ _PROTOS = {
     "moloch_sur_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_ulonglong]),
     "moloch_sur_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong,
                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
-    "moloch_sur_attach": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float]),
+    "moloch_sur_attach": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
+                                         ctypes.c_float]),
     "moloch_sur_counts": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_longlong),
-                                         ctypes.POINTER(ctypes.c_longlong)]),
+                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
     "moloch_sur_param": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                         ctypes.c_int, ctypes.POINTER(ctypes.c_int)]),
     "moloch_sur_gradients": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
@@ -125,6 +126,8 @@ _PROTOS = {
                                             ctypes.c_void_p]),
     "moloch_sur_dims": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)]),
     "moloch_sur_stats": (ctypes.c_int, [ctypes.c_void_p] * 5 + [ctypes.c_int]),
+    "moloch_sur_profile": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                          ctypes.c_int]),
     "moloch_sur_destroy": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
@@ -394,19 +397,29 @@ class Surrogate:
         _check(self.L.moloch_sur_train(self.h, iters, lr, seed, ctypes.byref(tl), ctypes.byref(vl)))
         return tl.value, vl.value
 
-    def attach(self, model, threshold=8.0):
-        _check(self.L.moloch_sur_attach(model.h, self.h, threshold))
+    def attach(self, model, threshold=4.0, judge_every=6, tol=0.3):
+        """threshold: multiple of the training envelope an increment may
+        reach; judge_every: plain-loop judge every n-th sound() call (0:
+        never); tol: largest relative RMS error of the increments the judge
+        accepts."""
+        _check(self.L.moloch_sur_attach(model.h, self.h, threshold, judge_every, tol))
         self.attached = model
 
     def detach(self):
         if self.attached is not None and getattr(self.attached, "h", None):
-            _check(self.L.moloch_sur_attach(self.attached.h, None, 0.0))
+            _check(self.L.moloch_sur_attach(self.attached.h, None, 0.0, 0, 0.0))
         self.attached = None
 
     def counts(self):
-        c, f = ctypes.c_longlong(), ctypes.c_longlong()
-        _check(self.L.moloch_sur_counts(self.h, ctypes.byref(c), ctypes.byref(f)))
-        return c.value, f.value
+        """(sound() calls, calls run by the plain loop)."""
+        return self.stats_counts()["cycles"], self.stats_counts()["plain"]
+
+    def stats_counts(self):
+        c = (ctypes.c_longlong * 4)()
+        r, e = ctypes.c_float(), ctypes.c_float()
+        _check(self.L.moloch_sur_counts(self.h, c, ctypes.byref(r), ctypes.byref(e)))
+        return {"cycles": c[0], "plain": c[1], "judged": c[2], "judge_rejections": c[3],
+                "max_ratio": r.value, "last_judge_error": e.value}
 
     def param(self, layer):
         io = (ctypes.c_int * 2)()
@@ -424,6 +437,13 @@ class Surrogate:
         if W.shape != (io[1], io[0]) or b.shape != (io[1],):
             raise ValueError(f"layer {layer} is {io[1]}x{io[0]}")
         _check(self.L.moloch_sur_param(self.h, layer, W.ctypes.data, b.ctypes.data, 1, io))
+
+    def profile(self, model):
+        """CUDA-event ms of the inference stages of one cycle on the model's
+        state (changes no field)."""
+        ms = (ctypes.c_double * 6)()
+        _check(self.L.moloch_sur_profile(self.h, model.h, ms, 6))
+        return dict(zip(("features", "layer1", "layer2", "layer3", "layer4", "check"), list(ms)))
 
     def stats(self):
         """(xmean, xstd, ymean, ystd), each [5, kz] (u, v, w, pai, tetav)."""

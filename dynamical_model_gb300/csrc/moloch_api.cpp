@@ -447,11 +447,15 @@ int launch_phase(moloch_handle* h, View<T>& v, int phase) {
     }
   }
   if constexpr (sizeof(T) == sizeof(float)) {
-    if (phase == 1 && h->sur) n += moloch::mlp::sur_cycle(h->sur, v, h->stream, fl.nsound);
+    if (phase == 1 && h->sur) {
+      n = moloch::mlp::sur_cycle(h->sur, v, h->stream, fl.nsound);
+      n += kfast::launch_sound<T>(v, h->stream, fl);
+      return n + moloch::mlp::sur_after(h->sur, v, h->stream);
+    }
   }
   switch (phase) {
     case 0: n = kfast::launch_prediag<T>(v, h->stream, fl); break;
-    case 1: n += kfast::launch_sound<T>(v, h->stream, fl); break;
+    case 1: n = kfast::launch_sound<T>(v, h->stream, fl); break;
     case 2: n = kfast::launch_advection<T>(v, h->stream); break;
     case 3: n = kfast::launch_postdiag<T>(v, h->stream, fl, zk, zkm1); break;
     case 4: n = kfast::launch_diag<T>(v, h->stream); break;
@@ -1146,8 +1150,7 @@ int moloch_internal_attach(moloch_handle_t* h, moloch::mlp::Surrogate* s) {
   if (h->elem != 4) return fail(MOLOCH_ERR_ARG, "the surrogate needs FP32 storage (MOLOCH_FP32_MIXED)");
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   h->sur = s;
-  h->vf.sur_skip = s ? s->flag : nullptr;
-  if (s) CUDA_TRY(cudaMemsetAsync(s->flag, 0, sizeof(int), h->stream));
+  h->vf.sur_skip = s ? s->ctl : nullptr;  // ctl[0]: the cycle's commit flag
   drop_graphs(h);
   return MOLOCH_OK;
 }

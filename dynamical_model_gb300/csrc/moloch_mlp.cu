@@ -4,16 +4,17 @@
 //
 // k_gemm_tc computes C = act(A * B^T + bias) for A [M][K] and B [N][K] in
 // BF16, row-major with K contiguous (both operands K-major), C in FP32
-// and/or BF16.  One CTA owns 128 rows x up to 256 columns; the K loop
-// stages 64-wide chunks of A and B in shared memory in the no-swizzle
-// K-major core-matrix layout (moloch_tc.cuh), one thread issues four
-// 128 x N x 16 MMAs per chunk and commits them to an mbarrier that the
-// whole CTA waits on (bounded).  The accumulator lives in TMEM and is read
-// back with tcgen05.ld by the four warps, one 32-lane quarter each.
+// and/or BF16, in output tiles of 128 rows x up to 256 columns handed out
+// round-robin to persistent CTAs (one per SM).  Every wait is bounded; a
+// wait that gives up sets g_tc_error, and the CTA still drains its copies
+// and MMAs in flight (bounded) before it frees TMEM.
+#include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdio>
+#include <mutex>
 
 #include "../../include/moloch_gb300.h"
 #include "moloch_tc.cuh"
@@ -23,12 +24,14 @@ extern "C" void moloch_internal_set_error(const char* msg);
 namespace moloch {
 namespace mlp {
 
-constexpr int kChunkK = 64;              // K elements staged per chunk
-constexpr int kTileM = 128;              // UMMA M
-constexpr int kTileN = 256;              // max N per CTA
-constexpr int kASlot = 32 * 1024;        // A chunk (16 KB) with room to spare
-constexpr int kBSlot = 64 * 1024;        // B chunk (32 KB) with room to spare
-constexpr int kSmem = kASlot + kBSlot;
+constexpr int kChunkK = 64;               // K elements per stage (128 B rows: one swizzle atom)
+constexpr int kTileM = 128;               // UMMA M
+constexpr int kTileN = 256;               // max N per CTA
+constexpr int kStages = 4;
+constexpr int kAStage = kTileM * kChunkK * 2;   // 16 KB
+constexpr int kBStage = kTileN * kChunkK * 2;   // 32 KB
+constexpr int kSmem = kStages * (kAStage + kBStage) + 1024;  // + alignment slack
+constexpr int kThreads = 192;  // loader warp, MMA warp, four epilogue warps
 
 enum Act { ACT_NONE = 0, ACT_SILU = 1 };
 
@@ -36,88 +39,237 @@ static __device__ int g_tc_error;  // set when a bounded wait gives up
 
 __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
 
-__global__ void __launch_bounds__(128, 1)
-    k_gemm_tc(const __nv_bfloat16* __restrict__ A, int lda, const __nv_bfloat16* __restrict__ B, int ldb,
+// Persistent CTA (one per SM), six warps: warp 0 issues the TMA loads of
+// 64-wide K chunks of A and B (128-byte swizzle) into a kStages-deep ring of
+// shared-memory stages, warp 1 issues the 128 x N x 16 MMAs of each chunk
+// and commits them to the stage's "empty" barrier, and warps 2-5 drain the
+// accumulator of the previous tile from TMEM (tcgen05.ld, one 32-lane
+// quarter per warp) while the next tile accumulates: two accumulators of
+// 256 columns each are double-buffered in the 512 TMEM columns.
+__global__ void __launch_bounds__(kThreads, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int boxB,
               float* __restrict__ C, int ldc, __nv_bfloat16* __restrict__ Cb, int ldcb,
-              const float* __restrict__ bias, int M, int N, int K, int act) {
-  extern __shared__ __align__(1024) uint8_t smem[];
-  __shared__ uint64_t bar;
+              const float* __restrict__ bias, int M, int N, int K, int act, const int* __restrict__ run) {
+  if (run && !*run) return;  // device-side skip (a captured step whose surrogate is off)
+  extern __shared__ uint8_t smem_raw[];
+  __shared__ uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], done;
   __shared__ uint32_t tmem_base;
-  uint8_t* sA = smem;
-  uint8_t* sB = smem + kASlot;
+  __shared__ int s_fail, s_issued, s_consumed;
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * kTileM, n0 = blockIdx.y * kTileN;
-  const int nt = min(kTileN, N - n0);  // multiple of 16
-  if (warp == 0) tc::tmem_alloc(&tmem_base, 256);
-  if (tid == 0) tc::mbar_init(&bar, 1);
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  const int nm = (M + kTileM - 1) / kTileM, nn = (N + kTileN - 1) / kTileN, ntiles = nm * nn;
+  const int nk = K / kChunkK;
+  if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
+  if (tid == 32) {
+    for (int s = 0; s < kStages; ++s) {
+      tc::mbar_init(&full[s], 1);
+      tc::mbar_init(&empty[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      tc::mbar_init(&acc_full[b], 1);
+      tc::mbar_init(&acc_empty[b], 128);
+    }
+    tc::mbar_init(&done, 1);
+    s_fail = 0;
+    s_issued = 0;
+    s_consumed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tbase = tmem_base;
-  const uint32_t idesc = tc::idesc_bf16(nt);
-  const uint32_t aaddr = tc::smem_u32(sA), baddr = tc::smem_u32(sB);
-  constexpr uint32_t kLBO = 128, kSBO = (kChunkK / 8) * 128;
-  uint32_t parity = 0;
-  bool ok = true;
-  for (int k0 = 0; k0 < K; k0 += kChunkK) {
-    // stage the chunk: one 16-byte vector = one core-matrix row (8 BF16)
-    for (int q = tid; q < kTileM * (kChunkK / 8); q += 128) {
-      const int r = q / (kChunkK / 8), kc = q % (kChunkK / 8);
-      uint4 val = make_uint4(0, 0, 0, 0);
-      if (m0 + r < M) val = *reinterpret_cast<const uint4*>(A + (size_t)(m0 + r) * lda + k0 + kc * 8);
-      *reinterpret_cast<uint4*>(sA + ((r >> 3) * (kChunkK / 8) + kc) * 128 + (r & 7) * 16) = val;
-    }
-    for (int q = tid; q < nt * (kChunkK / 8); q += 128) {
-      const int r = q / (kChunkK / 8), kc = q % (kChunkK / 8);
-      const uint4 val = *reinterpret_cast<const uint4*>(B + (size_t)(n0 + r) * ldb + k0 + kc * 8);
-      *reinterpret_cast<uint4*>(sB + ((r >> 3) * (kChunkK / 8) + kc) * 128 + (r & 7) * 16) = val;
-    }
-    tc::fence_proxy_async();  // generic-proxy stores -> visible to the tensor core
-    __syncthreads();
-    if (tid == 0) {
-      tc::tc_fence_after();
-#pragma unroll
-      for (int kk = 0; kk < kChunkK / 16; ++kk) {  // K = 16 per MMA = two core matrices
-        const uint64_t ad = tc::smem_desc(aaddr + kk * 256, kLBO, kSBO);
-        const uint64_t bd = tc::smem_desc(baddr + kk * 256, kLBO, kSBO);
-        tc::mma_bf16(tbase, ad, bd, idesc, (k0 > 0 || kk > 0) ? 1 : 0);
+  const uint32_t stage_bytes = (uint32_t)(kTileM + boxB) * kChunkK * 2;
+  if (tid == 0) {
+    // ---- loader
+    int it = 0;
+    for (int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x) {
+      const int m0 = (t % nm) * kTileM, n0 = (t / nm) * kTileN;
+      for (int kc = 0; kc < nk; ++kc, ++it) {
+        const int s = it % kStages;
+        if (it >= kStages && !tc::mbar_wait(&empty[s], ((it / kStages) - 1) & 1)) {
+          s_fail = 1;
+          break;
+        }
+        uint8_t* sa = smem + s * (kAStage + kBStage);
+        tc::mbar_arrive_expect_tx(&full[s], stage_bytes);
+        tc::tma_load_2d(sa, &tmA, kc * kChunkK, m0, &full[s]);
+        tc::tma_load_2d(sa + kAStage, &tmB, kc * kChunkK, n0, &full[s]);
+        s_issued = it + 1;
       }
-      tc::mma_commit(&bar);
     }
-    if (!tc::mbar_wait(&bar, parity)) {
-      ok = false;
-      atomicExch(&g_tc_error, 1);
-      break;
-    }
-    parity ^= 1;
-    tc::tc_fence_after();
-    __syncthreads();  // everyone saw the MMAs finish: the chunk buffers are free
-  }
-  if (ok) {
-    const uint32_t lrow = (uint32_t)(warp * 32) << 16;
-    const int row = m0 + warp * 32 + lane;
-    for (int c = 0; c < nt; c += 16) {
-      float v[16];
-      tc::tmem_ld16(tbase + lrow + c, v);
-      if (row < M) {
+  } else if (tid == 32) {
+    // ---- MMA issuer
+    int it = 0, lt = 0;
+    for (int t = blockIdx.x; t < ntiles && !*(volatile int*)&s_fail; t += gridDim.x, ++lt) {
+      const int n0 = (t / nm) * kTileN;
+      const int nt = min(kTileN, N - n0);
+      const uint32_t idesc = tc::idesc_bf16(nt);
+      const int b = lt & 1;
+      if (lt >= 2 && !tc::mbar_wait(&acc_empty[b], ((lt >> 1) - 1) & 1)) {
+        s_fail = 1;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t dacc = tbase + (uint32_t)(b * kTileN);
+      for (int kc = 0; kc < nk; ++kc, ++it) {
+        const int s = it % kStages;
+        if (!tc::mbar_wait(&full[s], (it / kStages) & 1)) {
+          s_fail = 1;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t aaddr = tc::smem_u32(smem + s * (kAStage + kBStage));
+        const uint32_t baddr = aaddr + kAStage;
 #pragma unroll
-        for (int q = 0; q < 16; ++q) {
-          const int col = n0 + c + q;
-          float x = v[q] + (bias ? bias[col] : 0.f);
-          if (C) C[(size_t)row * ldc + col] = x;
-          if (Cb) Cb[(size_t)row * ldcb + col] = __float2bfloat16_rn(act == ACT_SILU ? silu(x) : x);
+        for (int kk = 0; kk < kChunkK / 16; ++kk)
+          tc::mma_bf16(dacc, tc::smem_desc_sw128(aaddr + kk * 32), tc::smem_desc_sw128(baddr + kk * 32), idesc,
+                       (kc > 0 || kk > 0) ? 1 : 0);
+        tc::mma_commit(&empty[s]);
+        s_consumed = it + 1;
+      }
+      if (*(volatile int*)&s_fail) break;
+      tc::mma_commit(&acc_full[b]);
+    }
+    tc::mma_commit(&done);  // arrives once every MMA issued above has completed
+  } else if (warp >= 2) {
+    // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
+    const int q = warp & 3;
+    const uint32_t lrow = (uint32_t)(q * 32) << 16;
+    int lt = 0;
+    for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
+      const int b = lt & 1;
+      if (!tc::mbar_wait(&acc_full[b], (lt >> 1) & 1)) {
+        s_fail = 1;
+        break;
+      }
+      tc::tc_fence_after();
+      const int m0 = (t % nm) * kTileM, n0 = (t / nm) * kTileN;
+      const int nt = min(kTileN, N - n0);
+      const int row = m0 + q * 32 + lane;
+      for (int c = 0; c < nt; c += 16) {
+        float v[16];
+        tc::tmem_ld16(tbase + lrow + (uint32_t)(b * kTileN + c), v);
+        if (row < M) {
+#pragma unroll
+          for (int e = 0; e < 16; ++e) v[e] += bias ? bias[n0 + c + e] : 0.f;
+          if (C) {
+            float4* cp = reinterpret_cast<float4*>(C + (size_t)row * ldc + n0 + c);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) cp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
+          }
+          if (Cb) {
+            uint32_t pk[8];
+#pragma unroll
+            for (int e = 0; e < 8; ++e) {
+              float x0 = v[2 * e], x1 = v[2 * e + 1];
+              if (act == ACT_SILU) {
+                x0 = silu(x0);
+                x1 = silu(x1);
+              }
+              const __nv_bfloat162 b2 = __floats2bfloat162_rn(x0, x1);
+              pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
+            }
+            uint4* bp = reinterpret_cast<uint4*>(Cb + (size_t)row * ldcb + n0 + c);
+            bp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+            bp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+          }
         }
       }
+      tc::tc_fence_before();
+      tc::mbar_arrive(&acc_empty[b]);
     }
-  } else {
-    // a wait gave up: let any MMA still in flight finish (bounded) before
-    // the accumulator columns are released
-    tc::mbar_wait(&bar, parity);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // every MMA has completed before TMEM is released; loads still in
+    // flight after a failed wait are drained (all waits bounded)
+    if (!tc::mbar_wait(&done, 0)) s_fail = 1;
+    if (s_fail) {
+      atomicExch(&g_tc_error, 1);
+      for (int it = s_consumed; it < s_issued; ++it) tc::mbar_wait(&full[it % kStages], (it / kStages) & 1);
+    }
   }
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tbase, 256);
+  tc::tc_fence_after();
+  if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+// ---- host side -------------------------------------------------------------
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+
+// BF16 row-major [rows][cols] (ld elements) as a TMA map with box
+// [box_rows][64], 128-byte swizzle, zero fill outside
+static bool make_map(CUtensorMap* m, const void* base, int rows, int cols, int ld, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {(cuuint64_t)cols, (cuuint64_t)rows};
+  const cuuint64_t strides[1] = {(cuuint64_t)ld * 2};
+  const cuuint32_t box[2] = {(cuuint32_t)kChunkK, (cuuint32_t)box_rows};
+  const cuuint32_t es[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static int num_sms() {
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+    if (n <= 0) n = 1;
+  }
+  return n;
+}
+
+static void gemm_attr() {
+  static std::once_flag once;
+  std::call_once(once, [] { cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem); });
+}
+
+// checks shapes, builds the two maps and launches; MOLOCH_OK or an error code
+static int launch_gemm(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
+                       const float* bias, int M, int N, int K, int act, cudaStream_t st,
+                       const int* run = nullptr) {
+  if (!A || !B || (!C && !Cb) || M <= 0 || N <= 0 || K <= 0) {
+    moloch_internal_set_error("tc_gemm: bad arguments");
+    return MOLOCH_ERR_ARG;
+  }
+  if (N % 16 || K % kChunkK || lda % 8 || ldb % 8 || lda < K || ldb < K || (C && (ldc < N || ldc % 4)) ||
+      (Cb && (ldcb < N || ldcb % 8)) || ((uintptr_t)A | (uintptr_t)B) % 16 || ((uintptr_t)C % 16) ||
+      ((uintptr_t)Cb % 16)) {
+    moloch_internal_set_error("tc_gemm: need N % 16 == 0, K % 64 == 0, 16-byte aligned rows");
+    return MOLOCH_ERR_ARG;
+  }
+  gemm_attr();
+  const int boxB = N < kTileN ? N : kTileN;
+  CUtensorMap ta, tb;
+  if (!make_map(&ta, A, M, K, lda, kTileM) || !make_map(&tb, B, N, K, ldb, boxB)) {
+    moloch_internal_set_error("tc_gemm: cuTensorMapEncodeTiled failed");
+    return MOLOCH_ERR_CUDA;
+  }
+  const int ntiles = ((M + kTileM - 1) / kTileM) * ((N + kTileN - 1) / kTileN);
+  k_gemm_tc<<<std::min(ntiles, num_sms()), kThreads, kSmem, st>>>(ta, tb, boxB, C, ldc, (__nv_bfloat16*)Cb, ldcb,
+                                                                   bias, M, N, K, act, run);
+  return MOLOCH_OK;
 }
 
 }  // namespace mlp
@@ -128,22 +280,8 @@ using namespace moloch::mlp;
 // GEMM on device buffers for the surrogate and its tests.
 extern "C" int moloch_tc_gemm(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
                               const float* bias, int M, int N, int K, int act, void* stream) {
-  if (!A || !B || (!C && !Cb) || M <= 0 || N <= 0 || K <= 0) {
-    moloch_internal_set_error("tc_gemm: bad arguments");
-    return MOLOCH_ERR_ARG;
-  }
-  if (N % 16 || K % kChunkK || lda % 8 || ldb % 8 || lda < K || ldb < K || (C && ldc < N) || (Cb && ldcb < N)) {
-    moloch_internal_set_error("tc_gemm: need N % 16 == 0, K % 64 == 0, 16-byte aligned rows");
-    return MOLOCH_ERR_ARG;
-  }
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    attr = true;
-  }
-  dim3 grid((M + kTileM - 1) / kTileM, (N + kTileN - 1) / kTileN);
-  k_gemm_tc<<<grid, 128, kSmem, (cudaStream_t)stream>>>((const __nv_bfloat16*)A, lda, (const __nv_bfloat16*)B, ldb, C, ldc,
-                                                         (__nv_bfloat16*)Cb, ldcb, bias, M, N, K, act);
+  int rc = launch_gemm(A, lda, B, ldb, C, ldc, Cb, ldcb, bias, M, N, K, act, (cudaStream_t)stream);
+  if (rc) return rc;
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     moloch_internal_set_error(cudaGetErrorString(e));
@@ -171,8 +309,7 @@ extern "C" int moloch_tc_status(void) {
 namespace moloch {
 namespace mlp {
 
-// feature x[(nb * 5 + f) * kz + k]: neighbour nb = (di + 1) * 3 + (dj + 1),
-// field f = u, v, w (levels 2..kz+1), pai, tetav, level k
+// value of field f (u, v, w levels 2..kz+1, pai, tetav) at (j, i, level k)
 __device__ __forceinline__ float sur_field(const View<float>& d, int f, int j, int i, int k) {
   const size_t q = (size_t)j + (size_t)d.nj * i + (size_t)k * d.pl;
   switch (f) {
@@ -184,50 +321,96 @@ __device__ __forceinline__ float sur_field(const View<float>& d, int f, int j, i
   }
 }
 
-// Features of ncols columns (cols == nullptr: all columns in order).  Block
-// = 32 columns x 8 feature lanes; a 64-feature slab is staged in shared
-// memory so both the field reads (consecutive j) and the row writes
-// (consecutive features) are coalesced.  NORM: subtract/scale with the
-// dataset statistics and write BF16; else write raw FP32.
+// Features of ncols columns (cols == nullptr: all columns in order), one
+// block per 128 columns, one thread per column.  Feature index
+// (f * kz + k) * 9 + nb: field f (u, v, w levels 2..kz+1, pai, tetav), level
+// k, neighbour nb = (di + 1) * 3 + (dj + 1) fastest, so that a 64-feature
+// chunk touches about 7 field planes.  For each chunk a table in shared
+// memory gives every feature's plane, neighbour slot and normalisation; each
+// thread gathers its column's 64 values (consecutive threads read
+// consecutive j: coalesced, and the 9 neighbours hit L1), and the chunk
+// is transposed through shared memory so that 8 threads write one column's
+// 128-byte (BF16) or 256-byte (FP32) row segment together.  NORM: normalise
+// with the dataset statistics and write BF16; else write raw FP32.
 template <bool NORM>
-__global__ void __launch_bounds__(256) k_sur_features(View<float> d, const int* __restrict__ cols, int ncols,
+__global__ void __launch_bounds__(128) k_sur_features(View<float> d, const int* __restrict__ cols, int ncols,
                                                       const float* __restrict__ xmean, const float* __restrict__ xstd,
-                                                      void* out, int ldo) {
-  __shared__ float tile[64][33];
-  const int tx = threadIdx.x, ty = threadIdx.y;
-  const int c0 = blockIdx.x * 32;
+                                                      void* out, int ldo, const int* __restrict__ run) {
+  if (run && !*run) return;
+  __shared__ int nbo[9][128];                 // neighbour column offsets
+  __shared__ const float* tptr[64];           // field plane of each feature of the chunk
+  __shared__ int tnb[64];                     // neighbour slot (-1: padding)
+  __shared__ float tsub[64], tmul[64];        // normalisation
+  __shared__ float tile[128][65];             // [column][feature]
+  const int t = threadIdx.x;
+  const int c0 = blockIdx.x * 128;
   const int kz = d.kz, nf = 45 * kz;
-  const int cidx = c0 + tx;
-  int j = 0, i = 0;
-  if (cidx < ncols) {
-    const int col = cols ? cols[cidx] : cidx;
-    j = col % d.nj;
-    i = col / d.nj;
+  const int cidx = c0 + t;
+  {
+    int j = 0, i = 0;
+    if (cidx < ncols) {
+      const int col = cols ? cols[cidx] : cidx;
+      j = col % d.nj;
+      i = col / d.nj;
+    }
+    const int jm = j == 0 ? d.nj - 1 : j - 1, jp = j == d.nj - 1 ? 0 : j + 1;
+    const int im = i == 0 ? d.ni - 1 : i - 1, ip = i == d.ni - 1 ? 0 : i + 1;
+    const int jj[3] = {jm, j, jp}, ii[3] = {im, i, ip};
+#pragma unroll
+    for (int nb = 0; nb < 9; ++nb) nbo[nb][t] = jj[nb % 3] + d.nj * ii[nb / 3];
   }
   for (int f0 = 0; f0 < ldo; f0 += 64) {
-    for (int r = ty; r < 64; r += 8) {
-      const int fe = f0 + r;
-      float val = 0.f;
-      if (cidx < ncols && fe < nf) {
-        const int k = fe % kz, fk = fe / kz, fld = fk % 5, nb = fk / 5;
-        const int dj = nb % 3 - 1, di = nb / 3 - 1;
-        int jj = j + dj, ii = i + di;
-        jj = jj < 0 ? jj + d.nj : (jj >= d.nj ? jj - d.nj : jj);
-        ii = ii < 0 ? ii + d.ni : (ii >= d.ni ? ii - d.ni : ii);
-        val = sur_field(d, fld, jj, ii, k);
-        if (NORM) val = (val - xmean[fld * kz + k]) / xstd[fld * kz + k];
+    if (t < 64) {
+      const int fe = f0 + t;
+      if (fe < nf) {
+        const int plane = fe / 9, k = plane % kz, fld = plane / kz;
+        const float* base = fld == 0 ? d.ubuf[d.cur] : fld == 1 ? d.vbuf[d.cur] : fld == 2 ? d.w + d.pl
+                          : fld == 3 ? d.pai : d.tetav;
+        tptr[t] = base + (size_t)k * d.pl;
+        tnb[t] = fe - 9 * plane;
+        if (NORM) {
+          tsub[t] = xmean[plane];
+          tmul[t] = 1.0f / xstd[plane];
+        }
+      } else {
+        tnb[t] = -1;
       }
-      tile[r][tx] = val;
     }
     __syncthreads();
-    // write rows: column c0 + cc, features f0 .. f0+63
-    for (int q = tx + 32 * ty; q < 32 * 64; q += 256) {
-      const int cc = q / 64, r = q % 64;
-      if (c0 + cc < ncols && f0 + r < ldo) {
-        if (NORM)
-          reinterpret_cast<__nv_bfloat16*>(out)[(size_t)(c0 + cc) * ldo + f0 + r] = __float2bfloat16_rn(tile[r][cc]);
-        else
-          reinterpret_cast<float*>(out)[(size_t)(c0 + cc) * ldo + f0 + r] = tile[r][cc];
+    if (cidx < ncols) {
+#pragma unroll 8
+      for (int r = 0; r < 64; ++r) {
+        const int nb = tnb[r];
+        float val = 0.f;
+        if (nb >= 0) {
+          val = __ldg(tptr[r] + nbo[nb][t]);
+          if (NORM) val = (val - tsub[r]) * tmul[r];
+        }
+        tile[t][r] = val;
+      }
+    }
+    __syncthreads();
+    // write: 8 (BF16) or 16 (FP32) threads per column row segment
+    if (NORM) {
+      for (int q = t; q < 128 * 8; q += 128) {
+        const int cc = q >> 3, part = q & 7;
+        if (c0 + cc < ncols && f0 + part * 8 < ldo) {
+          uint32_t pk[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const __nv_bfloat162 b2 = __floats2bfloat162_rn(tile[cc][part * 8 + 2 * e], tile[cc][part * 8 + 2 * e + 1]);
+            pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
+          }
+          *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) + (size_t)(c0 + cc) * ldo + f0 + part * 8) =
+              make_uint4(pk[0], pk[1], pk[2], pk[3]);
+        }
+      }
+    } else {
+      for (int q = t; q < 128 * 16; q += 128) {
+        const int cc = q >> 4, part = q & 15;
+        if (c0 + cc < ncols && f0 + part * 4 < ldo)
+          *reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + (size_t)(c0 + cc) * ldo + f0 + part * 4) =
+              make_float4(tile[cc][part * 4], tile[cc][part * 4 + 1], tile[cc][part * 4 + 2], tile[cc][part * 4 + 3]);
       }
     }
     __syncthreads();
@@ -254,16 +437,16 @@ __global__ void k_sur_increment(View<float> d, const int* __restrict__ cols, int
     T[(size_t)c * ldt + q] = q < 5 * kz ? sur_field(d, q / kz, j, i, q % kz) - snap[(size_t)c * 5 * kz + q] : 0.f;
 }
 
-// in-place normalisation of a row-major [n][ld] FP32 array by per-column
-// statistics (the first m columns), with optional BF16 copy
+// in-place normalisation of a row-major [n][ld] FP32 array (the first m
+// columns; column c uses statistic c / group), with optional BF16 copy
 __global__ void k_sur_normalize(float* __restrict__ a, int n, int ld, int m, const float* __restrict__ mean,
-                                const float* __restrict__ stdv, __nv_bfloat16* __restrict__ ab, int period) {
+                                const float* __restrict__ stdv, __nv_bfloat16* __restrict__ ab, int group) {
   const size_t tot = (size_t)n * ld;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(q % ld);
     float v = a[q];
     if (c < m) {
-      const int s = c % period;
+      const int s = c / group;
       v = (v - mean[s]) / stdv[s];
     } else {
       v = 0.f;
@@ -351,25 +534,138 @@ __global__ void k_adam(float* __restrict__ W, const float* __restrict__ g, float
   }
 }
 
-// acceptance check of one surrogate cycle: every increment finite and its
-// normalised size within the threshold.  k_sur_check marks *bad; the
-// one-thread k_sur_decide turns it into *flag = 1 (accept) / 0 (fall back to
-// the plain sound loop), counts, and clears *bad for the next cycle.
-__global__ void k_sur_check(const float* __restrict__ Y, int n, int ld, int m, float threshold, int* __restrict__ bad) {
+// ---- control of a surrogate cycle (all decisions on the device, so that a
+// whole step stays one captured graph).  Control block `ctl`:
+//   [0] flag       1: the surrogate's increments are committed this cycle
+//                  and the plain substeps return at once (their skip flag)
+//   [1] bad        set by k_sur_check
+//   [2] cycle      sound() calls seen since attach
+//   [3] judge      1: this cycle is a judge cycle
+//   [4] enabled    verdict of the last judge cycle
+//   [5] maxratio   largest |y| / envelope seen since attach (float bits)
+//   [6] lasterr    error of the last judge cycle (float bits)
+//   [7] run        1: the inference runs this cycle (enabled or judge)
+//   [8] nextjudge  cycle of the next judge
+//   [9] interval   cycles from this judge to the next one
+// counts: [0] cycles, [1] cycles run by the plain loop, [2] judge cycles,
+// [3] judge cycles that disabled the surrogate.
+// A judge cycle runs both the inference and the plain sound loop, and the
+// plain loop judges the prediction: the relative RMS error of the
+// increments, worst of the five fields, must be <= tol.  After a passing
+// verdict the next judge comes judge_every cycles later; after a failing
+// one the surrogate is off (no inference at all) and the interval doubles,
+// up to max_interval cycles.
+enum {
+  CTL_FLAG = 0, CTL_BAD, CTL_CYCLE, CTL_JUDGE, CTL_ENABLED, CTL_MAXRATIO, CTL_LASTERR, CTL_RUN, CTL_NEXTJUDGE,
+  CTL_INTERVAL, CTL_COUNT = 32
+};
+
+__global__ void k_sur_begin(int* __restrict__ ctl, int judge_every, double* __restrict__ jacc) {
+  const int cyc = ctl[CTL_CYCLE]++;
+  const int judge = judge_every > 0 && cyc == ctl[CTL_NEXTJUDGE];
+  ctl[CTL_JUDGE] = judge;
+  ctl[CTL_RUN] = judge || ctl[CTL_ENABLED];
+  ctl[CTL_BAD] = 0;
+  if (judge)
+    for (int q = 0; q < 10; ++q) jacc[q] = 0.0;
+}
+
+// every increment finite and within threshold x the envelope of the
+// training targets (per output, normalised units); tracks the largest ratio
+__global__ void k_sur_check(const float* __restrict__ Y, int n, int ld, int m, const float* __restrict__ env,
+                            float threshold, int* __restrict__ ctl, const int* __restrict__ run) {
+  if (run && !*run) return;
   const size_t tot = (size_t)n * ld;
   int b = 0;
+  float rmax = 0.f;
   for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
     const int c = (int)(q % ld);
-    if (c < m && !(fabsf(Y[q]) <= threshold)) b = 1;  // also catches NaN
+    if (c < m) {
+      const float r = fabsf(Y[q]) / env[c];
+      if (!(r <= threshold)) b = 1;  // also catches NaN
+      rmax = r == r ? fmaxf(rmax, r) : __int_as_float(0x7f800000);
+    }
   }
-  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(bad, 1);
+  for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(&ctl[CTL_BAD], 1);
+  if ((threadIdx.x & 31) == 0) atomicMax(&ctl[CTL_MAXRATIO], __float_as_int(rmax));
 }
-__global__ void k_sur_decide(int* __restrict__ bad, int* __restrict__ flag, unsigned long long* __restrict__ counts) {
-  const int b = *bad;
-  *flag = b ? 0 : 1;
+
+__global__ void k_sur_decide(int* __restrict__ ctl, unsigned long long* __restrict__ counts) {
+  const int use = ctl[CTL_RUN] && ctl[CTL_ENABLED] && !ctl[CTL_BAD] && !ctl[CTL_JUDGE];
+  ctl[CTL_FLAG] = use;
   counts[0] += 1;
-  if (b) counts[1] += 1;
-  *bad = 0;
+  if (!use) counts[1] += 1;
+}
+
+// judge cycles: copy of the pre-cycle state of the five fields
+__global__ void k_sur_judge_snapshot(View<float> d, const int* __restrict__ ctl, float* __restrict__ snap) {
+  if (!ctl[CTL_JUDGE]) return;
+  const size_t n = (size_t)d.pl * d.kz;
+  const float* src[5] = {d.ubuf[d.cur], d.vbuf[d.cur], d.w + d.pl, d.pai, d.tetav};
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < 5 * n; q += (size_t)gridDim.x * blockDim.x) {
+    const int f = (int)(q / n);
+    snap[q] = src[f][q - (size_t)f * n];
+  }
+}
+
+// judge cycles, after the plain loop: sums of (predicted - actual)^2 and
+// actual^2 of the increments, per field
+__global__ void __launch_bounds__(256) k_sur_judge(View<float> d, const int* __restrict__ ctl,
+                                                   const float* __restrict__ snap, const float* __restrict__ Y, int ld,
+                                                   const float* __restrict__ ymean, const float* __restrict__ ystd,
+                                                   double* __restrict__ jacc) {
+  if (!ctl[CTL_JUDGE]) return;
+  const size_t pl = d.pl, n = pl * d.kz;
+  const float* post[5] = {d.ubuf[d.cur], d.vbuf[d.cur], d.w + d.pl, d.pai, d.tetav};
+  __shared__ double red[8][10];
+  double acc[10];
+#pragma unroll
+  for (int q = 0; q < 10; ++q) acc[q] = 0.0;
+  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < n; q += (size_t)gridDim.x * blockDim.x) {
+    const int k = (int)(q / pl);
+    const size_t c = q - (size_t)k * pl;
+#pragma unroll
+    for (int f = 0; f < 5; ++f) {
+      const int o = f * d.kz + k;
+      const float act = post[f][q] - snap[(size_t)f * n + q];
+      const float pred = Y[c * ld + o] * ystd[o] + ymean[o];
+      const float e = pred - act;
+      acc[2 * f] += (double)e * e;
+      acc[2 * f + 1] += (double)act * act;
+    }
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int q = 0; q < 10; ++q) {
+    double v = acc[q];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wid][q] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 10) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+    atomicAdd(&jacc[threadIdx.x], v);
+  }
+}
+
+__global__ void k_sur_verdict(int* __restrict__ ctl, const double* __restrict__ jacc, float tol, int judge_every,
+                              int max_interval, unsigned long long* __restrict__ counts) {
+  if (!ctl[CTL_JUDGE]) return;
+  double worst = 0.0;
+  for (int f = 0; f < 5; ++f) {
+    const double r = jacc[2 * f + 1] > 0.0 ? sqrt(jacc[2 * f] / jacc[2 * f + 1]) : (jacc[2 * f] > 0.0 ? 1e30 : 0.0);
+    worst = r == r ? fmax(worst, r) : 1e30;
+  }
+  const int ok = worst <= (double)tol;
+  ctl[CTL_ENABLED] = ok;
+  ctl[CTL_LASTERR] = __float_as_int((float)worst);
+  const int iv = ok ? judge_every : min(2 * ctl[CTL_INTERVAL], max_interval);
+  ctl[CTL_INTERVAL] = iv;
+  ctl[CTL_NEXTJUDGE] = ctl[CTL_CYCLE] - 1 + iv;  // counted from this (judge) cycle
+  counts[2] += 1;
+  if (!ok) counts[3] += 1;
 }
 
 // gather rows of a row-major array: out[r] = in[idx[r]]
@@ -389,8 +685,8 @@ __global__ void k_gather_rows(const E* __restrict__ in, const int* __restrict__ 
 // new w.  Writes s only, so it runs before part 2 changes u, v, w.
 __global__ void __launch_bounds__(256) k_sur_vvel(View<float> d, const float* __restrict__ Y, int ld,
                                                   const float* __restrict__ ymean, const float* __restrict__ ystd,
-                                                  const int* __restrict__ flag, int nsound) {
-  if (!*flag) return;
+                                                  const int* __restrict__ ctl, int nsound) {
+  if (!ctl[CTL_FLAG]) return;
   const int jj = blockIdx.x * 32 + threadIdx.x, ii = blockIdx.y * 8 + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
@@ -421,8 +717,8 @@ __global__ void __launch_bounds__(256) k_sur_vvel(View<float> d, const float* __
 // substeps.
 __global__ void __launch_bounds__(256) k_sur_apply(View<float> d, const float* __restrict__ Y, int ld,
                                                    const float* __restrict__ ymean, const float* __restrict__ ystd,
-                                                   const int* __restrict__ flag, int nsound) {
-  if (!*flag) return;
+                                                   const int* __restrict__ ctl, int nsound) {
+  if (!ctl[CTL_FLAG]) return;
   const int jj = blockIdx.x * 32 + threadIdx.x, ii = blockIdx.y * 8 + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
@@ -451,7 +747,7 @@ __global__ void __launch_bounds__(256) k_sur_apply(View<float> d, const float* _
 // =========================================================================
 #include <algorithm>
 #include <cmath>
-#include <mutex>
+#include <cstring>
 #include <vector>
 
 // accessors into a handle (moloch_api.cpp)
@@ -485,16 +781,9 @@ static double u01h(uint64_t& st) { return (double)(sm64(st) >> 11) * (1.0 / 9007
     }                                                                                  \
   } while (0)
 
-static int g_gemm_attr_done = 0;
 static int gemm(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
-                const float* bias, int M, int N, int K, int act, cudaStream_t st) {
-  if (!g_gemm_attr_done) {
-    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    g_gemm_attr_done = 1;
-  }
-  dim3 grid((M + kTileM - 1) / kTileM, (N + kTileN - 1) / kTileN);
-  k_gemm_tc<<<grid, 128, kSmem, st>>>((const __nv_bfloat16*)A, lda, (const __nv_bfloat16*)B, ldb, C, ldc,
-                                       (__nv_bfloat16*)Cb, ldcb, bias, M, N, K, act);
+                const float* bias, int M, int N, int K, int act, cudaStream_t st, const int* run = nullptr) {
+  launch_gemm(A, lda, B, ldb, C, ldc, Cb, ldcb, bias, M, N, K, act, st, run);
   return 1;
 }
 
@@ -508,12 +797,13 @@ static int transpose(const void* in, int rows, int cols, int ld_in, void* out, i
 }
 
 // forward of n rows: X -> H[0..2] (BF16, SiLU) -> Y (FP32); Z (pre-activations) optional
-static int forward(Surrogate* s, const void* X, int n, void* const* H, float* const* Z, float* Y, cudaStream_t st) {
+static int forward(Surrogate* s, const void* X, int n, void* const* H, float* const* Z, float* Y, cudaStream_t st,
+                   const int* run = nullptr) {
   const int hid = s->hid;
-  gemm(X, s->kin, s->L[0].Wb, s->kin, Z ? Z[0] : nullptr, hid, H[0], hid, s->L[0].b, n, hid, s->kin, ACT_SILU, st);
-  gemm(H[0], hid, s->L[1].Wb, hid, Z ? Z[1] : nullptr, hid, H[1], hid, s->L[1].b, n, hid, hid, ACT_SILU, st);
-  gemm(H[1], hid, s->L[2].Wb, hid, Z ? Z[2] : nullptr, hid, H[2], hid, s->L[2].b, n, hid, hid, ACT_SILU, st);
-  gemm(H[2], hid, s->L[3].Wb, hid, Y, s->nop, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st);
+  gemm(X, s->kin, s->L[0].Wb, s->kin, Z ? Z[0] : nullptr, hid, H[0], hid, s->L[0].b, n, hid, s->kin, ACT_SILU, st, run);
+  gemm(H[0], hid, s->L[1].Wb, hid, Z ? Z[1] : nullptr, hid, H[1], hid, s->L[1].b, n, hid, hid, ACT_SILU, st, run);
+  gemm(H[1], hid, s->L[2].Wb, hid, Z ? Z[2] : nullptr, hid, H[2], hid, s->L[2].b, n, hid, hid, ACT_SILU, st, run);
+  gemm(H[2], hid, s->L[3].Wb, hid, Y, s->nop, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st, run);
   return 4;
 }
 
@@ -563,14 +853,25 @@ static void adam_all(Surrogate* s, float lr, int t, cudaStream_t st) {
 
 int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound) {
   const int n = v.nj * v.ni;
-  k_sur_features<true><<<(n + 31) / 32, dim3(32, 8), 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf, s->kin);
-  forward(s, s->Xinf, n, s->Hinf, nullptr, s->Yinf, st);
-  k_sur_check<<<grid1((size_t)n * s->nop), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->threshold, s->bad);
-  k_sur_decide<<<1, 1, 0, st>>>(s->bad, s->flag, s->counts);
+  k_sur_begin<<<1, 1, 0, st>>>(s->ctl, s->judge_every, s->jacc);
+  const int* run = s->ctl + CTL_RUN;
+  k_sur_features<true><<<(n + 127) / 128, 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf, s->kin, run);
+  forward(s, s->Xinf, n, s->Hinf, nullptr, s->Yinf, st, run);
+  k_sur_check<<<grid1((size_t)n * s->nop), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold, s->ctl,
+                                                          run);
+  k_sur_decide<<<1, 1, 0, st>>>(s->ctl, s->counts);
+  k_sur_judge_snapshot<<<grid1((size_t)5 * n * v.kz), 256, 0, st>>>(v, s->ctl, s->jsnap);
   const dim3 cg((v.nj + 31) / 32, (v.ni + 7) / 8);
-  k_sur_vvel<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, s->nop, s->ymean, s->ystd, s->flag, nsound);
-  k_sur_apply<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, s->nop, s->ymean, s->ystd, s->flag, nsound);
-  return 9;
+  k_sur_vvel<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, s->nop, s->ymean, s->ystd, s->ctl, nsound);
+  k_sur_apply<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, s->nop, s->ymean, s->ystd, s->ctl, nsound);
+  return 11;
+}
+
+int sur_after(Surrogate* s, View<float>& v, cudaStream_t st) {
+  const size_t n = (size_t)v.nj * v.ni * v.kz;
+  k_sur_judge<<<grid1(n), 256, 0, st>>>(v, s->ctl, s->jsnap, s->Yinf, s->nop, s->ymean, s->ystd, s->jacc);
+  k_sur_verdict<<<1, 1, 0, st>>>(s->ctl, s->jacc, s->tol, s->judge_every, s->max_interval, s->counts);
+  return 2;
 }
 
 static void free_sur(Surrogate* s) {
@@ -581,7 +882,7 @@ static void free_sur(Surrogate* s) {
   F(s->xmean); F(s->xstd); F(s->ymean); F(s->ystd); F(s->Xraw); F(s->Xb); F(s->T); F(s->snap); F(s->cols);
   F(s->Xbat); F(s->XbatT); F(s->Tbat); F(s->Y); F(s->dY); F(s->dYT); F(s->loss); F(s->perm);
   for (int l = 0; l < 3; ++l) { F(s->H[l]); F(s->HT[l]); F(s->Z[l]); F(s->dH[l]); F(s->dZ[l]); F(s->dZT[l]); F(s->Hinf[l]); }
-  F(s->Xinf); F(s->Yinf); F(s->flag); F(s->bad); F(s->counts);
+  F(s->Xinf); F(s->Yinf); F(s->ctl); F(s->counts); F(s->env); F(s->jacc); F(s->jsnap);
 }
 
 }  // namespace mlp
@@ -598,9 +899,10 @@ int moloch_sur_create(int kz, int capacity, int batch, unsigned long long seed, 
     return MOLOCH_ERR_ARG;
   }
   *out = nullptr;
-  if (!g_gemm_attr_done) {  // before any capture of a step that runs the GEMM
-    cudaFuncSetAttribute(k_gemm_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmem);
-    g_gemm_attr_done = 1;
+  gemm_attr();  // before any capture of a step that runs the GEMM
+  if (!encode_fn()) {
+    moloch_internal_set_error("sur_create: cuTensorMapEncodeTiled unavailable");
+    return MOLOCH_ERR_CUDA;
   }
   moloch_surrogate* s = new moloch_surrogate();
   s->kz = kz;
@@ -654,7 +956,13 @@ int moloch_sur_create(int kz, int capacity, int batch, unsigned long long seed, 
     A((void**)&s->Z[l], (size_t)batch * hid * 4); A((void**)&s->dH[l], (size_t)batch * hid * 4);
     A(&s->dZ[l], (size_t)batch * hid * 2); A(&s->dZT[l], (size_t)batch * hid * 2);
   }
-  A((void**)&s->flag, 16); A((void**)&s->bad, 16); A((void**)&s->counts, 16);
+  A((void**)&s->ctl, CTL_COUNT * sizeof(int)); A((void**)&s->counts, 4 * sizeof(unsigned long long));
+  A((void**)&s->jacc, 16 * sizeof(double));
+  A((void**)&s->env, (size_t)s->nop * 4);
+  if (e == cudaSuccess) {  // envelope 1 until moloch_sur_prepare measures it
+    std::vector<float> one(s->nop, 1.f);
+    e = cudaMemcpy(s->env, one.data(), s->nop * 4, cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) {  // BF16 copies of the initial weights: an Adam step with zero gradient
     adam_all(s, 0.f, 1, 0);
     e = cudaDeviceSynchronize();
@@ -694,8 +1002,9 @@ int moloch_sur_collect(moloch_surrogate_t* s, moloch_handle_t* h, int nsteps, in
         SUR_TRY(cudaMemcpyAsync(s->cols, pick.data(), take * sizeof(int), cudaMemcpyHostToDevice, st));
         SUR_TRY(cudaStreamSynchronize(st));
         View<float>& v = *moloch_internal_viewf(h);
-        k_sur_features<false><<<(take + 31) / 32, dim3(32, 8), 0, st>>>(v, s->cols, take, nullptr, nullptr,
-                                                                       s->Xraw + (size_t)s->npairs * s->kin, s->kin);
+        k_sur_features<false><<<(take + 127) / 128, 128, 0, st>>>(v, s->cols, take, nullptr, nullptr,
+                                                                   s->Xraw + (size_t)s->npairs * s->kin, s->kin,
+                                                                   nullptr);
         k_sur_snapshot<<<take, 128, 0, st>>>(v, s->cols, take, s->snap);
       }
       if ((rc = moloch_gpu_phase(h, 1))) return rc;
@@ -728,7 +1037,7 @@ int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long
   std::vector<double> xs(n5, 0.0), xq(n5, 0.0), ys(n5, 0.0), yq(n5, 0.0);
   for (int p = 0; p < n; ++p) {
     const float* xr = &X[(size_t)p * s->kin];
-    for (int f = 0; f < s->nin; ++f) { const double x = xr[f]; xs[f % n5] += x; xq[f % n5] += x * x; }
+    for (int f = 0; f < s->nin; ++f) { const double x = xr[f]; xs[f / 9] += x; xq[f / 9] += x * x; }
     const float* tr = &T[(size_t)p * s->nop];
     for (int q = 0; q < n5; ++q) { const double y = tr[q]; ys[q] += y; yq[q] += y * y; }
   }
@@ -746,9 +1055,16 @@ int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long
   SUR_TRY(cudaMemcpy(s->xstd, xd.data(), n5 * 4, cudaMemcpyHostToDevice));
   SUR_TRY(cudaMemcpy(s->ymean, ym.data(), n5 * 4, cudaMemcpyHostToDevice));
   SUR_TRY(cudaMemcpy(s->ystd, yd.data(), n5 * 4, cudaMemcpyHostToDevice));
+  std::vector<float> env(s->nop, 1.f);  // largest |normalised target| per output
+  for (int q = 0; q < n5; ++q) {
+    double mx = 0.0;
+    for (int p = 0; p < n; ++p) mx = std::max(mx, std::fabs((T[(size_t)p * s->nop + q] - ym[q]) / (double)yd[q]));
+    env[q] = (float)std::max(mx, 1e-3);
+  }
+  SUR_TRY(cudaMemcpy(s->env, env.data(), s->nop * 4, cudaMemcpyHostToDevice));
   k_sur_normalize<<<grid1((size_t)n * s->kin), 256>>>(s->Xraw, n, s->kin, s->nin, s->xmean, s->xstd,
-                                                      (__nv_bfloat16*)s->Xb, n5);
-  k_sur_normalize<<<grid1((size_t)n * s->nop), 256>>>(s->T, n, s->nop, s->nout, s->ymean, s->ystd, nullptr, n5);
+                                                      (__nv_bfloat16*)s->Xb, 9);
+  k_sur_normalize<<<grid1((size_t)n * s->nop), 256>>>(s->T, n, s->nop, s->nout, s->ymean, s->ystd, nullptr, 1);
   // shuffle once, keep the tail as the validation split
   std::vector<int> perm(n);
   for (int q = 0; q < n; ++q) perm[q] = q;
@@ -825,7 +1141,7 @@ int moloch_sur_train(moloch_surrogate_t* s, int iters, float lr, unsigned long l
   return rc;
 }
 
-int moloch_sur_attach(moloch_handle_t* h, moloch_surrogate_t* s, float threshold) {
+int moloch_sur_attach(moloch_handle_t* h, moloch_surrogate_t* s, float threshold, int judge_every, float tol) {
   if (!h) {
     moloch_internal_set_error("sur_attach: null handle");
     return MOLOCH_ERR_ARG;
@@ -836,28 +1152,52 @@ int moloch_sur_attach(moloch_handle_t* h, moloch_surrogate_t* s, float threshold
       moloch_internal_set_error("sur_attach: needs a trained surrogate and an FP32-storage handle with its kz");
       return MOLOCH_ERR_ARG;
     }
+    if (judge_every < 0 || !(threshold >= 0.f) || !(tol >= 0.f)) {
+      moloch_internal_set_error("sur_attach: threshold, tol >= 0, judge_every >= 0");
+      return MOLOCH_ERR_ARG;
+    }
     const int n = vp->nj * vp->ni;
     if (n > s->ninf) {
       auto F = [](void* p) { if (p) cudaFree(p); };
-      F(s->Xinf); F(s->Yinf);
+      F(s->Xinf); F(s->Yinf); F(s->jsnap);
       for (int l = 0; l < 3; ++l) F(s->Hinf[l]);
+      s->Xinf = s->Yinf = s->jsnap = nullptr;
+      s->ninf = 0;
       SUR_TRY(cudaMalloc(&s->Xinf, (size_t)n * s->kin * 2));
       SUR_TRY(cudaMalloc((void**)&s->Yinf, (size_t)n * s->nop * 4));
+      SUR_TRY(cudaMalloc((void**)&s->jsnap, (size_t)5 * n * s->kz * 4));
       for (int l = 0; l < 3; ++l) SUR_TRY(cudaMalloc(&s->Hinf[l], (size_t)n * s->hid * 2));
       s->ninf = n;
     }
     s->threshold = threshold;
+    s->judge_every = judge_every;
+    s->tol = tol;
+    s->max_interval = std::max(16 * judge_every, 1);
+    // judge_every == 0: no judge, the surrogate is enabled from the start
+    int ctl[CTL_COUNT] = {0};
+    ctl[CTL_ENABLED] = judge_every == 0 ? 1 : 0;
+    ctl[CTL_NEXTJUDGE] = 0;
+    ctl[CTL_INTERVAL] = judge_every;
+    SUR_TRY(cudaMemcpy(s->ctl, ctl, sizeof ctl, cudaMemcpyHostToDevice));
+    SUR_TRY(cudaMemset(s->counts, 0, 4 * sizeof(unsigned long long)));
   }
   return moloch_internal_attach(h, s);
 }
 
-int moloch_sur_counts(moloch_surrogate_t* s, long long* cycles, long long* fallbacks) {
+// cycles seen, cycles run by the plain loop (rejected, disabled or judge),
+// judge cycles, judge verdicts that disabled the surrogate, the largest
+// |y| / envelope since attach and the error of the last judge cycle
+int moloch_sur_counts(moloch_surrogate_t* s, long long* counts4, float* max_ratio, float* last_error) {
   if (!s) return MOLOCH_ERR_ARG;
-  unsigned long long c[2] = {0, 0};
+  unsigned long long c[4] = {0, 0, 0, 0};
+  int ctl[CTL_COUNT];
   SUR_TRY(cudaDeviceSynchronize());
   SUR_TRY(cudaMemcpy(c, s->counts, sizeof c, cudaMemcpyDeviceToHost));
-  if (cycles) *cycles = (long long)c[0];
-  if (fallbacks) *fallbacks = (long long)c[1];
+  SUR_TRY(cudaMemcpy(ctl, s->ctl, sizeof ctl, cudaMemcpyDeviceToHost));
+  if (counts4)
+    for (int q = 0; q < 4; ++q) counts4[q] = (long long)c[q];
+  if (max_ratio) std::memcpy(max_ratio, &ctl[CTL_MAXRATIO], sizeof(float));
+  if (last_error) std::memcpy(last_error, &ctl[CTL_LASTERR], sizeof(float));
   return MOLOCH_OK;
 }
 
@@ -924,6 +1264,48 @@ int moloch_sur_stats(moloch_surrogate_t* s, float* xmean, float* xstd, float* ym
       SUR_TRY(cudaMemcpy(host[q], dev[q], b, cudaMemcpyDeviceToHost));
   }
   if (set) s->ready = true;
+  return MOLOCH_OK;
+}
+
+// CUDA-event times (ms) of the inference stages of one cycle on the
+// handle's current state: ms[0] features, ms[1..4] the four layers, ms[5]
+// the envelope check.  Changes no field (nothing is committed).
+int moloch_sur_profile(moloch_surrogate_t* s, moloch_handle_t* h, double* ms, int nms) {
+  View<float>* vp = moloch_internal_viewf(h);
+  if (!s || !vp || !ms || nms < 6 || vp->nj * vp->ni > s->ninf) {
+    moloch_internal_set_error("sur_profile: attach the surrogate to this handle first");
+    return MOLOCH_ERR_ARG;
+  }
+  View<float>& v = *vp;
+  cudaStream_t st = moloch_internal_stream(h);
+  const int n = v.nj * v.ni, hid = s->hid;
+  cudaEvent_t ev[7];
+  for (auto& e : ev) SUR_TRY(cudaEventCreate(&e));
+  cudaEventRecord(ev[0], st);
+  k_sur_features<true><<<(n + 127) / 128, 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf, s->kin, nullptr);
+  cudaEventRecord(ev[1], st);
+  gemm(s->Xinf, s->kin, s->L[0].Wb, s->kin, nullptr, hid, s->Hinf[0], hid, s->L[0].b, n, hid, s->kin, ACT_SILU, st);
+  cudaEventRecord(ev[2], st);
+  gemm(s->Hinf[0], hid, s->L[1].Wb, hid, nullptr, hid, s->Hinf[1], hid, s->L[1].b, n, hid, hid, ACT_SILU, st);
+  cudaEventRecord(ev[3], st);
+  gemm(s->Hinf[1], hid, s->L[2].Wb, hid, nullptr, hid, s->Hinf[2], hid, s->L[2].b, n, hid, hid, ACT_SILU, st);
+  cudaEventRecord(ev[4], st);
+  gemm(s->Hinf[2], hid, s->L[3].Wb, hid, s->Yinf, s->nop, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st);
+  cudaEventRecord(ev[5], st);
+  // the check writes slots CTL_BAD and CTL_MAXRATIO of the block it is
+  // given: point it at the unused upper half of the control block
+  static_assert(16 + CTL_MAXRATIO < CTL_COUNT, "control block too small");
+  k_sur_check<<<grid1((size_t)n * s->nop), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
+                                                          s->ctl + 16, nullptr);
+  cudaEventRecord(ev[6], st);
+  SUR_TRY(cudaEventSynchronize(ev[6]));
+  SUR_TRY(cudaGetLastError());
+  for (int q = 0; q < 6; ++q) {
+    float t = 0.f;
+    cudaEventElapsedTime(&t, ev[q], ev[q + 1]);
+    ms[q] = t;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
   return MOLOCH_OK;
 }
 

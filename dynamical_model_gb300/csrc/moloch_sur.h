@@ -46,14 +46,23 @@ struct Surrogate {
   void* Xinf = nullptr;
   void* Hinf[3] = {};
   float* Yinf = nullptr;
-  int *flag = nullptr, *bad = nullptr;
-  unsigned long long* counts = nullptr;
-  float threshold = 8.f;
+  int* ctl = nullptr;                   // device control block (see moloch_mlp.cu)
+  unsigned long long* counts = nullptr;  // [4] cycles, plain cycles, judge cycles, judge rejections
+  double* jacc = nullptr;               // judge sums
+  float* jsnap = nullptr;               // judge cycles: pre-cycle state, 5 fields
+  int judge_every = 6;                  // plain-loop judge every n-th sound() call (0: never)
+  int max_interval = 96;                // judge interval cap after failing verdicts
+  float tol = 0.3f;                     // judge: largest relative RMS error of the increments
+  float* env = nullptr;   // [nop] largest |normalised target| seen in training
+  float threshold = 4.f;  // accepted: |y| <= threshold * env for every output
   bool ready = false;  // normalisation statistics exist
 };
 
-// one surrogate cycle in place of sound(): features, MLP, check, apply
+// one surrogate cycle before sound(): features, MLP, check, decision,
+// commit (the plain substeps then skip); returns the kernel count
 int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound);
+// after sound(): the judge's comparison on judge cycles
+int sur_after(Surrogate* s, View<float>& v, cudaStream_t st);
 
 }  // namespace mlp
 }  // namespace moloch

@@ -225,12 +225,21 @@ int moloch_tc_status(void);
  * (45*kz features, normalised per field and level); output: the increments
  * of the same five fields of the centre column over the whole cycle.
  * Layers: 45kz -> 256 -> 256 -> 256 -> 5kz, SiLU, BF16 operands and FP32
- * accumulation on tcgen05 for training and inference.  When attached, each
- * sound() first runs the MLP over every column and checks every increment
- * (finite and |normalised| <= threshold); on acceptance the increments are
- * committed and the plain substeps return immediately, otherwise the plain
- * sound loop runs unchanged (the fallback; decided on the device, so the
- * step stays one captured graph).  No reference counterpart.
+ * accumulation on tcgen05 for training and inference.  No reference
+ * counterpart.
+ * While attached, each sound() call first runs the MLP over every column.
+ * Its increments are committed (and the plain substeps return at once)
+ * when all of these hold, else the plain sound loop runs unchanged:
+ *   - every increment is finite and |normalised| <= threshold x the largest
+ *     |normalised target| of that output in the training set (x 1 before
+ *     moloch_sur_prepare);
+ *   - the cycle is not a judge cycle: every judge_every-th call (the first
+ *     included; 0 = never) runs the plain loop, which judges the
+ *     prediction of that cycle;
+ *   - the last judge found the relative RMS error of the increments (worst
+ *     of the five fields) <= tol (with judge_every == 0 it is never judged
+ *     and starts enabled).
+ * All decisions are taken on the device, so a step stays one graph.
  *   create:   kz, dataset capacity (pairs), batch rows (multiple of 64)
  *   collect:  advance the handle nsteps plain steps, recording
  *             cols_per_cycle random columns per sound() call as pairs
@@ -239,7 +248,9 @@ int moloch_tc_status(void);
  *             squared error in normalised units on training rows and on
  *             the validation split
  *   attach:   s == NULL detaches; the surrogate must outlive the attachment
- *   counts:   sound() calls seen while attached and how many fell back
+ *   counts:   counts4 = {sound() calls, calls run by the plain loop, judge
+ *             calls, judge verdicts that disabled the surrogate}; the
+ *             largest |y| / envelope since attach; the last judge's error
  *   param:    layer weights [out][in] and bias, read (set 0) or written
  *   gradients: one forward+backward pass on n == batch rows of normalised
  *             features X [n][kin] and targets T [n][nop]: summed squared
@@ -254,12 +265,16 @@ int moloch_sur_pairs(moloch_surrogate_t* s);
 int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long long seed);
 int moloch_sur_train(moloch_surrogate_t* s, int iters, float lr, unsigned long long seed, float* train_loss,
                      float* val_loss);
-int moloch_sur_attach(moloch_handle_t* h, moloch_surrogate_t* s, float threshold);
-int moloch_sur_counts(moloch_surrogate_t* s, long long* cycles, long long* fallbacks);
+int moloch_sur_attach(moloch_handle_t* h, moloch_surrogate_t* s, float threshold, int judge_every, float tol);
+int moloch_sur_counts(moloch_surrogate_t* s, long long* counts4, float* max_ratio, float* last_error);
 int moloch_sur_param(moloch_surrogate_t* s, int layer, float* W, float* b, int set, int* in_out);
 int moloch_sur_gradients(moloch_surrogate_t* s, const float* X, const float* T, int n, float* loss, int layer,
                          float* gW, float* gb);
 int moloch_sur_dims(moloch_surrogate_t* s, int* dims);
+/* CUDA-event times (ms) of the inference stages of one cycle on the
+ * attached handle's current state: features, the four layers, the check
+ * (nms >= 6).  Changes no field. */
+int moloch_sur_profile(moloch_surrogate_t* s, moloch_handle_t* h, double* ms, int nms);
 /* normalisation statistics, 5*kz each (field-major: u, v, w, pai, tetav):
  * read (set 0) or write (set != 0, which also makes the surrogate
  * attachable without moloch_sur_prepare) */

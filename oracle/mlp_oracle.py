@@ -7,7 +7,7 @@ are the ones the GPU computes:
 
 * features(): the 45*kz inputs of a column -- u, v, w (levels 2..kz+1), pai
   and tetav of the column and its 8 periodic neighbours, feature index
-  (nb*5 + f)*kz + k with nb = (di+1)*3 + (dj+1);
+  (f*kz + k)*9 + nb with nb = (di+1)*3 + (dj+1);
 * forward() / backward(): the MLP 45kz -> 256 -> 256 -> 256 -> 5kz with SiLU,
   mean-squared-error loss and its gradients, with the GPU's BF16 roundings
   (operands and stored activations rounded to nearest-even BF16, products
@@ -41,24 +41,22 @@ def features(st):
     u = st["u"]
     kz, ni, nj = u.shape
     flds = (st["u"], st["v"], st["w"][1:kz + 1], st["pai"], st["tetav"])
-    out = np.empty((ni * nj, 9, 5, kz), np.float64)
+    out = np.empty((ni * nj, 5, kz, 9), np.float64)
     for di in (-1, 0, 1):
         for dj in (-1, 0, 1):
             nb = (di + 1) * 3 + (dj + 1)
             for f, a in enumerate(flds):
                 sh = np.roll(np.roll(a, -di, axis=1), -dj, axis=2)  # value at (i+di, j+dj)
-                out[:, nb, f, :] = sh.reshape(kz, ni * nj).T
+                out[:, f, :, nb] = sh.reshape(kz, ni * nj).T
     return out.reshape(ni * nj, 45 * kz)
 
 
 def normalise(X, xmean, xstd, kin):
     """Normalised features padded with zeros to kin columns."""
     n, nin = X.shape
-    kz = xmean.shape[-1]
-    period = 5 * kz
     m = np.asarray(xmean, np.float64).ravel()
     s = np.asarray(xstd, np.float64).ravel()
-    idx = np.arange(nin) % period
+    idx = np.arange(nin) // 9  # statistic of field plane f * kz + k
     out = np.zeros((n, kin))
     out[:, :nin] = (X - m[idx]) / s[idx]
     return out

@@ -9,6 +9,10 @@
   <= 5e-3;
 * fallback: a surrogate whose check rejects every cycle leaves the step
   bit-identical to the plain FP32 step (graph and stepwise);
+* judge: judge cycles run the plain loop; a judge with tol 0 keeps the
+  surrogate off with a doubling interval (bit-identical to the plain step),
+  a judge with an infinite tol enables it between judge cycles (schedule
+  and counts checked);
 * training: collect, prepare, train on a small hilly domain; the validation
   loss falls and the surrogate run stays within a stated error of the FP64
   run (see the test for the bound).
@@ -71,13 +75,13 @@ def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz):
     rng = np.random.default_rng(jx)
     P = _random_params(sur, rng)
     feats = mo.features(pre)
-    x5 = feats.reshape(-1, 9, 5, kz)
-    xmean = x5.mean(axis=(0, 1)).astype(np.float32)
-    xstd = (x5.std(axis=(0, 1)) + 1e-3).astype(np.float32)
+    x5 = feats.reshape(-1, 5, kz, 9)
+    xmean = x5.mean(axis=(0, 3)).astype(np.float32)
+    xstd = (x5.std(axis=(0, 3)) + 1e-3).astype(np.float32)
     ymean = rng.normal(0, 0.05, (5, kz)).astype(np.float32)
     ystd = rng.uniform(0.2, 0.5, (5, kz)).astype(np.float32)
     sur.set_stats(xmean, xstd, ymean, ystd)
-    sur.attach(g, threshold=1e30)
+    sur.attach(g, threshold=1e30, judge_every=0)
     g.phase(1)
     assert sur.counts() == (1, 0)
     post = _state(g)
@@ -106,7 +110,7 @@ def test_sur_fallback_is_bit_identical(gpu_lib):
     sur = gpu_lib.Surrogate(kz, capacity=256, batch=128)
     _random_params(sur, np.random.default_rng(2))
     sur.set_stats(np.zeros((5, kz)), np.ones((5, kz)), np.zeros((5, kz)), np.ones((5, kz)))
-    sur.attach(b, threshold=0.0)  # nothing passes: every cycle falls back
+    sur.attach(b, threshold=0.0, judge_every=0)  # nothing passes: every cycle falls back
     for s in range(1, 3):
         a.moloch(s)
         b.moloch(s)
@@ -116,6 +120,45 @@ def test_sur_fallback_is_bit_identical(gpu_lib):
     assert sur.counts() == (4 * nadv, 4 * nadv)
     for f in ("u", "v", "w", "pai", "t", "qv", "ps", "s"):
         assert np.array_equal(a.get(f), b.get(f)), f
+    sur.close()
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("tol,judge_every", [(0.0, 2), (1e30, 3)])
+def test_sur_judge(gpu_lib, tol, judge_every):
+    jx, iy, kz = 32, 24, 10
+    a = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    b = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    for g in (a, b):
+        g.setup_idealized(hills=((300.0, 16.0, 12.0, 3.0),), u0=4.0)
+    sur = gpu_lib.Surrogate(kz, capacity=256, batch=128)
+    _random_params(sur, np.random.default_rng(4), scale=0.3)
+    sur.set_stats(np.zeros((5, kz)), np.ones((5, kz)), np.zeros((5, kz)), np.full((5, kz), 1e-4))
+    sur.attach(b, threshold=1e30, judge_every=judge_every, tol=tol)
+    a.run(2, graph=True)
+    b.run(2, graph=True)
+    a.moloch(3)
+    b.moloch(3)
+    n = 3 * a.params.mo_nadv
+    c = sur.stats_counts()
+    # judge schedule: first cycle, then judge_every later after a pass,
+    # doubling (up to 16 x judge_every) after a failure
+    judged, nxt, iv = 0, 0, judge_every
+    for cyc in range(n):
+        if cyc == nxt:
+            judged += 1
+            iv = judge_every if tol > 0 else min(2 * iv, 16 * judge_every)
+            nxt = cyc + iv
+    assert c["cycles"] == n and c["judged"] == judged, (c, judged)
+    if tol == 0.0:
+        assert c["judge_rejections"] == judged and c["plain"] == n
+        for f in ("u", "v", "w", "pai", "t", "ps"):
+            assert np.array_equal(a.get(f), b.get(f)), f
+    else:
+        assert c["judge_rejections"] == 0 and c["plain"] == judged
+        assert np.isfinite(c["last_judge_error"])
+        assert not np.array_equal(a.get("pai"), b.get("pai"))
     sur.close()
     a.close()
     b.close()
@@ -144,15 +187,14 @@ def test_sur_train_and_run(gpu_lib):
     run = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     for g in (ref, pl, run):
         g.setup_idealized(**setup)
-    sur.attach(run, threshold=8.0)
+    sur.attach(run)
     for g in (ref, pl, run):
         g.run(6, graph=True)
-    cyc, fb = sur.counts()
+    c = sur.stats_counts()
     e_pl = np.sqrt(np.mean((pl.get("tetav") - ref.get("tetav")) ** 2))
     e_sur = np.sqrt(np.mean((run.get("tetav") - ref.get("tetav")) ** 2))
-    print(f"surrogate: cycles {cyc}, fallbacks {fb}, tetav rms vs fp64: plain fp32 {e_pl:.3g}, "
-          f"surrogate {e_sur:.3g}")
-    assert cyc == 6 * run.params.mo_nadv
+    print(f"surrogate: {c}, tetav rms vs fp64: plain fp32 {e_pl:.3g}, surrogate {e_sur:.3g}")
+    assert c["cycles"] == 6 * run.params.mo_nadv
     assert np.isfinite(e_sur) and e_sur <= 0.05
     sur.close()
     for g in (col, ref, pl, run):

@@ -62,4 +62,4 @@ def test_feature_layout():
             di, dj = nb // 3 - 1, nb % 3 - 1
             for f in range(5):
                 for k in range(kz):
-                    assert X[c, (nb * 5 + f) * kz + k] == flds[f][k, (i + di) % ni, (j + dj) % nj]
+                    assert X[c, (f * kz + k) * 9 + nb] == flds[f][k, (i + di) % ni, (j + dj) % nj]
