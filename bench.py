@@ -12,8 +12,13 @@ substeps.  value = jx*iy*kz*steps / time of the timed steps (device time,
 CUDA events on the library's stream), summed over replicas for --gpus N
 (one independent domain per GPU, "replicas only": the path has no exchange
 between domains).  The headline path is FP32 storage with the FP64
-tridiagonal solve; the plain FP64 step is timed beside it on the same state
-and the error of the FP32 path against it is reported.
+tridiagonal solve and the learned acoustic-cycle surrogate attached under
+its judge: the surrogate is trained first (pairs collected from plain steps
+of a scratch domain, outside the timed region), and every sound() call of
+the timed steps runs it or the plain sound loop as the on-device judge
+decides.  The plain FP32 step and the plain FP64 step are timed beside it
+on the same state, and the errors against the FP64 step are reported.
+--workload surrogate runs the 256 x 256 x 40 surrogate case instead.
 
 --impl reference times the CPU restatement of the reference (the reference
 itself is Fortran and no Fortran compiler exists on these machines) on the
@@ -55,6 +60,11 @@ ALG_WORDS = {
     "k_stag_from_x": 6,       # r: ux vx wx | w: u v w
     "k_postdiag": 12,         # r: pai tetav q(5) | w: tvirt t p rho qsat
 }
+# DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of one launch
+# from an ncu capture of the kernel, and the grid points of that capture;
+# scaled by the point count to the benchmarked size (traffic grows in
+# proportion: one pass over each array per launch)
+NCU_TRAFFIC = {"k_sound_column": (336.8e6, 256 * 256 * 60)}
 # whole-step algorithmic words per grid point of the fused design target
 # (pre-diag 11 + 3 sound cycles x 91 + 3 advection steps x 23 + post-diag 11)
 B_ALG_WORDS = 364
@@ -248,9 +258,11 @@ def time_steps(torch, d, stream, steps, graph=True):
 
 
 def e2e_steps(torch, dm, d, stream, steps):
-    """Through the reference-facing C ABI with host arrays: upload the
-    prognostic state, one moloch() call, download the output fields t, ps
-    (the fields the reference driver writes, regcm_dynamical_core.F90:203-216)."""
+    """Through the reference-facing C ABI with host arrays, as a driver time
+    loop does it: every step uploads the prognostic state (u, v, w, pai, t,
+    qx), runs one moloch() call and reads back the output fields t and ps
+    (the fields the reference driver writes, regcm_dynamical_core.F90:203-216)
+    with the asynchronous output path, whose copy overlaps the next step."""
     names_in = ("u", "v", "w", "pai", "t", "qx")
     host = {n: d.download(n) for n in names_in}
     e0 = torch.cuda.Event(enable_timing=True)
@@ -263,8 +275,10 @@ def e2e_steps(torch, dm, d, stream, steps):
         for n in names_in:
             d.upload(n, host[n])
         d.moloch(s + 1)
-        out = (d.download("t"), d.download("ps"))
-        host["t"] = out[0]
+        if s > 0:
+            out = d.output_finish()
+        d.output_start()
+    out = d.output_finish()
     e1.record(stream)
     e1.synchronize()
     wall = time.perf_counter() - t0
@@ -288,6 +302,85 @@ def ensemble_members(dm, stream, n=64, seed=2024):
         d.setup_idealized(pert_amp=1.0, pert_levels=kz, seed=seed + m, u0=u0, v0=1.0)
         out.append(d)
     return out
+
+
+SUR = {"collect_steps": 4, "cols_per_cycle": 2048, "iters": 3000, "lr": 1e-3, "batch": 256,
+       "threshold": 4.0, "judge_every": 6, "tol": 0.3}
+
+
+def train_surrogate(dm, mode, stream, jx, iy, kz, hills, cfg=SUR):
+    """Collect (state, post-sound-cycle state) pairs from plain steps of a
+    scratch domain and train the surrogate on the GPU."""
+    t0 = time.perf_counter()
+    scratch = dm.Moloch(jx, iy, kz, mode=mode, stream=stream)
+    scratch.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED + 7)
+    cap = cfg["collect_steps"] * scratch.params.mo_nadv * cfg["cols_per_cycle"]
+    sur = dm.Surrogate(kz, capacity=cap, batch=cfg["batch"], seed=1)
+    pairs = sur.collect(scratch, cfg["collect_steps"], cols_per_cycle=cfg["cols_per_cycle"])
+    sur.prepare(0.1)
+    _, v0 = sur.train(0)
+    tl, vl = sur.train(cfg["iters"], lr=cfg["lr"])
+    scratch.close()
+    info = {"pairs": pairs, "iters": cfg["iters"], "batch": cfg["batch"], "val_loss_untrained": v0,
+            "val_loss": vl, "train_loss": tl, "seconds": time.perf_counter() - t0,
+            "mlp": f"{45 * kz}->256->256->256->{5 * kz}, SiLU, BF16 operands, FP32 accumulate (tcgen05)"}
+    return sur, info
+
+
+def surrogate_forced_error(dm, sur, stream, jx, iy, kz, hills, ref_fields, steps):
+    """The surrogate committed on every cycle (no judge, no envelope check),
+    from the same initial state as the FP64 reference: its error after
+    `steps` steps.  Shows what the judge protects against."""
+    d = dm.Moloch(jx, iy, kz, mode="fp32_mixed", stream=stream)
+    d.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED)
+    sur.attach(d, threshold=1e30, judge_every=0)
+    d.run(steps, graph=True)
+    out = {"steps": steps,
+           "theta_rmse_K": rmse(d.get("t") / d.get("pai"), ref_fields["theta"]),
+           "u_rmse_ms": rmse(d.get("u"), ref_fields["u"]),
+           "v_rmse_ms": rmse(d.get("v"), ref_fields["v"])}
+    sur.detach()
+    d.close()
+    return out
+
+
+def run_accuracy(args, torch, dm, stream):
+    """Long-run error of the FP32 paths against the FP64 GPU step (which
+    matches the FP64 oracle to <= 1e-9 relative L2 after 100 steps): the
+    512 x 512 x 60 workload advanced --steps steps, RMSE checkpoints every
+    --steps/10 steps."""
+    sptr = stream.cuda_stream
+    sur, sur_train = train_surrogate(dm, "fp32_mixed", sptr, JX, IY, KZ, HILLS)
+    d64 = make_domain(dm, "fp64", sptr)
+    dmix = make_domain(dm, "fp32_mixed", sptr)
+    dsur = make_domain(dm, "fp32_mixed", sptr)
+    sur.attach(dsur, threshold=SUR["threshold"], judge_every=SUR["judge_every"], tol=SUR["tol"])
+    every = max(1, args.steps // 10)
+    curve = []
+    done = 0
+    t0 = time.perf_counter()
+    while done < args.steps:
+        n = min(every, args.steps - done)
+        for d in (d64, dmix, dsur):
+            d.run(n, graph=True)
+        done += n
+        th64 = d64.get("t") / d64.get("pai")
+        u64, v64 = d64.get("u"), d64.get("v")
+        row = {"step": done}
+        for name, d in (("fp32", dmix), ("fp32_surrogate", dsur)):
+            row[name] = {"theta_rmse_K": rmse(d.get("t") / d.get("pai"), th64),
+                         "u_rmse_ms": rmse(d.get("u"), u64), "v_rmse_ms": rmse(d.get("v"), v64),
+                         "w_rmse_ms": rmse(d.get("w"), d64.get("w"))}
+        curve.append(row)
+    line = {"metric": "RMSE against the FP64 GPU step", "workload": f"{JX}x{IY}x{KZ}", "steps": args.steps,
+            "target": {"theta_rmse_K": 0.05, "u_v_rmse_ms": 0.05}, "curve": curve,
+            "surrogate": {"training": sur_train, "judge": sur.stats_counts()},
+            "seconds": time.perf_counter() - t0}
+    print(json.dumps(line), flush=True)
+    sur.close()
+    for d in (d64, dmix, dsur):
+        d.close()
+    return 0
 
 
 def run_ensemble(args, dist, rank, ws):
@@ -348,8 +441,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--size", default=None, help="JXxIYxKZ override (profiling a smaller case)")
     ap.add_argument("--only", default=None, choices=["mixed", "fp64"], help="time one path only (profiling)")
-    ap.add_argument("--workload", default="single", choices=["single", "ensemble", "full1024"],
-                    help="single: 512x512x60 (headline); ensemble: 64 uneven members; full1024: 1024x1024x60")
+    ap.add_argument("--workload", default="single",
+                    choices=["single", "ensemble", "full1024", "surrogate", "accuracy"],
+                    help="single: 512x512x60 (headline); ensemble: 64 uneven members; full1024: 1024x1024x60; "
+                         "surrogate: 256x256x40 surrogate case; accuracy: --steps-long error run vs FP64")
     args = ap.parse_args()
     global JX, IY, KZ, HILLS
     if args.size:
@@ -365,6 +460,11 @@ def main():
     import dynamical_model_gb300 as dm
     if args.workload == "ensemble":
         return run_ensemble(args, dist, rank, ws)
+    if args.workload == "surrogate":
+        # learned acoustic-cycle surrogate case: 256 x 256 x 40, 20k training pairs
+        JX, IY, KZ = 256, 256, 40
+        HILLS = ((500.0, (JX + 1) / 2.0, (IY + 1) / 2.0, 10.0),)
+        SUR.update(collect_steps=7, cols_per_cycle=1024, iters=4000)
     if args.workload == "full1024":
         JX, IY = 1024, 1024
         HILLS = ((1000.0, (JX + 1) / 3.0, (IY + 1) / 2.0, 20.0), (1000.0, 2.0 * (JX + 1) / 3.0, (IY + 1) / 2.0, 20.0))
@@ -374,6 +474,8 @@ def main():
     stream = torch.cuda.Stream(device=device)
     sptr = stream.cuda_stream
 
+    if args.workload == "accuracy":
+        return run_accuracy(args, torch, dm, stream) if rank == 0 else 0
     # ---- headline path: FP32 storage + FP64 solve --------------------------
     if args.only:
         d, _ = tuned(dm, "fp32_mixed" if args.only == "mixed" else "fp64", sptr)
@@ -384,37 +486,56 @@ def main():
                               "value": JX * IY * KZ * args.steps / (ms / 1e3), "gpu_launches": launches}))
         d.close()
         return 0
-    dmix, tune_mix = tuned(dm, "fp32_mixed", sptr)
-    d64, tune_64 = tuned(dm, "fp64", sptr)
-    dmix.run(args.warmup, graph=True)
-    d64.run(args.warmup, graph=True)
-    dmix.sync(); d64.sync()
+    return run_single(args, dist, rank, ws, torch, dm, stream, local, device)
 
+
+def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
+    sptr = stream.cuda_stream
+    gp = JX * IY * KZ
+    # ---- the surrogate: trained on the GPU outside the timed region --------
+    sur, sur_train = train_surrogate(dm, "fp32_mixed", sptr, JX, IY, KZ, HILLS)
+    dsur, tune_mix = tuned(dm, "fp32_mixed", sptr)
+    sur.attach(dsur, threshold=SUR["threshold"], judge_every=SUR["judge_every"], tol=SUR["tol"])
+    dmix = make_domain(dm, "fp32_mixed", sptr)
+    dmix.set_tuning(tune_mix)
+    d64, tune_64 = tuned(dm, "fp64", sptr)
+    for d in (dsur, dmix, d64):
+        d.run(args.warmup, graph=True)
+        d.sync()
+
+    # ---- timed: FP32 + surrogate (headline), plain FP32, plain FP64 ---------
     clk = ClockSampler(local)
     barrier(dist, device)
     clk.start()
-    ms_mix, launches_mix = time_steps(torch, dmix, stream, args.steps)
+    ms_sur, launches_sur = time_steps(torch, dsur, stream, args.steps)
     barrier(dist, device)
     clocks = clk.stop()
+    ms_sur = reduce_max(dist, ms_sur, device)
+    ms_mix, launches_mix = time_steps(torch, dmix, stream, args.steps)
     ms_mix = reduce_max(dist, ms_mix, device)
-    # plain FP64 on the same state and the same number of steps
     ms_64, launches_64 = time_steps(torch, d64, stream, args.steps)
     ms_64 = reduce_max(dist, ms_64, device)
-
-    gp = JX * IY * KZ
     n_dom = reduce_sum(dist, 1.0, device)
-    value = n_dom * gp * args.steps / (ms_mix / 1e3)
+    value = n_dom * gp * args.steps / (ms_sur / 1e3)
+    value_mix = n_dom * gp * args.steps / (ms_mix / 1e3)
     value64 = n_dom * gp * args.steps / (ms_64 / 1e3)
 
-    # error of the FP32 path against the FP64 GPU step after warmup+steps steps
-    th_mix = dmix.get("tetav")
-    err = {"steps": args.warmup + args.steps,
-           "theta_rmse_K": rmse(dmix.get("t") / dmix.get("pai"), d64.get("t") / d64.get("pai")),
-           "u_rmse_ms": rmse(dmix.get("u"), d64.get("u")),
-           "v_rmse_ms": rmse(dmix.get("v"), d64.get("v")),
-           "w_rmse_ms": rmse(dmix.get("w"), d64.get("w")),
-           "ps_rmse_Pa": rmse(dmix.get("ps"), d64.get("ps"))}
-    del th_mix
+    # ---- errors against the FP64 GPU step after warmup + steps steps --------
+    ref = {"theta": d64.get("t") / d64.get("pai"), "u": d64.get("u"), "v": d64.get("v"), "w": d64.get("w"),
+           "ps": d64.get("ps")}
+
+    def errors(d):
+        return {"steps": args.warmup + args.steps,
+                "theta_rmse_K": rmse(d.get("t") / d.get("pai"), ref["theta"]),
+                "u_rmse_ms": rmse(d.get("u"), ref["u"]), "v_rmse_ms": rmse(d.get("v"), ref["v"]),
+                "w_rmse_ms": rmse(d.get("w"), ref["w"]), "ps_rmse_Pa": rmse(d.get("ps"), ref["ps"])}
+
+    err_sur = errors(dsur)
+    err_mix = errors(dmix)
+    judge = sur.stats_counts()
+    inference_ms = sur.profile(dsur)
+    forced = surrogate_forced_error(dm, sur, sptr, JX, IY, KZ, HILLS, ref, args.warmup + args.steps)
+    sur.attach(dsur, threshold=SUR["threshold"], judge_every=SUR["judge_every"], tol=SUR["tol"])
 
     # ---- per-kernel CUDA-event profile of one step (roofline) ---------------
     prof = dmix.profile_step()
@@ -430,8 +551,9 @@ def main():
     roofline = {"bound": "hbm", "kernel": tname, "achieved": achieved, "peak": peak,
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
-                "traffic": None,
-                "step_alg_GBps": B_ALG_WORDS * esz * value / n_dom / 1e9}
+                "traffic": (NCU_TRAFFIC[tname][0] * gp / NCU_TRAFFIC[tname][1]) if tname in NCU_TRAFFIC else None,
+                "traffic_note": "ncu dram bytes of one launch at 256x256x60, scaled by grid points",
+                "step_alg_GBps": B_ALG_WORDS * esz * value_mix / n_dom / 1e9}
     kernels = {k: {"ms": round(v[0], 4), "launches": v[1],
                    "GBps_alg": (ALG_WORDS.get(k, 0) * esz * gp * v[1] / (v[0] / 1e3) / 1e9) if v[0] > 0 else None}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
@@ -440,46 +562,58 @@ def main():
     # ---- end to end through the C ABI with host arrays ----------------------
     e2e = None
     if not args.no_e2e:
-        ms_e2e, h2d, d2h = e2e_steps(torch, dm, dmix, stream, max(2, min(args.steps, 5)))
         n_e2e = max(2, min(args.steps, 5))
+        ms_e2e, h2d, d2h = e2e_steps(torch, dm, dsur, stream, n_e2e)
         ms_e2e = reduce_max(dist, ms_e2e, device)
         e2e = {"value": n_dom * gp * n_e2e / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": n_e2e,
-               "path": "moloch_gpu_upload(u,v,w,pai,t,qx) + moloch_gpu_step + moloch_gpu_download(t,ps), FP64 host arrays"}
+               "path": "moloch_gpu_upload(u,v,w,pai,t,qx) + moloch_gpu_step + moloch_gpu_output_start/finish(t,ps), "
+                       "FP64 host arrays, FP32 + surrogate handle"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        v, dt, threads = cpu_sample(2)
+        v, dt, threads = cpu_sample(2, kz=KZ)
         cpu = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"2 steps of a 256x256x60 sample of the workload, {dt:.1f} s, OpenMP C restatement "
+               "sample": f"2 steps of a 256x256x{KZ} sample of the workload, {dt:.1f} s, OpenMP C restatement "
                          f"of nompi/mod_moloch.F90 (no Fortran compiler: reference build unavailable)"}
 
     if rank == 0:
+        n_cyc = judge["cycles"]
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_mix / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 tridiagonal solve)",
+            "warmup": args.warmup, "ms_per_step": ms_sur / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 tridiagonal solve; bf16/f32 surrogate)",
             "data": "synthetic",
-            "config": {"workload": f"{JX}x{IY}x{KZ} idealized state, 500 m hill r=20 gp, seeded +-0.5 K theta noise",
-                       "jx": JX, "iy": IY, "kz": KZ, "path": "fp32_mixed (surrogate not in this path)",
+            "config": {"workload": f"{JX}x{IY}x{KZ} idealized state, hill {HILLS[0][0]:.0f} m r={HILLS[0][3]:.0f} gp, "
+                                   f"seeded +-0.5 K theta noise",
+                       "jx": JX, "iy": IY, "kz": KZ,
+                       "path": "fp32_mixed + acoustic-cycle surrogate under the plain-loop judge",
                        "graph": True, "parallelism": f"replicas x{ws}",
                        "autotuned": {"fp32_mixed": tune_mix, "fp64": tune_64},
                        "l2": "inputs larger than L2 (state > 1 GB per domain)"},
+            "speedup_vs_fp64": value / value64,
+            "error_vs_fp64": err_sur,
+            "fp32_plain": {"value": value_mix, "ms_per_step": ms_mix / args.steps, "gpu_launches": launches_mix,
+                           "speedup_vs_fp64": value_mix / value64, "error_vs_fp64": err_mix},
             "fp64_plain": {"value": value64, "ms_per_step": ms_64 / args.steps, "dtype": "f64",
                            "gpu_launches": launches_64},
-            "speedup_vs_fp64": value / value64,
-            "error_vs_fp64": err,
+            "surrogate": {"training": sur_train, "attach": {k: SUR[k] for k in ("threshold", "judge_every", "tol")},
+                          "judge": judge,
+                          "committed_cycles": n_cyc - judge["plain"],
+                          "inference_ms_per_cycle": inference_ms,
+                          "forced_on_error_vs_fp64": forced},
             "roofline": roofline,
             "kernels": kernels,
             "kernels_fp64": kernels64,
             "cpu_baseline": cpu,
             "e2e": e2e,
-            "gpu_launches": launches_mix,
+            "gpu_launches": launches_sur,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
-    dmix.close()
-    d64.close()
+    sur.close()
+    for d in (dsur, dmix, d64):
+        d.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0

@@ -107,6 +107,11 @@ _PROTOS = {
     "moloch_tc_status": (ctypes.c_int, []),
     "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
                                   [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
+    "moloch_gpu_output_start": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_output_finish": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                                ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_int),
+                                                ctypes.POINTER(ctypes.c_int)]),
     "moloch_sur_create": (ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_ulonglong,
                                          ctypes.POINTER(ctypes.c_void_p)]),
     "moloch_sur_collect": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
@@ -291,6 +296,23 @@ class Moloch:
         _check(self.L.moloch_gpu_download(self.h, FIELD[name], a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                                           lb, ub))
         return a
+
+    def output_start(self):
+        """Snapshot t and ps now (in stream order) and start their copy to
+        the host; the next steps overlap the copy."""
+        _check(self.L.moloch_gpu_output_start(self.h))
+
+    def output_finish(self):
+        """(t, ps) of the last output_start, reference layout with halos."""
+        arrs, args = [], []
+        for name in ("t", "ps"):
+            bnds = field_bounds(name, self.jx, self.iy, self.kz)
+            a = np.zeros(tuple(u - l + 1 for l, u in bnds), dtype=np.float64, order="F")
+            arrs.append(a)
+            args += [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                     (ctypes.c_int * 4)(*[l for l, _ in bnds]), (ctypes.c_int * 4)(*[u for _, u in bnds])]
+        _check(self.L.moloch_gpu_output_finish(self.h, *args))
+        return arrs[0], arrs[1]
 
     def get_1d(self, name):
         """A 1-D level table (zita, zitah) as uploaded."""

@@ -17,7 +17,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <cstdlib>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/moloch_gb300.h"
@@ -131,6 +133,33 @@ void scatter_periodic(const std::vector<double>& in, const FieldShape& s, int nj
       }
 }
 
+// host threads for the layout conversion of uploads and downloads
+// (MOLOCH_HOST_THREADS overrides; default: the hardware threads, at most 32)
+unsigned host_threads() {
+  static unsigned n = [] {
+    const char* e = std::getenv("MOLOCH_HOST_THREADS");
+    long v = e ? std::strtol(e, nullptr, 10) : 0;
+    if (v <= 0) v = (long)std::thread::hardware_concurrency();
+    return (unsigned)std::max(1L, std::min(v, 32L));
+  }();
+  return n;
+}
+
+// fn(begin, end) over [0, n) split across the host threads
+template <class F>
+void host_parallel(size_t n, F&& fn) {
+  const unsigned nt = (unsigned)std::min<size_t>(host_threads(), (n + 7) / 8);
+  if (nt <= 1) {
+    fn((size_t)0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  th.reserve(nt - 1);
+  for (unsigned t = 1; t < nt; ++t) th.emplace_back([&, t] { fn(n * t / nt, n * (t + 1) / nt); });
+  fn((size_t)0, n / nt);
+  for (auto& x : th) x.join();
+}
+
 double gzita(double zita, double ztop, double a0) {  // nompi/mod_zita.F90:109-120
   double ratio = zita / ztop;
   double r2 = ratio * ratio, r3 = r2 * ratio;
@@ -158,8 +187,19 @@ struct moloch_handle {
   cudaGraph_t graph[2] = {nullptr, nullptr};
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   double* hres = nullptr;  // pinned diag result
+  // output path: device snapshot of t and ps, copied to pinned host memory
+  // on a second stream while the step stream runs on
+  void* out_dev = nullptr;
+  void* out_host = nullptr;
+  cudaStream_t out_stream = nullptr;
+  cudaEvent_t out_taken = nullptr, out_done = nullptr;
+  bool out_pending = false;
   void* stage = nullptr;   // pinned staging buffer, one 3-D field (kz+1 levels) of doubles
   size_t stage_bytes = 0;
+  // the two halves of `stage` as a ring for streamed transfers: the event
+  // of a half is recorded after the copy that last used it
+  cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+  bool stage_busy[2] = {false, false};
   // host copies of the static inputs (dense interiors)
   std::vector<double> zeta, fmz, fmzf, msfx, msfu, msfv, hx, hy, ulat, vlat, zita, zitah;
   unsigned uploaded = 0;  // bit per field id
@@ -262,6 +302,95 @@ int download_dense(moloch_handle* h, const T* src, size_t n, std::vector<double>
     std::memcpy(out.data(), st, bytes);
   else
     for (size_t q = 0; q < n; ++q) out[q] = (double)st[q];
+  return MOLOCH_OK;
+}
+
+// Streamed transfer of one field between a bounded host array (Fortran
+// layout, halo rings included) and its dense device copy.  The field is cut
+// into level chunks that fit one half of the pinned staging buffer; host
+// threads convert a chunk (interior gather + bulk-type conversion, or
+// periodic scatter + conversion back) while the other half is in flight.
+// An upload returns once its chunks are staged: the copies complete in
+// stream order before any later work of the handle.
+int stage_wait(moloch_handle* h, int slot) {
+  if (h->stage_busy[slot]) {
+    CUDA_TRY(cudaEventSynchronize(h->stage_ev[slot]));
+    h->stage_busy[slot] = false;
+  }
+  return MOLOCH_OK;
+}
+
+template <class T>
+int upload_streamed(moloch_handle* h, T* dst, const double* base, const FieldShape& s, int nj, int ni, int nk,
+                    int level4) {
+  const long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1;
+  const long n3 = s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1;
+  const long off4 = (long)level4 * n1 * n2 * n3;
+  const size_t plane = (size_t)nj * ni;
+  const int chunk = (int)std::max<size_t>(1, (h->stage_bytes / 2) / (sizeof(T) * plane));
+  int slot = 0;
+  for (int k0 = 0; k0 < nk; k0 += chunk, slot ^= 1) {
+    const int k1 = std::min(nk, k0 + chunk);
+    int rc = stage_wait(h, slot);
+    if (rc) return rc;
+    T* st = (T*)((char*)h->stage + slot * (h->stage_bytes / 2));
+    host_parallel((size_t)(k1 - k0) * ni, [&](size_t r0, size_t r1) {
+      for (size_t r = r0; r < r1; ++r) {
+        const int kk = k0 + (int)(r / ni), i = (int)(r % ni) + 1;
+        const long q = off4 + (long)(s.ndim >= 3 ? kk + 1 - s.lb[2] : 0) * n1 * n2 +
+                       (long)(s.ndim >= 2 ? i - s.lb[1] : 0) * n1 + (1 - s.lb[0]);
+        const double* src = base + q;
+        T* o = st + r * nj;
+        for (int j = 0; j < nj; ++j) o[j] = (T)src[j];
+      }
+    });
+    CUDA_TRY(cudaMemcpyAsync(dst + (size_t)k0 * plane, st, sizeof(T) * plane * (k1 - k0), cudaMemcpyHostToDevice,
+                             h->stream));
+    CUDA_TRY(cudaEventRecord(h->stage_ev[slot], h->stream));
+    h->stage_busy[slot] = true;
+  }
+  return MOLOCH_OK;
+}
+
+template <class T>
+int download_streamed(moloch_handle* h, const T* src, const FieldShape& s, int nj, int ni, int nk, int level4,
+                      double* base) {
+  const long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1;
+  const long n3 = s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1;
+  const long off4 = (long)level4 * n1 * n2 * n3;
+  const int k1b = s.ndim >= 3 ? s.lb[2] : 1, i1 = s.ndim >= 2 ? s.lb[1] : 1, i2 = s.ndim >= 2 ? s.ub[1] : 1;
+  const size_t plane = (size_t)nj * ni;
+  const int chunk = (int)std::max<size_t>(1, (h->stage_bytes / 2) / (sizeof(T) * plane));
+  const int nchunks = (nk + chunk - 1) / chunk;
+  auto issue = [&](int c) -> int {
+    const int slot = c & 1, k0 = c * chunk, k1 = std::min(nk, k0 + chunk);
+    int rc = stage_wait(h, slot);
+    if (rc) return rc;
+    T* st = (T*)((char*)h->stage + slot * (h->stage_bytes / 2));
+    CUDA_TRY(cudaMemcpyAsync(st, src + (size_t)k0 * plane, sizeof(T) * plane * (k1 - k0), cudaMemcpyDeviceToHost,
+                             h->stream));
+    CUDA_TRY(cudaEventRecord(h->stage_ev[slot], h->stream));
+    h->stage_busy[slot] = true;
+    return MOLOCH_OK;
+  };
+  int rc = issue(0);
+  if (rc) return rc;
+  for (int c = 0; c < nchunks; ++c) {
+    if (c + 1 < nchunks && (rc = issue(c + 1))) return rc;
+    const int slot = c & 1, k0 = c * chunk, k1 = std::min(nk, k0 + chunk);
+    if ((rc = stage_wait(h, slot))) return rc;
+    const T* st = (const T*)((const char*)h->stage + slot * (h->stage_bytes / 2));
+    const int nrow_i = i2 - i1 + 1;
+    host_parallel((size_t)(k1 - k0) * nrow_i, [&](size_t r0, size_t r1) {
+      for (size_t r = r0; r < r1; ++r) {
+        const int kk = k0 + (int)(r / nrow_i), i = i1 + (int)(r % nrow_i);
+        const long q = off4 + (long)(s.ndim >= 3 ? kk + 1 - k1b : 0) * n1 * n2 + (long)(i - i1) * n1;
+        const T* row = st + ((size_t)(kk - k0) * ni + wrap(i, ni)) * nj;
+        double* o = base + q;
+        for (int j = s.lb[0]; j <= s.ub[0]; ++j) o[j - s.lb[0]] = (double)row[wrap(j, nj)];
+      }
+    });
+  }
   return MOLOCH_OK;
 }
 
@@ -580,6 +709,7 @@ int moloch_gpu_create(const moloch_grid_t* grid, const moloch_params_t* params, 
     h->stage_bytes = sizeof(double) * (size_t)grid->jx * grid->iy * (grid->kz + 1);
     e = cudaMallocHost(&h->stage, h->stage_bytes);
   }
+  for (int q = 0; q < 2 && e == cudaSuccess; ++q) e = cudaEventCreateWithFlags(&h->stage_ev[q], cudaEventDisableTiming);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) {
     cudaFree(h->arena);
@@ -622,24 +752,22 @@ int moloch_gpu_upload(moloch_handle_t* h, int field, const double* host_base, co
   }
   if (field == MOLOCH_F_QX) {
     for (int n = 0; n < 5; ++n) {
-      gather_interior(host_base, s, nj, ni, nk, n, dense);
-      int rc = h->elem == 8 ? upload_dense<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), dense)
-                            : upload_dense<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), dense);
+      int rc = h->elem == 8 ? upload_streamed<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), host_base, s, nj, ni, nk, n)
+                            : upload_streamed<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), host_base, s, nj, ni, nk, n);
       if (rc) return rc;
       h->uploaded |= 1u << (MOLOCH_F_QV + n);
     }
     return MOLOCH_OK;
   }
-  gather_interior(host_base, s, nj, ni, nk, 0, dense);
   int rc;
   if (h->elem == 8) {
     double* p = field_ptr(h->vd, field);
     if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", field);
-    rc = upload_dense<double>(h, p, dense);
+    rc = upload_streamed<double>(h, p, host_base, s, nj, ni, nk, 0);
   } else {
     float* p = field_ptr(h->vf, field);
     if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", field);
-    rc = upload_dense<float>(h, p, dense);
+    rc = upload_streamed<float>(h, p, host_base, s, nj, ni, nk, 0);
   }
   if (!rc) h->uploaded |= 1u << field;
   return rc;
@@ -764,18 +892,79 @@ int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base, const 
   if (field == MOLOCH_F_QX) {
     for (int n = 0; n < 5; ++n) {
       int rc = h->elem == 8
-                   ? download_dense<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), (size_t)nj * ni * kz, dense)
-                   : download_dense<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), (size_t)nj * ni * kz, dense);
+                   ? download_streamed<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), s, nj, ni, kz, n, host_base)
+                   : download_streamed<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), s, nj, ni, kz, n, host_base);
       if (rc) return rc;
-      scatter_periodic(dense, s, nj, ni, kz, n, host_base);
     }
     return MOLOCH_OK;
   }
-  const size_t n = (size_t)nj * ni * nk;
-  int rc = h->elem == 8 ? download_dense<double>(h, field_ptr(h->vd, field), n, dense)
-                        : download_dense<float>(h, field_ptr(h->vf, field), n, dense);
-  if (rc) return rc;
-  scatter_periodic(dense, s, nj, ni, nk, 0, host_base);
+  int rc = h->elem == 8 ? download_streamed<double>(h, field_ptr(h->vd, field), s, nj, ni, nk, 0, host_base)
+                        : download_streamed<float>(h, field_ptr(h->vf, field), s, nj, ni, nk, 0, host_base);
+  return rc;
+}
+
+// Output path (the fields the reference driver writes every iout steps,
+// nompi/regcm_dynamical_core.F90:203-216): t and ps are copied on the device
+// into a snapshot in stream order, and the snapshot goes to pinned host
+// memory on a second stream, so the caller's next steps overlap the copy.
+int moloch_gpu_output_start(moloch_handle_t* h) {
+  g_err.clear();
+  if (!h || !h->initialized) return fail(MOLOCH_ERR_STATE, "output before moloch_gpu_init");
+  if (h->out_pending) return fail(MOLOCH_ERR_STATE, "output_start twice without output_finish");
+  const size_t pl = (size_t)h->nj() * h->ni(), n3 = pl * h->kz();
+  const size_t bytes = (n3 + pl) * h->elem;
+  if (!h->out_dev) {
+    CUDA_TRY(cudaMalloc(&h->out_dev, bytes));
+    CUDA_TRY(cudaMallocHost(&h->out_host, bytes));
+    CUDA_TRY(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking));
+    CUDA_TRY(cudaEventCreateWithFlags(&h->out_taken, cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&h->out_done, cudaEventDisableTiming));
+  }
+  const void* t = h->elem == 8 ? (const void*)h->vd.t : (const void*)h->vf.t;
+  const void* ps = h->elem == 8 ? (const void*)h->vd.ps : (const void*)h->vf.ps;
+  CUDA_TRY(cudaMemcpyAsync(h->out_dev, t, n3 * h->elem, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaMemcpyAsync((char*)h->out_dev + n3 * h->elem, ps, pl * h->elem, cudaMemcpyDeviceToDevice, h->stream));
+  CUDA_TRY(cudaEventRecord(h->out_taken, h->stream));
+  CUDA_TRY(cudaStreamWaitEvent(h->out_stream, h->out_taken, 0));
+  CUDA_TRY(cudaMemcpyAsync(h->out_host, h->out_dev, bytes, cudaMemcpyDeviceToHost, h->out_stream));
+  CUDA_TRY(cudaEventRecord(h->out_done, h->out_stream));
+  h->out_pending = true;
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb, const int* t_ub, double* ps_host,
+                             const int* ps_lb, const int* ps_ub) {
+  g_err.clear();
+  if (!h || !h->out_pending) return fail(MOLOCH_ERR_STATE, "output_finish without output_start");
+  const int nj = h->nj(), ni = h->ni(), kz = h->kz();
+  const FieldShape st = shape_of(MOLOCH_F_T, nj, ni, kz), sp = shape_of(MOLOCH_F_PS, nj, ni, kz);
+  for (int d = 0; d < st.ndim; ++d)
+    if (t_host && (t_lb[d] != st.lb[d] || t_ub[d] != st.ub[d])) return fail(MOLOCH_ERR_BOUNDS, "output t bounds");
+  for (int d = 0; d < sp.ndim; ++d)
+    if (ps_host && (ps_lb[d] != sp.lb[d] || ps_ub[d] != sp.ub[d])) return fail(MOLOCH_ERR_BOUNDS, "output ps bounds");
+  CUDA_TRY(cudaEventSynchronize(h->out_done));
+  h->out_pending = false;
+  const size_t pl = (size_t)nj * ni, n3 = pl * kz;
+  auto scatter = [&](const FieldShape& s, int nk, size_t off, double* base) {
+    const long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ub[1] - s.lb[1] + 1;
+    const int i1 = s.lb[1], nrow_i = s.ub[1] - s.lb[1] + 1;
+    host_parallel((size_t)nk * nrow_i, [&](size_t r0, size_t r1) {
+      for (size_t r = r0; r < r1; ++r) {
+        const int kk = (int)(r / nrow_i), i = i1 + (int)(r % nrow_i);
+        double* o = base + (long)kk * n1 * n2 + (long)(i - i1) * n1;
+        const size_t row = off + ((size_t)kk * ni + wrap(i, ni)) * nj;
+        if (h->elem == 8) {
+          const double* src = (const double*)h->out_host + row;
+          for (int j = s.lb[0]; j <= s.ub[0]; ++j) o[j - s.lb[0]] = src[wrap(j, nj)];
+        } else {
+          const float* src = (const float*)h->out_host + row;
+          for (int j = s.lb[0]; j <= s.ub[0]; ++j) o[j - s.lb[0]] = (double)src[wrap(j, nj)];
+        }
+      }
+    });
+  };
+  if (t_host) scatter(st, kz, 0, t_host);
+  if (ps_host) scatter(sp, 1, n3, ps_host);
   return MOLOCH_OK;
 }
 
@@ -1174,6 +1363,14 @@ int moloch_gpu_destroy(moloch_handle_t* h) {
   if (h->arena) cudaFree(h->arena);
   if (h->hres) cudaFreeHost(h->hres);
   if (h->stage) cudaFreeHost(h->stage);
+  if (h->out_stream) cudaStreamSynchronize(h->out_stream);
+  if (h->out_dev) cudaFree(h->out_dev);
+  if (h->out_host) cudaFreeHost(h->out_host);
+  if (h->out_stream) cudaStreamDestroy(h->out_stream);
+  if (h->out_taken) cudaEventDestroy(h->out_taken);
+  if (h->out_done) cudaEventDestroy(h->out_done);
+  for (int q = 0; q < 2; ++q)
+    if (h->stage_ev[q]) cudaEventDestroy(h->stage_ev[q]);
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return MOLOCH_OK;

@@ -147,6 +147,17 @@ int moloch_gpu_run(moloch_handle_t* h, int nsteps, int use_graph);
 int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base,
                         const int* lb, const int* ub);
 
+/* Output path (nompi/regcm_dynamical_core.F90:203-216 writes t and ps
+ * every iout steps).  output_start snapshots t and ps on the device in
+ * stream order (after the steps already issued) and starts their copy to
+ * pinned host memory on a second stream, then returns: the next steps run
+ * while the copy is in flight.  output_finish waits for that copy and fills
+ * reference-layout host arrays (either may be NULL) with the snapshot.
+ * One snapshot at a time: start, finish, start, ... */
+int moloch_gpu_output_start(moloch_handle_t* h);
+int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb, const int* t_ub,
+                             double* ps_host, const int* ps_lb, const int* ps_ub);
+
 /* Block until the handle's stream is idle. */
 int moloch_gpu_sync(moloch_handle_t* h);
 

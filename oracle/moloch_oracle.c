@@ -8,9 +8,10 @@
  * PARITY UNPINNED: the reference is Fortran and no Fortran compiler exists
  * on any machine this project runs on, so the reference itself cannot be
  * run and it ships no golden vectors or tests.  This restatement is pinned
- * only by known-answer checks written from the equations and by an
- * independent NumPy restatement (tests/golden/numpy_moloch.py) that must
- * agree with it to the last bit.
+ * only by known-answer checks written from the equations
+ * (tests/test_oracle_known_answers.py) and by golden fixtures it generated
+ * itself (tests/golden/), which guard it against regressions, not against
+ * misreading the reference.
  *
  * What it restates (paths relative to the reference project):
  *   nompi/mod_moloch.F90            moloch(), sound(), divdamp(), advection(),

@@ -6,7 +6,7 @@ Tolerances (floating point, FP64):
     transcendental calls pow/exp differ between CUDA and the host libm);
   * 100 steps at the reference defaults (100 x 100 x 30): relative L2 <= 1e-9
     per prognostic field, for the FP64 (contracting) and FP64_EXACT builds;
-  * FP32 storage with FP64 solve: see test_gpu_mixed.py.
+  * FP32 storage with FP64 solve: tests/test_gpu_mixed.py.
 """
 import numpy as np
 import pytest
@@ -178,3 +178,26 @@ def test_upload_download_roundtrip_and_bounds(gpu_lib):
     buf = np.zeros(14 * 12 * 6)
     rc = L.moloch_gpu_upload(g.h, gpu_lib.FIELD["u"], buf.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), lb, ub)
     assert rc == 2  # u has bounds (-1:nj+2, 0:ni+1, 1:kz)
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
+def test_output_path_overlaps_steps(gpu_lib, mode):
+    """output_start after step 2, two more steps, output_finish: the arrays
+    hold t and ps of step 2 (with periodic halos), and the run itself is
+    not disturbed."""
+    a = gpu_lib.Moloch(40, 28, 12, mode=mode)
+    b = gpu_lib.Moloch(40, 28, 12, mode=mode)
+    for g in (a, b):
+        g.setup_idealized(hills=((300.0, 20.0, 14.0, 4.0),), u0=3.0)
+    a.run(2, graph=True)
+    b.run(2, graph=True)
+    a.output_start()
+    a.run(2, graph=True)
+    t2, ps2 = a.output_finish()
+    assert np.array_equal(t2, b.download("t"))
+    assert np.array_equal(ps2, b.download("ps"))
+    b.run(2, graph=True)
+    for n in ("t", "ps", "u", "pai"):
+        assert np.array_equal(a.get(n), b.get(n)), n
+    with pytest.raises(gpu_lib.MolochError):
+        a.output_finish()

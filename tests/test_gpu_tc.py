@@ -33,6 +33,27 @@ def test_tc_gemm(gpu_lib, M, N, K, act):
     assert errb.item() <= 1e-2, errb.item()
 
 
+def test_tc_gemm_surrogate_layer1(gpu_lib):
+    """The first surrogate layer at 256 x 256 x 40: 65536 columns x 1856
+    features -> 256 (BF16 out with SiLU), many tiles per persistent CTA."""
+    torch = pytest.importorskip("torch")
+    L = gpu_lib.lib()
+    M, N, K = 65536, 256, 1856
+    g = torch.Generator(device="cpu").manual_seed(7)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = (torch.randn(N, K, generator=g) / K ** 0.5).to(torch.bfloat16).cuda()
+    bias = torch.randn(N, generator=g).cuda()
+    Cb = torch.zeros(M, N, device="cuda", dtype=torch.bfloat16)
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    rc = L.moloch_tc_gemm(P(A), K, P(B), K, None, 0, P(Cb), N, P(bias), M, N, K, 1, None)
+    assert rc == 0, L.moloch_gpu_last_error()
+    assert L.moloch_tc_status() == 0
+    for r0 in (0, 30000, M - 512):
+        ref = torch.nn.functional.silu(A[r0:r0 + 512].float() @ B.float().T + bias)
+        err = (Cb[r0:r0 + 512].float() - ref).norm() / ref.norm()
+        assert err.item() <= 1e-2, (r0, err.item())
+
+
 def test_tc_gemm_rejects_bad_shapes(gpu_lib):
     L = gpu_lib.lib()
     dummy = ctypes.c_void_p(16)
