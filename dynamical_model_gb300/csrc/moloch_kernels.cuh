@@ -365,15 +365,28 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     const T zd_t = ((zcs2 * fk) * zrom1w) * pk + ff;
     const double zu = (double)zu_t;
     const double zdd = (double)zd_t;
-    const double zrapp = pivot_rcp<T>(((1.0 + zdd) + zu) - zdd * wwp1);
-    const double wwk = zrapp * zu;
+    const double den = ((1.0 + zdd) + zu) - zdd * wwp1;
     ST wpk;
-    if constexpr (kF32)
-      wpk = (float)zrapp * (zwexpl + zd_t * wkp1);
-    else
+    double wwk;
+    if constexpr (kF32) {
+      // FP32 estimate r of 1/den, one FP64 Newton step for the pivot
+      // (relative error ~1e-14); the FP32 right-hand side and the stash use
+      // r itself, so no FP64 result has to be converted back (the FP64
+      // pipe is 1/64 of the FP32 rate on GB300 and converts count there)
+      float r;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)den));
+      const double r0 = (double)r;
+      const double zrapp = fma(r0, fma(-den, r0, 1.0), r0);
+      wwk = zrapp * zu;
+      wpk = r * (zwexpl + zd_t * wkp1);
+      WWs[o] = r * zu_t;
+    } else {
+      const double zrapp = pivot_rcp<T>(den);
+      wwk = zrapp * zu;
       wpk = zrapp * ((double)zwexpl + zdd * wkp1);
+      WWs[o] = (ST)wwk;
+    }
     WPs[o] = wpk;
-    WWs[o] = (ST)wwk;
     wkp1 = wpk; wwp1 = wwk;
     zd_k = zd_km; tk = tkm; pk = pkm; fk = fkm; qsk = qskm;
   }
