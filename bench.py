@@ -228,7 +228,7 @@ def run_reference(args, dist, rank, ws):
 
 def make_domain(dm, mode, stream):
     d = dm.Moloch(JX, IY, KZ, mode=mode, stream=stream)
-    d.setup_idealized(hills=HILLS, pert_amp=0.5, pert_levels=10, seed=SEED)
+    d.setup_idealized(hills=HILLS, pert_amp=0.5, pert_levels=10, seed=SEED, device=True)
     return d
 
 
@@ -299,7 +299,7 @@ def ensemble_members(dm, stream, n=64, seed=2024):
         kz = int(rng.choice([30, 40, 60]))
         u0 = float(rng.uniform(0.0, 10.0))
         d = dm.Moloch(jx, iy, kz, mode="fp32_mixed", stream=stream)
-        d.setup_idealized(pert_amp=1.0, pert_levels=kz, seed=seed + m, u0=u0, v0=1.0)
+        d.setup_idealized(pert_amp=1.0, pert_levels=kz, seed=seed + m, u0=u0, v0=1.0, device=True)
         out.append(d)
     return out
 
@@ -313,7 +313,7 @@ def train_surrogate(dm, mode, stream, jx, iy, kz, hills, cfg=SUR):
     scratch domain and train the surrogate on the GPU."""
     t0 = time.perf_counter()
     scratch = dm.Moloch(jx, iy, kz, mode=mode, stream=stream)
-    scratch.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED + 7)
+    scratch.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED + 7, device=True)
     cap = cfg["collect_steps"] * scratch.params.mo_nadv * cfg["cols_per_cycle"]
     sur = dm.Surrogate(kz, capacity=cap, batch=cfg["batch"], seed=1)
     pairs = sur.collect(scratch, cfg["collect_steps"], cols_per_cycle=cfg["cols_per_cycle"])
@@ -332,7 +332,7 @@ def surrogate_forced_error(dm, sur, stream, jx, iy, kz, hills, ref_fields, steps
     from the same initial state as the FP64 reference: its error after
     `steps` steps.  Shows what the judge protects against."""
     d = dm.Moloch(jx, iy, kz, mode="fp32_mixed", stream=stream)
-    d.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED)
+    d.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED, device=True)
     sur.attach(d, threshold=1e30, judge_every=0)
     d.run(steps, graph=True)
     out = {"steps": steps,

@@ -84,6 +84,7 @@ _PROTOS = {
     "moloch_gpu_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "moloch_gpu_last_error": (ctypes.c_char_p, []),
     "moloch_gpu_setup_idealized": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Ideal)]),
+    "moloch_gpu_setup_idealized_device": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Ideal)]),
     "moloch_gpu_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_kernel_kinds": (ctypes.c_int, []),
@@ -217,13 +218,16 @@ class Moloch:
         self.h = h
 
     # -- init_moloch ----------------------------------------------------------
-    def setup_idealized(self, hills=(), pert_amp=0.5, pert_levels=10, seed=1234, u0=1.0, v0=1.0):
+    def setup_idealized(self, hills=(), pert_amp=0.5, pert_levels=10, seed=1234, u0=1.0, v0=1.0, device=False):
+        """param() + init() + init_moloch.  device=True computes the state on
+        the GPU (moloch_gpu_setup_idealized_device) instead of on the host."""
         z = Ideal()
         z.nhills = len(hills)
         for n, (hh, cj, ci, r) in enumerate(hills):
             z.hill_h[n], z.hill_j[n], z.hill_i[n], z.hill_r[n] = hh, cj, ci, r
         z.pert_amp, z.pert_levels, z.seed, z.u0, z.v0 = pert_amp, pert_levels, seed, u0, v0
-        _check(self.L.moloch_gpu_setup_idealized(self.h, ctypes.byref(z)))
+        fn = self.L.moloch_gpu_setup_idealized_device if device else self.L.moloch_gpu_setup_idealized
+        _check(fn(self.h, ctypes.byref(z)))
 
     def upload(self, name, arr):
         """Upload a reference-layout array (Fortran order, with its halo)."""

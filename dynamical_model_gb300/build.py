@@ -61,6 +61,7 @@ def build(force=False, verbose=False):
         nv_common + ["--fmad=false", "-c", os.path.join(CSRC, "moloch_noalloc.cu"),
                      "-o", os.path.join(BUILD, "noalloc.o")],
         nv_common + ["-c", os.path.join(CSRC, "moloch_mlp.cu"), "-o", os.path.join(BUILD, "mlp.o")],
+        nv_common + ["--fmad=false", "-c", os.path.join(CSRC, "moloch_init.cu"), "-o", os.path.join(BUILD, "init.o")],
         ["g++", "-std=c++17", "-O2", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math"] + inc +
         ["-c", os.path.join(CSRC, "moloch_api.cpp"), "-o", os.path.join(BUILD, "api.o")],
         ["g++", "-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math"] + inc +
@@ -79,7 +80,7 @@ def build(force=False, verbose=False):
         raise RuntimeError("build failed:\n" + msg)
     tmp = LIB + ".tmp"
     link = [nvcc, ARCH, "-shared", "-o", tmp] + [os.path.join(BUILD, o) for o in
-                                                 ("kexact.o", "kfast.o", "noalloc.o", "mlp.o", "api.o", "ideal.o")] + ["-lcudart", "-Xcompiler", "-pthread"]
+                                                 ("kexact.o", "kfast.o", "noalloc.o", "mlp.o", "init.o", "api.o", "ideal.o")] + ["-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

@@ -281,10 +281,9 @@ int upload_dense(moloch_handle* h, T* dst, const std::vector<double>& src) {
   if (bytes > h->stage_bytes) return fail(MOLOCH_ERR_ARG, "upload of %zu bytes exceeds staging", bytes);
   CUDA_TRY(cudaStreamSynchronize(h->stream));  // staging buffer free again
   T* st = (T*)h->stage;
-  if (sizeof(T) == sizeof(double))
-    std::memcpy(st, src.data(), bytes);
-  else
-    for (size_t q = 0; q < src.size(); ++q) st[q] = (T)src[q];
+  host_parallel(src.size(), [&](size_t q0, size_t q1) {
+    for (size_t q = q0; q < q1; ++q) st[q] = (T)src[q];
+  });
   CUDA_TRY(cudaMemcpyAsync(dst, st, bytes, cudaMemcpyHostToDevice, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
   return MOLOCH_OK;
@@ -510,8 +509,9 @@ int init_impl(moloch_handle* h, View<T>& v) {
   // 3-D static terms
   const size_t n3 = pl * kz;
   std::vector<double> rfw(n3), rfs(n3), wu(n3), wd(n3), wn(n3), ws(n3), we(n3), ww(n3), dz(n3);
-  for (int k = 1; k <= kz; ++k)
-    for (int i = 1; i <= ni; ++i)
+  host_parallel((size_t)kz * ni, [&](size_t r0, size_t r1) {
+    for (size_t r = r0; r < r1; ++r) {
+      const int k = (int)(r / ni) + 1, i = (int)(r % ni) + 1;
       for (int j = 1; j <= nj; ++j) {
         const size_t q = I3(j, i, k);
         const double f = fmz[q];
@@ -538,6 +538,8 @@ int init_impl(moloch_handle* h, View<T>& v) {
         }
         dz[q] = dzita / f;  // layer thickness for the column sums
       }
+    }
+  });
   auto up3 = [&](const T* dst, const std::vector<double>& src) { return upload_dense<T>(h, (T*)dst, src); };
   if ((rc = up3(v.fmz, fmz)) || (rc = up3(v.fmzf, fmzf)) || (rc = up3(v.zeta, h->zeta))) return rc;
   if ((rc = up3(v.rfw, rfw)) || (rc = up3(v.rfs, rfs)) || (rc = up3(v.wafu, wu)) || (rc = up3(v.wafd, wd)))
@@ -966,6 +968,85 @@ int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb
   if (t_host) scatter(st, kz, 0, t_host);
   if (ps_host) scatter(sp, 1, n3, ps_host);
   return MOLOCH_OK;
+}
+
+// Idealized initial state computed on the device (param() and
+// fill_atmosphere() as in moloch_gpu_setup_idealized, one thread per
+// column): the prognostic fields are written in place in the bulk type, the
+// FP64 static fields come back to the host copies init uses, then
+// moloch_gpu_init runs as after a Fortran caller's uploads.
+int moloch_gpu_setup_idealized_device(moloch_handle_t* h, const moloch_ideal_t* ideal) {
+  g_err.clear();
+  if (!h || !ideal) return fail(MOLOCH_ERR_ARG, "null argument");
+  const int nj = h->nj(), ni = h->ni(), kz = h->kz();
+  if (kz < 2) return fail(MOLOCH_ERR_ARG, "kz >= 2");
+  const moloch_params_t& P = h->prm;
+  const size_t pl = (size_t)nj * ni;
+  // zita levels (model_zitaf / model_zitah), 1-based with kz+2 entries
+  std::vector<double> zita(kz + 2, 0.0), zitah(kz + 2, 0.0);
+  const double dz = P.mo_ztop / (double)kz;
+  zita[kz + 1] = 0.0;
+  for (int k = kz; k >= 1; --k) zita[k] = zita[k + 1] + dz;
+  zitah[kz] = dz * 0.5;
+  for (int k = kz - 1; k >= 1; --k) zitah[k] = zitah[k + 1] + dz;
+  moloch::init::IdealArgs a{};
+  a.nj = nj; a.ni = ni; a.kz = kz; a.rotllr = P.rotllr;
+  a.dx = P.dx; a.ztop = P.mo_ztop; a.zh = P.mo_h; a.a0 = P.mo_a0;
+  a.nhills = std::min(ideal->nhills, 4);
+  for (int n = 0; n < 4; ++n) {
+    a.hill_h[n] = ideal->hill_h[n]; a.hill_j[n] = ideal->hill_j[n];
+    a.hill_i[n] = ideal->hill_i[n]; a.hill_r[n] = ideal->hill_r[n];
+  }
+  a.pert_amp = ideal->pert_amp; a.pert_levels = ideal->pert_levels; a.seed = ideal->seed;
+  // FP64 scratch: zita, zitah, zeta, fmz, fmzf, hx, hy, ulat, vlat
+  const size_t n_z = 2 * (size_t)(kz + 2), n3 = pl * kz, n3p = pl * (kz + 1);
+  double* dev = nullptr;
+  CUDA_TRY(cudaMalloc(&dev, sizeof(double) * (n_z + 2 * n3 + n3p + 4 * pl)));
+  double *dzita = dev, *dzitah = dev + (kz + 2), *dzeta = dev + n_z, *dfmz = dzeta + n3, *dfmzf = dfmz + n3;
+  double *dhx = dfmzf + n3p, *dhy = dhx + pl, *dulat = dhy + pl, *dvlat = dulat + pl;
+  auto done = [&](int rc) { cudaFree(dev); return rc; };
+  if (cudaMemcpyAsync(dzita, zita.data(), sizeof(double) * (kz + 2), cudaMemcpyHostToDevice, h->stream) ||
+      cudaMemcpyAsync(dzitah, zitah.data(), sizeof(double) * (kz + 2), cudaMemcpyHostToDevice, h->stream))
+    return done(fail(MOLOCH_ERR_CUDA, "setup_idealized_device: copy of the zita levels"));
+  using moloch::init::launch_fill;
+  using moloch::init::launch_ideal;
+  if (h->elem == 8) {
+    View<double>& v = h->vd;
+    launch_ideal<double>(a, dzita, dzitah, dzeta, dfmz, dfmzf, dhx, dhy, dulat, dvlat, v.t, v.pai, v.q[0], h->stream);
+    for (int n = 1; n < 5; ++n) launch_fill<double>(v.q[n], pl * kz, 0.0, h->stream);
+    launch_fill<double>(v.ubuf[v.cur], pl * kz, ideal->u0, h->stream);
+    launch_fill<double>(v.vbuf[v.cur], pl * kz, ideal->v0, h->stream);
+    launch_fill<double>(v.w, pl * (kz + 1), 0.0, h->stream);
+  } else {
+    View<float>& v = h->vf;
+    launch_ideal<float>(a, dzita, dzitah, dzeta, dfmz, dfmzf, dhx, dhy, dulat, dvlat, v.t, v.pai, v.q[0], h->stream);
+    for (int n = 1; n < 5; ++n) launch_fill<float>(v.q[n], pl * kz, 0.0, h->stream);
+    launch_fill<float>(v.ubuf[v.cur], pl * kz, ideal->u0, h->stream);
+    launch_fill<float>(v.vbuf[v.cur], pl * kz, ideal->v0, h->stream);
+    launch_fill<float>(v.w, pl * (kz + 1), 0.0, h->stream);
+  }
+  if (cudaGetLastError() != cudaSuccess) return done(fail(MOLOCH_ERR_CUDA, "setup_idealized_device: launch"));
+  h->zeta.resize(n3); h->fmz.resize(n3); h->fmzf.resize(n3p);
+  h->hx.resize(pl); h->hy.resize(pl); h->ulat.resize(pl); h->vlat.resize(pl);
+  struct { double* dst; const double* src; size_t n; } cp[] = {
+      {h->zeta.data(), dzeta, n3}, {h->fmz.data(), dfmz, n3}, {h->fmzf.data(), dfmzf, n3p},
+      {h->hx.data(), dhx, pl}, {h->hy.data(), dhy, pl}, {h->ulat.data(), dulat, pl}, {h->vlat.data(), dvlat, pl}};
+  for (auto& x : cp)
+    if (cudaMemcpyAsync(x.dst, x.src, sizeof(double) * x.n, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+      return done(fail(MOLOCH_ERR_CUDA, "setup_idealized_device: copy of the static fields"));
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess)
+    return done(fail(MOLOCH_ERR_CUDA, "setup_idealized_device: %s", cudaGetErrorString(cudaGetLastError())));
+  cudaFree(dev);
+  h->msfx.assign(pl, 1.0); h->msfu.assign(pl, 1.0); h->msfv.assign(pl, 1.0);
+  h->zita.assign(zita.begin() + 1, zita.begin() + kz + 2);
+  h->zitah.assign(zitah.begin() + 1, zitah.begin() + kz + 1);
+  const int fields[] = {MOLOCH_F_U, MOLOCH_F_V, MOLOCH_F_W, MOLOCH_F_PAI, MOLOCH_F_T, MOLOCH_F_QV, MOLOCH_F_QC,
+                        MOLOCH_F_QI, MOLOCH_F_QR, MOLOCH_F_QS, MOLOCH_F_ZETA, MOLOCH_F_FMZ, MOLOCH_F_FMZF,
+                        MOLOCH_F_MSFX, MOLOCH_F_MSFU, MOLOCH_F_MSFV, MOLOCH_F_HX, MOLOCH_F_HY, MOLOCH_F_ULAT,
+                        MOLOCH_F_VLAT, MOLOCH_F_ZITA, MOLOCH_F_ZITAH};
+  for (int f : fields) h->uploaded |= 1u << f;
+  h->initialized = false;
+  return moloch_gpu_init(h);
 }
 
 int moloch_gpu_sync(moloch_handle_t* h) {

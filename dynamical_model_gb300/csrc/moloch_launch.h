@@ -25,4 +25,22 @@ template <class T> int blaunch_step(const Batch<T>& b, cudaStream_t st, const Ph
 template <class T> int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur);
 }
 #undef MOLOCH_DECLARE_LAUNCHERS
+
+// idealized initial state on the device (moloch_init.cu)
+namespace init {
+struct IdealArgs {
+  int nj, ni, kz, rotllr;
+  double dx, ztop, zh, a0;
+  int nhills;
+  double hill_h[4], hill_j[4], hill_i[4], hill_r[4];
+  double pert_amp;
+  int pert_levels;
+  unsigned long long seed;
+};
+template <class T>
+int launch_ideal(const IdealArgs& a, const double* zita, const double* zitah, double* zeta, double* fmz,
+                 double* fmzf, double* hx, double* hy, double* ulat, double* vlat, T* t, T* pai, T* qv,
+                 cudaStream_t st);
+template <class T> int launch_fill(T* p, size_t n, double value, cudaStream_t st);
+}  // namespace init
 }  // namespace moloch

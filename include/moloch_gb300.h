@@ -341,6 +341,14 @@ typedef struct moloch_ideal {
 
 int moloch_gpu_setup_idealized(moloch_handle_t* h, const moloch_ideal_t* ideal);
 
+/* The same initial state computed on the device, one thread per column
+ * (no host arrays of the grid size are built or uploaded): the prognostic
+ * fields are written in place, the FP64 static fields are copied back to
+ * the library's host copies, then moloch_gpu_init runs.  Results agree with
+ * moloch_gpu_setup_idealized to the rounding of exp/pow/sqrt (CUDA's versus
+ * the host library's). */
+int moloch_gpu_setup_idealized_device(moloch_handle_t* h, const moloch_ideal_t* ideal);
+
 #ifdef __cplusplus
 }
 #endif

@@ -201,3 +201,28 @@ def test_output_path_overlaps_steps(gpu_lib, mode):
         assert np.array_equal(a.get(n), b.get(n)), n
     with pytest.raises(gpu_lib.MolochError):
         a.output_finish()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
+def test_setup_on_device_matches_host(gpu_lib, mode):
+    """The idealized state computed on the device against the host
+    restatement: static and prognostic fields to 1e-13 relative (FP64; only
+    exp/pow/sqrt roundings differ) or to the FP32 rounding, and 5 steps from
+    each to 1e-11 / 1e-5."""
+    kw = dict(hills=((500.0, 30.5, 20.5, 6.0), (300.0, 10.0, 33.0, 3.0)), u0=4.0, v0=-1.5, pert_amp=0.5,
+              pert_levels=7, seed=99)
+    a = gpu_lib.Moloch(61, 41, 17, mode=mode)
+    b = gpu_lib.Moloch(61, 41, 17, mode=mode)
+    a.setup_idealized(**kw)
+    b.setup_idealized(device=True, **kw)
+    tol0 = 1e-13 if mode == "fp64" else 1e-7
+    for n in ("zeta", "fmz", "fmzf", "hx", "hy", "u", "v", "w", "t", "pai", "qv", "qc"):
+        e = rel_l2(b.get(n), a.get(n))
+        assert e <= tol0, (n, e)
+    for s in range(1, 6):
+        a.moloch(s)
+        b.moloch(s)
+    tol = 1e-11 if mode == "fp64" else 1e-5
+    for n in PROG + DIAG:
+        e = rel_l2(b.get(n), a.get(n))
+        assert e <= tol, (n, e)
