@@ -1107,7 +1107,9 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 
 // ---- autotuner --------------------------------------------------------------
 // Tunable launch shapes, in order: [0] levels per k_waf_horizontal block.
-static const int kTuneCandidates[][4] = {{1, 2, 4, 8}};
+// horizontal WAF launch shape: 1..8 = levels per 32x8 tile block, >= 16 =
+// rows per warp strip
+static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
 static const int kTuneCount = 1;
 
 int moloch_gpu_tuning_count(void) { return kTuneCount; }
@@ -1138,9 +1140,9 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   CUDA_TRY(cudaEventCreate(&e1));
   double best = 1e30;
   int pick = h->elem == 8 ? h->vd.hz_levels : h->vf.hz_levels;
-  for (int c = 0; c < 4; ++c) {
+  for (int c = 0; c < 7; ++c) {
     const int cand = kTuneCandidates[0][c];
-    if (cand > h->kz()) continue;
+    if (cand < 16 && cand > h->kz()) continue;
     h->vd.hz_levels = cand;
     h->vf.hz_levels = cand;
     float ms = 0.f, tot = 0.f;
@@ -1213,10 +1215,16 @@ void ens_tiles(moloch_ensemble* e) {
       for (int x = 0; x < tj; ++x) e->tiles[TK_COLUMN].push_back(make_int4(q, x, y, 0));
     for (int y = 0; y < (ni + 3) / 4; ++y)
       for (int x = 0; x < tj * kNumAdvected; ++x) e->tiles[TK_VERTICAL].push_back(make_int4(q, x, y, 0));
-    const int hz = std::min(e->hz_levels, kz);
-    for (int z = 0; z < (kz + hz - 1) / hz; ++z)
-      for (int y = 0; y < (ni + 7) / 8; ++y)
-        for (int x = 0; x < tj; ++x) e->tiles[TK_HORIZONTAL].push_back(make_int4(q, x, y, z));
+    if (e->hz_levels >= 16) {  // warp strips: 4 strips of hz_levels rows per block, every level
+      const int nstrips = ((nj + 27) / 28) * ((ni + e->hz_levels - 1) / e->hz_levels);
+      for (int z = 0; z < kz; ++z)
+        for (int x = 0; x < (nstrips + 3) / 4; ++x) e->tiles[TK_HORIZONTAL].push_back(make_int4(q, x, z, 0));
+    } else {
+      const int hz = std::min(e->hz_levels, kz);
+      for (int z = 0; z < (kz + hz - 1) / hz; ++z)
+        for (int y = 0; y < (ni + 7) / 8; ++y)
+          for (int x = 0; x < tj; ++x) e->tiles[TK_HORIZONTAL].push_back(make_int4(q, x, y, z));
+    }
   }
 }
 
@@ -1236,7 +1244,7 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
         View<T> v = e->m[q]->*vm;
         v.cur = cur;
         v.fcur = fc;
-        v.hz_levels = std::min(e->hz_levels, v.kz);
+        v.hz_levels = e->hz_levels >= 16 ? e->hz_levels : std::min(e->hz_levels, v.kz);
         v.bind_fields();
         hv[(size_t)(cur * 2 + fc) * n + q] = v;
       }
@@ -1249,6 +1257,7 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     CUDA_TRY(cudaMemcpy(p + off, e->tiles[t].data(), e->tiles[t].size() * sizeof(int4), cudaMemcpyHostToDevice));
     b.tiles[t] = (const int4*)(p + off);
     b.ntiles[t] = (int)e->tiles[t].size();
+    b.hstrip = e->hz_levels >= 16;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
   return MOLOCH_OK;
@@ -1356,7 +1365,7 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   CUDA_TRY(cudaEventCreate(&e1));
   double best = 1e30;
   int pick = e->hz_levels;
-  for (int c = 0; c < 4; ++c) {
+  for (int c = 0; c < 7; ++c) {
     e->hz_levels = kTuneCandidates[0][c];
     int rc = ens_build(e);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }

@@ -968,6 +968,155 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2)
   b_waf_horizontal<T>(sv, t.y, t.z, t.w);
 }
 
+// ---- advection: horizontal WAF as warp strips (:1075-1187) ---------------
+// One warp per strip of 28 output columns x R rows of one level (R =
+// d.hz_levels, 16..64), 32 lanes on columns j0-2 .. j0+29.  Each lane marches
+// down its own column: the wz values of rows i-1 .. i+2 and the meridional
+// flux of the face above the row stay in registers, p0 of the row is formed
+// in the lane, and the zonal fluxes take their p0 neighbours from the lanes
+// beside it (warp shuffles).  No shared memory and no barriers.  Fields are
+// processed G at a time so the per-row velocities and metric factors are
+// loaded once per group.  The result goes to the other field buffer.
+constexpr int kStripJ = 28;
+template <class T> struct StripG { static constexpr int G = 10; };
+template <> struct StripG<double> { static constexpr int G = 5; };
+
+template <class T>
+__device__ __forceinline__ void b_waf_hstrip(const View<T>& d, const int bx, const int k) {
+  constexpr int G = StripG<T>::G;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nj = d.nj, ni = d.ni, pl = d.pl, kz = d.kz;
+  const int R = d.hz_levels;
+  const int nsj = (nj + kStripJ - 1) / kStripJ, nsi = (ni + R - 1) / R;
+  const int w = bx * (blockDim.x >> 5) + wid;
+  if (w >= nsj * nsi) return;  // whole warp
+  const int sj = w % nsj, si = w / nsj;
+  const int j0 = sj * kStripJ;
+  const int jl = j0 - 2 + lane;  // this lane's column before wrapping
+  const int j = wrapn(jl, nj);
+  const bool out_lane = lane >= 2 && lane < 2 + kStripJ && jl < nj;
+  const int i_s = si * R, i_e = min(i_s + R, ni);
+  const T* __restrict__ u = d.ubuf[d.cur] + (size_t)k * pl;
+  const T* __restrict__ v = d.vbuf[d.cur] + (size_t)k * pl;
+  const T* __restrict__ wn_ = d.wafn + (size_t)k * pl;
+  const T* __restrict__ ws_ = d.wafs + (size_t)k * pl;
+  const T* __restrict__ we_ = d.wafe + (size_t)k * pl;
+  const T* __restrict__ ww_ = d.wafw + (size_t)k * pl;
+  const T dtrdx = d.dtrdx_a, dtrdy = d.dtrdy_a;
+  const bool rot = d.rotllr;
+  auto row = [&](int i) { return (size_t)j + (size_t)nj * wrapn(i, ni); };
+
+  for (int g0 = 0; g0 < kNumAdvected; g0 += G) {
+    const int ng = min(G, kNumAdvected - g0);
+    const T* wz[G];
+    const T* pp[G];
+    T* out[G];
+    T wm1_[G], w0_[G], wp1_[G], fl_[G];  // wz(i-1), wz(i), wz(i+1), flux of face i
+#pragma unroll
+    for (int g = 0; g < G; ++g) {
+      if (g < ng) {
+        wz[g] = d.wz + ((size_t)(g0 + g) * kz + k) * pl;
+        pp[g] = d.fset[d.fcur][g0 + g] + (size_t)k * pl;
+        out[g] = d.fset[d.fcur ^ 1][g0 + g] + (size_t)k * pl;
+      }
+    }
+    // warm-up: the flux of face i_s (between rows i_s-1 and i_s)
+    T v_i, rmv_i = T(1);
+    {
+      const size_t r = row(i_s);
+      v_i = v[r];
+      if (!rot) rmv_i = d.rmv[r];
+      const T mz = rot ? v_i * dtrdy : (v_i * rmv_i) * dtrdy;
+      const T mfac = rot ? T(0.5) * v_i : (T(0.5) * v_i) * rmv_i;
+      const size_t r2 = row(i_s - 2), r1 = row(i_s - 1), rp = row(i_s + 1);
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        if (g < ng) {
+          const T a = wz[g][r2], b = wz[g][r1], c = wz[g][r], e = wz[g][rp];
+          fl_[g] = mfac * waf_hflux(mz, a, b, c, e);
+          wm1_[g] = b; w0_[g] = c; wp1_[g] = e;
+        }
+      }
+    }
+    // the loads of row i+1 are issued while row i is computed
+    T n_wp2[G], n_pold[G];
+    T n_vn, n_rmvn, n_pn, n_ps, n_uu, n_oe, n_ow, n_zm, n_mx2;
+    auto fetch_row = [&](int i) {
+      const size_t r = row(i), rn = row(i + 1), r2 = row(i + 2);
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        if (g < ng) {
+          n_wp2[g] = wz[g][r2];
+          n_pold[g] = pp[g][r];
+        }
+      }
+      n_vn = v[rn];
+      n_rmvn = rot ? T(1) : d.rmv[rn];
+      n_pn = wn_[r]; n_ps = ws_[r];
+      n_uu = u[r];
+      n_oe = we_[r]; n_ow = ww_[r];
+      n_zm = rot ? d.mu[r] : d.rmu[r];
+      n_mx2 = rot ? T(0) : d.mx2[r];
+    };
+    fetch_row(i_s);
+    for (int i = i_s; i < i_e; ++i) {
+      const size_t r = row(i);
+      // per-row values shared by the fields of the group
+      const T v_n = n_vn, rmv_n = n_rmvn, pn = n_pn, ps = n_ps, uu = n_uu, oe = n_oe, ow = n_ow;
+      const T zm = n_zm, mx2 = n_mx2;
+      T wp2v[G], poldv[G];
+#pragma unroll
+      for (int g = 0; g < G; ++g) { wp2v[g] = n_wp2[g]; poldv[g] = n_pold[g]; }
+      if (i + 1 < i_e) fetch_row(i + 1);
+      const T mz = rot ? v_n * dtrdy : (v_n * rmv_n) * dtrdy;
+      const T mfac = rot ? T(0.5) * v_n : (T(0.5) * v_n) * rmv_n;
+      const T pdv = rot ? (v_n * pn - v_i * ps) : ((v_n * rmv_n) * pn - (v_i * rmv_i) * ps);
+      const T zz = (uu * zm) * dtrdx;
+      const T zfac = rot ? T(0.5) * uu : (T(0.5) * uu) * zm;
+      const T ue = __shfl_down_sync(0xffffffffu, uu, 1);  // u(j+1)
+      const T zme = __shfl_down_sync(0xffffffffu, zm, 1);
+      const T odv = rot ? (ue * oe - uu * ow) : ((ue * zme) * oe - (uu * zm) * ow);
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        if (g < ng) {
+          const T wp2 = wp2v[g];
+          const T fl_n = mfac * waf_hflux(mz, wm1_[g], w0_[g], wp1_[g], wp2);  // face i+1
+          const T pold = poldv[g];
+          const T zdv = pdv * pold;
+          const T p0 = rot ? ((w0_[g] + fl_[g] * ps) - fl_n * pn) + zdv
+                           : w0_[g] + mx2 * (((fl_[g] * ps) - fl_n * pn) + zdv);
+          const T pm2 = __shfl_up_sync(0xffffffffu, p0, 2);
+          const T pm1 = __shfl_up_sync(0xffffffffu, p0, 1);
+          const T pp1 = __shfl_down_sync(0xffffffffu, p0, 1);
+          const T zf = zfac * waf_hflux(zz, pm2, pm1, p0, pp1);  // face between j-1 and j
+          const T zfe = __shfl_down_sync(0xffffffffu, zf, 1);    // face between j and j+1
+          if (out_lane) {
+            const T zdv2 = odv * pold;
+            out[g][r] = rot ? ((p0 + zf * ow) - zfe * oe) + zdv2 : p0 + mx2 * (((zf * ow) - zfe * oe) + zdv2);
+          }
+          wm1_[g] = w0_[g]; w0_[g] = wp1_[g]; wp1_[g] = wp2; fl_[g] = fl_n;
+        }
+      }
+      v_i = v_n; rmv_i = rmv_n;
+    }
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_waf_hstrip(View<T> d) {
+  b_waf_hstrip<T>(d, blockIdx.x, blockIdx.y);
+}
+
+template <class T>
+__global__ void __launch_bounds__(128)
+    kb_waf_hstrip(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_waf_hstrip<T>(sv, t.y, t.z);
+}
+
 
 // ---- advection: cross points -> staggered (:1343-1387) ------------------
 // Writes u, v into buffer 0 so every step replays the same pointers.
@@ -1207,7 +1356,12 @@ int launch_advection(View<T>& d, cudaStream_t st) {
   const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, (d.kz + d.hz_levels - 1) / d.hz_levels);
   MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pg, pb, 0, st>>>(d));
   MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<vg, dim3(kColBX, kColBY), 0, st>>>(d));
-  MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_horizontal<T><<<hg, dim3(32, 8), 0, st>>>(d));
+  if (d.hz_levels >= 16) {  // warp strips of hz_levels rows
+    const int nstrips = ((d.nj + kStripJ - 1) / kStripJ) * ((d.ni + d.hz_levels - 1) / d.hz_levels);
+    MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_hstrip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d));
+  } else {
+    MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_horizontal<T><<<hg, dim3(32, 8), 0, st>>>(d));
+  }
   d.fcur ^= 1;
   d.bind_fields();
   MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pg, pb, 0, st>>>(d));
@@ -1277,7 +1431,10 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
     }
     MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<npt, pb, 0, st>>>(V(), PT));
     MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T><<<nve, cb, 0, st>>>(V(), VE));
-    MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_horizontal<T><<<nhz, hb, 0, st>>>(V(), HZ));
+    if (b.hstrip)
+      MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_hstrip<T><<<nhz, 128, 0, st>>>(V(), HZ));
+    else
+      MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_horizontal<T><<<nhz, hb, 0, st>>>(V(), HZ));
     fcur ^= 1;
     MOLOCH_LAUNCH(KK_STAG_FROM_X, st, kb_stag_from_x<T><<<npt, pb, 0, st>>>(V(), PT));
     cur = 0;
@@ -1293,7 +1450,10 @@ int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur) {
   const dim3 pb(kPtBX, kPtBY), cb(kColBX, kColBY), hb(32, 8);
   MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
   MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T><<<b.ntiles[TK_VERTICAL], cb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_VERTICAL]));
-  MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_horizontal<T><<<b.ntiles[TK_HORIZONTAL], hb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_HORIZONTAL]));
+  if (b.hstrip)
+    MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_hstrip<T><<<b.ntiles[TK_HORIZONTAL], 128, 0, st>>>(b.views[cur][fcur], b.tiles[TK_HORIZONTAL]));
+  else
+    MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_horizontal<T><<<b.ntiles[TK_HORIZONTAL], hb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_HORIZONTAL]));
   fcur ^= 1;
   MOLOCH_LAUNCH(KK_STAG_FROM_X, st, kb_stag_from_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
   cur = 0;

@@ -161,6 +161,7 @@ struct Batch {
   const View<T>* views[2][2];   // device arrays, one view per member
   const int4* tiles[TK_COUNT];  // device tile tables
   int ntiles[TK_COUNT];
+  int hstrip = 0;               // horizontal WAF as warp strips (tiles: member, block, level)
 };
 
 // launch counts per phase are returned by the launchers so the API can

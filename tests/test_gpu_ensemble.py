@@ -68,3 +68,22 @@ def test_ensemble_autotune(gpu_lib, stream):
     ens.close()
     for m in ms:
         m.close()
+
+
+def test_ensemble_strip_shape_matches_members(gpu_lib, stream):
+    """Ensemble with the warp-strip horizontal WAF against the same members
+    run alone with the tile kernel."""
+    ms = members(gpu_lib, "fp64", stream=stream.cuda_stream)
+    solo = members(gpu_lib, "fp64", stream=stream.cuda_stream)
+    e = gpu_lib.Ensemble(ms)
+    e.set_tuning([32])
+    e.run(2, graph=True)
+    for m in solo:
+        m.set_tuning([1])
+        m.run(2, graph=True)
+    for m, s in zip(ms, solo):
+        for n in ("u", "v", "w", "pai", "t", "qv"):
+            assert rel_l2(m.get(n), s.get(n)) <= 1e-13, n
+    e.close()
+    for m in ms + solo:
+        m.close()

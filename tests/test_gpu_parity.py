@@ -226,3 +226,27 @@ def test_setup_on_device_matches_host(gpu_lib, mode):
     for n in PROG + DIAG:
         e = rel_l2(b.get(n), a.get(n))
         assert e <= tol, (n, e)
+
+
+@pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
+@pytest.mark.parametrize("shape", [16, 32, 64])
+def test_horizontal_waf_strips_match_tiles(gpu_lib, mode, tol, shape):
+    """The warp-strip horizontal WAF kernel (launch shape >= 16 rows per
+    strip) against the tile kernel (shape 1): the same arithmetic, so the
+    exact build agrees bit for bit.  The contracting builds fuse
+    multiply-adds differently in the two kernels, and in FP32 the limiter
+    turns last-bit differences into differences of the size of the FP32
+    error itself (w: 8e-5 relative after 3 steps), hence 1e-3 there; odd
+    sizes exercise partial strips."""
+    a = gpu_lib.Moloch(61, 45, 9, mode=mode)
+    b = gpu_lib.Moloch(61, 45, 9, mode=mode)
+    for g in (a, b):
+        g.setup_idealized(hills=((400.0, 30.0, 22.0, 4.0),), u0=6.0, v0=-4.0)
+    a.set_tuning([1])
+    b.set_tuning([shape])
+    for s in range(1, 4):
+        a.moloch(s)
+        b.moloch(s)
+    for n in PROG:
+        e = rel_l2(b.get(n), a.get(n))
+        assert e <= tol, (n, e)
