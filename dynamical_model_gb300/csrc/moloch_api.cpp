@@ -269,6 +269,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.nj = h->nj(); v.ni = h->ni(); v.kz = h->kz(); v.pl = (int)pl; v.rotllr = h->prm.rotllr;
   v.cur = 0;
   v.hz_levels = 1;
+  v.kmarch = 0;
   v.sur_skip = nullptr;
   return off + 256;
 }
@@ -1110,7 +1111,9 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 // horizontal WAF launch shape: 1..8 = levels per 32x8 tile block, >= 16 =
 // rows per warp strip
 static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
-static const int kTuneCount = 1;
+// [0] horizontal WAF shape, [1] k-marching sound kernels (bit mask:
+// 1 divergence, 2 damping, 4 momentum)
+static const int kTuneCount = 2;
 
 int moloch_gpu_tuning_count(void) { return kTuneCount; }
 
@@ -1121,6 +1124,11 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     if (choice[0] < 1 || choice[0] > 64) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
     h->vd.hz_levels = choice[0];
     h->vf.hz_levels = choice[0];
+  }
+  if (n > 1) {
+    if (choice[1] < 0 || choice[1] > 7) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    h->vd.kmarch = choice[1];
+    h->vf.kmarch = choice[1];
   }
   for (int q = 0; q < 2; ++q) {  // launch shapes are baked into captured graphs
     if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
@@ -1160,10 +1168,35 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
     }
     if (tot < best) { best = tot; pick = cand; }
   }
+  h->vd.hz_levels = pick;
+  h->vf.hz_levels = pick;
+  // sound point kernels: one level per thread or k-marching (each of the
+  // three), timed on sound()
+  double best1 = 1e30;
+  int pick1 = h->elem == 8 ? h->vd.kmarch : h->vf.kmarch;
+  for (int cand = 0; cand < 8; ++cand) {
+    h->vd.kmarch = cand;
+    h->vf.kmarch = cand;
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, h->stream);
+      int nk = h->elem == 8 ? launch_phase(h, h->vd, 1) : launch_phase(h, h->vf, 1);
+      h->kernels += nk;
+      cudaEventRecord(e1, h->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best1) { best1 = tot; pick1 = cand; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   choice[0] = pick;
-  if (best_ms) best_ms[0] = best / 2.0;
+  choice[1] = pick1;
+  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1 / 2.0; }
   return moloch_gpu_set_tuning(h, choice, kTuneCount);
 }
 
@@ -1181,6 +1214,7 @@ struct moloch_ensemble {
   cudaGraph_t graph[2] = {nullptr, nullptr};
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   int hz_levels = 4;
+  int kmarch = 0;
   int cur = 0, fcur = 0;
   long long kernels = 0;
   int kernels_per_step = 0;
@@ -1215,6 +1249,9 @@ void ens_tiles(moloch_ensemble* e) {
       for (int x = 0; x < tj; ++x) e->tiles[TK_COLUMN].push_back(make_int4(q, x, y, 0));
     for (int y = 0; y < (ni + 3) / 4; ++y)
       for (int x = 0; x < tj * kNumAdvected; ++x) e->tiles[TK_VERTICAL].push_back(make_int4(q, x, y, 0));
+    for (int z = 0; z < (kz + kKC - 1) / kKC; ++z)
+      for (int y = 0; y < (ni + 7) / 8; ++y)
+        for (int x = 0; x < tj; ++x) e->tiles[TK_CHUNK].push_back(make_int4(q, x, y, z));
     if (e->hz_levels >= 16) {  // warp strips: 4 strips of hz_levels rows per block, every level
       const int nstrips = ((nj + 27) / 28) * ((ni + e->hz_levels - 1) / e->hz_levels);
       for (int z = 0; z < kz; ++z)
@@ -1258,6 +1295,7 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     b.tiles[t] = (const int4*)(p + off);
     b.ntiles[t] = (int)e->tiles[t].size();
     b.hstrip = e->hz_levels >= 16;
+    b.kmarch = e->kmarch;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
   return MOLOCH_OK;
@@ -1384,11 +1422,37 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
     }
     if (tot < best) { best = tot; pick = e->hz_levels; }
   }
+  e->hz_levels = pick;
+  // sound point kernels: one level per thread or k-marching (each of the
+  // three), timed on whole steps
+  const PhaseFlags fl = flags_of(e->m[0]);
+  double best1 = 1e30;
+  int pick1 = e->kmarch;
+  for (int cand = 0; cand < 8; ++cand) {
+    e->kmarch = cand;
+    int rc = ens_build(e);
+    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 2; ++rep) {
+      cudaEventRecord(e0, e->stream);
+      e->kernels += e->elem == 8 ? kfast::blaunch_step(e->bd, e->stream, fl, e->cur, e->fcur)
+                                 : kfast::blaunch_step(e->bf, e->stream, fl, e->cur, e->fcur);
+      cudaEventRecord(e1, e->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "ensemble autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best1) { best1 = tot; pick1 = cand; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  e->hz_levels = pick;
+  e->kmarch = pick1;
   choice[0] = pick;
-  if (best_ms) best_ms[0] = best / 2.0;
+  choice[1] = pick1;
+  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; }
   ens_sync_members(e);
   return ens_build(e);
 }
@@ -1399,6 +1463,10 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
   if (nchoice > 0) {
     if (choice[0] < 1 || choice[0] > 64) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
     e->hz_levels = choice[0];
+  }
+  if (nchoice > 1) {
+    if (choice[1] < 0 || choice[1] > 7) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    e->kmarch = choice[1];
   }
   return ens_build(e);
 }

@@ -644,6 +644,224 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
   b_sound_momentum<T>(sv, t.y, t.z, t.w);
 }
 
+// ---- k-marching variants of the point kernels of the sound loop ---------
+// One thread per (j, i) and chunk of kKC levels; the inputs of level k+1
+// are loaded into registers before level k is computed and stored, so each
+// thread keeps a level of loads in flight (the one-level-per-thread
+// versions above leave that to the warp scheduler and stall on latency).
+// Same arithmetic, expression by expression.
+template <class T>
+__device__ __forceinline__ void b_sound_div_km(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const int jj = bx * kPtBX + threadIdx.x;
+  const int ii = by * kPtBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni, kz = d.kz;
+  if (jj >= nj || ii >= ni) return;
+  const int k0 = bz * kKC, k1 = min(kz, k0 + kKC);
+  const size_t pl = d.pl;
+  const int jp = wp1(jj, nj), ip = wp1(ii, ni);
+  const T* __restrict__ u = d.ubuf[d.cur];
+  const T* __restrict__ v = d.vbuf[d.cur];
+  const size_t c = (size_t)jj + (size_t)nj * ii;
+  const size_t ce = (size_t)jp + (size_t)nj * ii;  // (j+1, i)
+  const size_t cn = (size_t)jj + (size_t)nj * ip;  // (j, i+1)
+  const T hx0 = d.hx[c], hx1 = d.hx[ce], hy0 = d.hy[c], hy1 = d.hy[cn];
+  const T dtrdx = d.dtrdx, dtrdy = d.dtrdy;
+  const T rmv0 = d.rmv[c], rmv1 = d.rmv[cn];
+  const bool rot = d.rotllr;
+  const T mxc = rot ? d.mx[c] : d.mx2[c];
+  const T rmu0 = rot ? T(0) : d.rmu[c], rmu1 = rot ? T(0) : d.rmu[ce];
+  struct L { T u0, u1, v0, v1, f, rfw0, rfw1, rfs0, rfs1, gz; };
+  auto load = [&](int k, L& x) {
+    const size_t o = (size_t)k * pl;
+    x.u0 = u[c + o]; x.u1 = u[ce + o]; x.v0 = v[c + o]; x.v1 = v[cn + o];
+    x.f = d.fmz[c + o];
+    x.rfw0 = d.rfw[c + o]; x.rfw1 = d.rfw[ce + o]; x.rfs0 = d.rfs[c + o]; x.rfs1 = d.rfs[cn + o];
+    x.gz = d.gzitak[k];
+  };
+  T u0p = T(0), u1p = T(0), v0p = T(0), v1p = T(0);  // level k-1
+  if (k0 > 0) {
+    const size_t q = (size_t)(k0 - 1) * pl;
+    u0p = u[c + q]; u1p = u[ce + q]; v0p = v[c + q]; v1p = v[cn + q];
+  }
+  L cur, nxt;
+  load(k0, nxt);
+  for (int kk = k0; kk < k1; ++kk) {
+    cur = nxt;
+    if (kk + 1 < k1) load(kk + 1, nxt);
+    const size_t o = (size_t)kk * pl;
+    const T u0 = cur.u0, u1 = cur.u1, v0 = cur.v0, v1 = cur.v1;
+    if (kk > 0) {  // s(k), k = 2..kz  (:557-570)
+      T zuh = (u0 + u0p) * hx0 + (u1 + u1p) * hx1;
+      T zvh = (v0 + v0p) * hy0 + (v1 + v1p) * hy1;
+      d.s[c + o] = -((T(0.25) * (zuh + zvh)) * cur.gz);
+    }
+    const T f = cur.f;
+    if (rot) {
+      const T zum = (dtrdx * u0) * cur.rfw0;
+      const T zup = (dtrdx * u1) * cur.rfw1;
+      const T zvm = ((dtrdy * v0) * cur.rfs0) * rmv0;
+      const T zvp = ((dtrdy * v1) * cur.rfs1) * rmv1;
+      d.zdiv2a[c + o] = (f * mxc) * ((zup - zum) + (zvp - zvm));
+    } else {
+      const T zum = ((dtrdx * u0) * rmu0) * cur.rfw0;
+      const T zup = ((dtrdx * u1) * rmu1) * cur.rfw1;
+      const T zvm = ((dtrdy * v0) * rmv0) * cur.rfs0;
+      const T zvp = ((dtrdy * v1) * rmv1) * cur.rfs1;
+      d.zdiv2a[c + o] = (mxc * f) * ((zup - zum) + (zvp - zvm));
+    }
+    if (jj == 0) d.eu_j[ii + (size_t)ni * kk] = u0;
+    if (ii == ni - 1) d.eu_i[jj + (size_t)nj * kk] = u0;
+    if (jj == nj - 1) d.ev_j[ii + (size_t)ni * kk] = v0;
+    if (ii == 0) d.ev_i[jj + (size_t)nj * kk] = v0;
+    if (kk == kz - 1) {  // surface w(kz+1), s(kz+1)
+      T zuh = u0 * hx0 + u1 * hx1;
+      T zvh = v0 * hy0 + v1 * hy1;
+      T ws = T(0.5) * (zuh + zvh);
+      d.w[c + (size_t)kz * pl] = ws;
+      d.s[c + (size_t)kz * pl] = -ws;
+    }
+    u0p = u0; u1p = u1; v0p = v0; v1p = v1;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void b_sound_damp_km(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const int jj = bx * kPtBX + threadIdx.x;
+  const int ii = by * kPtBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni;
+  if (jj >= nj || ii >= ni) return;
+  const int k0 = bz * kKC, k1 = min(d.kz, k0 + kKC);
+  const size_t pl = d.pl;
+  const size_t c = (size_t)jj + (size_t)nj * ii;
+  const size_t cw = (size_t)wm1(jj, nj) + (size_t)nj * ii, ce = (size_t)wp1(jj, nj) + (size_t)nj * ii;
+  const size_t cs = (size_t)jj + (size_t)nj * wm1(ii, ni), cn = (size_t)jj + (size_t)nj * wp1(ii, ni);
+  T* __restrict__ u = d.ubuf[d.cur];
+  T* __restrict__ v = d.vbuf[d.cur];
+  const T muc = d.mu[c];
+  const T mvc = d.rotllr ? T(0) : d.mv[c];
+  const T ddamp2 = d.ddamp2, dtrdz = d.dtrdz;
+  struct L { T zc, zw, ze, zs, zn, s1, uc, vc, fz, cd; };
+  auto load = [&](int k, L& x) {
+    const size_t o = (size_t)k * pl;
+    x.zc = d.zdiv2a[c + o]; x.zw = d.zdiv2a[cw + o]; x.ze = d.zdiv2a[ce + o];
+    x.zs = d.zdiv2a[cs + o]; x.zn = d.zdiv2a[cn + o];
+    x.s1 = d.s[c + o + pl];
+    x.uc = u[c + o]; x.vc = v[c + o];
+    x.fz = d.fmz[c + o];
+    x.cd = d.cdamp[k];
+  };
+  T s_k = d.s[c + (size_t)k0 * pl];  // s(k); s(k+1) is carried to the next level
+  L cur, nxt;
+  load(k0, nxt);
+  for (int kk = k0; kk < k1; ++kk) {
+    cur = nxt;
+    if (kk + 1 < k1) load(kk + 1, nxt);
+    const size_t o = (size_t)kk * pl;
+    const T zc = cur.zc, zw = cur.zw, ze = cur.ze, zs = cur.zs, zn = cur.zn, cd = cur.cd;
+    u[c + o] = cur.uc + ((cd * muc) * (zc - zw));
+    if (d.rotllr)
+      v[c + o] = cur.vc + cd * (zc - zs);
+    else
+      v[c + o] = cur.vc + ((cd * mvc) * (zc - zs));
+    const T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
+    T zd = zc + ddamp2 * p2d;
+    zd = zd + (cur.fz * dtrdz) * (s_k - cur.s1);
+    d.zdiv2b[c + o] = zd;
+    s_k = cur.s1;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ void b_sound_momentum_km(const View<T>& d, const int bx, const int by, const int bz) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const int jj = bx * kPtBX + threadIdx.x;
+  const int ii = by * kPtBY + threadIdx.y;
+  const int nj = d.nj, ni = d.ni;
+  if (jj >= nj || ii >= ni) return;
+  const int k0 = bz * kKC, k1 = min(d.kz, k0 + kKC);
+  const size_t pl = d.pl;
+  const int jm = wm1(jj, nj), jp = wp1(jj, nj), im = wm1(ii, ni), ip = wp1(ii, ni);
+  const T* __restrict__ u = d.ubuf[d.cur];
+  const T* __restrict__ v = d.vbuf[d.cur];
+  T* __restrict__ uo = d.ubuf[d.cur ^ 1];
+  T* __restrict__ vo = d.vbuf[d.cur ^ 1];
+  const size_t c = (size_t)jj + (size_t)nj * ii;
+  const size_t cw = (size_t)jm + (size_t)nj * ii, ce = (size_t)jp + (size_t)nj * ii;
+  const size_t cs = (size_t)jj + (size_t)nj * im, cn = (size_t)jj + (size_t)nj * ip;
+  const size_t cwn = (size_t)jm + (size_t)nj * ip, ces = (size_t)jp + (size_t)nj * im;
+  const T dts = d.dts, egdts = d.egdts;
+  const T hcpd = T(0.5) * T(kCpd);
+  const T zcx = d.dtrdx * d.mu[c];
+  const T zcy = d.rotllr ? d.dtrdy : d.dtrdy * d.mv[c];
+  const T corx = (d.coru[c] * dts) * T(0.25), cory = (d.corv[c] * dts) * T(0.25);
+  const T hxc = d.hx[c], hyc = d.hy[c];
+  struct L { T dwc1, dww1, dws1, tc, tw, ts, pc, pw, ps, uc, us, ue, ues, vc, vw, vwn, vn, gzh; };
+  auto load = [&](int k, L& x) {
+    const size_t o = (size_t)k * pl, o1 = o + pl;
+    x.dwc1 = d.deltaw[c + o1]; x.dww1 = d.deltaw[cw + o1]; x.dws1 = d.deltaw[cs + o1];
+    x.tc = d.tetav[c + o]; x.tw = d.tetav[cw + o]; x.ts = d.tetav[cs + o];
+    x.pc = d.pai[c + o];
+    x.pw = jj == 0 ? d.ep_j[ii + (size_t)ni * k] : d.pai[cw + o];
+    x.ps = ii == 0 ? d.ep_i[jj + (size_t)nj * k] : d.pai[cs + o];
+    x.vc = v[c + o];
+    x.vw = jj == 0 ? d.ev_j[ii + (size_t)ni * k] : v[cw + o];
+    x.vwn = jj == 0 ? d.ev_j[ip + (size_t)ni * k] : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * k] : v[cwn + o]);
+    x.vn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * k] : v[cn + o];
+    x.uc = u[c + o];
+    x.us = ii == 0 ? d.eu_i[jj + (size_t)nj * k] : u[cs + o];
+    x.ue = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * k] : u[ce + o];
+    x.ues = jj == nj - 1 ? d.eu_j[im + (size_t)ni * k] : (ii == 0 ? d.eu_i[jp + (size_t)nj * k] : u[ces + o]);
+    x.gzh = d.gzitakh[k];
+  };
+  // deltaw at level k of (c, w, s); level k+1 is carried to the next level
+  T dw_c = d.deltaw[c + (size_t)k0 * pl], dw_w = d.deltaw[cw + (size_t)k0 * pl];
+  T dw_s = d.deltaw[cs + (size_t)k0 * pl];
+  L cur, nxt;
+  load(k0, nxt);
+  for (int kk = k0; kk < k1; ++kk) {
+    cur = nxt;
+    if (kk + 1 < k1) load(kk + 1, nxt);
+    const size_t o = (size_t)kk * pl;
+    const T tc = cur.tc, pc = cur.pc, gzh = cur.gzh;
+    // Equation 17
+    {
+      const T zfz = egdts + T(0.25) * (((dw_w + cur.dww1) + dw_c) + cur.dwc1);
+      const T zrom1u = hcpd * (cur.tw + tc);
+      const T zcor1u = corx * (((cur.vc + cur.vw) + cur.vwn) + cur.vn);
+      uo[c + o] = ((cur.uc + zcor1u) - (zfz * hxc) * gzh) - (zcx * zrom1u) * (pc - cur.pw);
+    }
+    // Equation 18
+    {
+      const T zfz = egdts + T(0.25) * (((dw_s + cur.dws1) + dw_c) + cur.dwc1);
+      const T zrom1v = hcpd * (cur.ts + tc);
+      const T zcor1v = cory * (((cur.uc + cur.us) + cur.ue) + cur.ues);
+      vo[c + o] = ((cur.vc - zcor1v) - (zfz * hyc) * gzh) - (zcy * zrom1v) * (pc - cur.ps);
+    }
+    dw_c = cur.dwc1; dw_w = cur.dww1; dw_s = cur.dws1;
+  }
+}
+
+#define MOLOCH_KM_KERNELS(NAME)                                                                      \
+  template <class T>                                                                                 \
+  __global__ void __launch_bounds__(kPtBX* kPtBY) k_##NAME##_km(View<T> d) {                          \
+    b_##NAME##_km<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);                                         \
+  }                                                                                                  \
+  template <class T>                                                                                 \
+  __global__ void __launch_bounds__(kPtBX* kPtBY)                                                    \
+      kb_##NAME##_km(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {            \
+    __shared__ View<T> sv;                                                                           \
+    const int4 t = tiles[blockIdx.x];                                                                \
+    copy_view(&sv, views + t.x);                                                                     \
+    __syncthreads();                                                                                 \
+    b_##NAME##_km<T>(sv, t.y, t.z, t.w);                                                             \
+  }
+MOLOCH_KM_KERNELS(sound_div)
+MOLOCH_KM_KERNELS(sound_damp)
+MOLOCH_KM_KERNELS(sound_momentum)
+#undef MOLOCH_KM_KERNELS
+
 // ---- advection: staggered -> cross points (:1327-1341, :1389-1417) -----
 template <class T>
 __device__ __forceinline__ void b_stag_to_x(const View<T>& d, const int bx, const int by, const int bz) {
@@ -1327,10 +1545,17 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   int n = 0;
   const dim3 cb(kColBX, kColBY), cg = col_grid(d.nj, d.ni);
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
+  const dim3 kg = pt_grid(d.nj, d.ni, (d.kz + kKC - 1) / kKC);  // k-marching: chunks of kKC levels
   for (int ns = 1; ns <= fl.nsound; ++ns) {
     const int last = ns == fl.nsound;
-    MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div<T><<<pg, pb, 0, st>>>(d));
-    MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp<T><<<pg, pb, 0, st>>>(d));
+    if (d.kmarch & 1)
+      MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div_km<T><<<kg, pb, 0, st>>>(d));
+    else
+      MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div<T><<<pg, pb, 0, st>>>(d));
+    if (d.kmarch & 2)
+      MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp_km<T><<<kg, pb, 0, st>>>(d));
+    else
+      MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp<T><<<pg, pb, 0, st>>>(d));
     n += 2;
     if (fl.divfilter) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 1));
@@ -1341,7 +1566,10 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
-    MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum<T><<<pg, pb, 0, st>>>(d));
+    if (d.kmarch & 4)
+      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum_km<T><<<kg, pb, 0, st>>>(d));
+    else
+      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum<T><<<pg, pb, 0, st>>>(d));
     ++n;
     d.cur ^= 1;
   }
@@ -1408,6 +1636,8 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
   const int4* CO = b.tiles[TK_COLUMN];
   const int4* VE = b.tiles[TK_VERTICAL];
   const int4* HZ = b.tiles[TK_HORIZONTAL];
+  const int4* KC = b.tiles[TK_CHUNK];
+  const int nkc = b.ntiles[TK_CHUNK];
   const int npt = b.ntiles[TK_POINT], nco = b.ntiles[TK_COLUMN];
   const int nve = b.ntiles[TK_VERTICAL], nhz = b.ntiles[TK_HORIZONTAL];
   MOLOCH_LAUNCH(KK_PREDIAG, st, kb_prediag<T><<<npt, pb, 0, st>>>(V(), PT, fl.filterpai, fl.filtertheta));
@@ -1415,8 +1645,14 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
   for (int a = 0; a < fl.nadv; ++a) {
     for (int ns = 1; ns <= fl.nsound; ++ns) {
       const int last = ns == fl.nsound;
-      MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div<T><<<npt, pb, 0, st>>>(V(), PT));
-      MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp<T><<<npt, pb, 0, st>>>(V(), PT));
+      if (b.kmarch & 1)
+        MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div_km<T><<<nkc, pb, 0, st>>>(V(), KC));
+      else
+        MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div<T><<<npt, pb, 0, st>>>(V(), PT));
+      if (b.kmarch & 2)
+        MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp_km<T><<<nkc, pb, 0, st>>>(V(), KC));
+      else
+        MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp<T><<<npt, pb, 0, st>>>(V(), PT));
       if (fl.divfilter) {
         MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 1));
         MOLOCH_LAUNCH(KK_LAP_FILTER, st, kb_lap_filter<T><<<npt, pb, 0, st>>>(V(), PT));
@@ -1425,7 +1661,10 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
       } else {
         MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 0));
       }
-      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum<T><<<npt, pb, 0, st>>>(V(), PT));
+      if (b.kmarch & 4)
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum_km<T><<<nkc, pb, 0, st>>>(V(), KC));
+      else
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum<T><<<npt, pb, 0, st>>>(V(), PT));
       n += 4;
       cur ^= 1;
     }

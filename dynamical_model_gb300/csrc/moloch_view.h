@@ -107,6 +107,7 @@ struct View {
 
   // launch shape chosen by the autotuner: levels per k_waf_horizontal block
   int hz_levels;
+  int kmarch;      // k-marching sound kernels, bit mask: 1 divergence, 2 damping, 4 momentum
 
   // set when a learned surrogate stands in for sound(): the plain sound
   // kernels return at once while *sur_skip == 1 (the surrogate's cycle was
@@ -155,13 +156,16 @@ struct KernelTimer {
 // takes a 1-D grid that walks a tile table of (member, bx, by, bz) entries
 // and reads the member's view from views[cur][fcur] (the u/v buffer and
 // field-set parities the step is at when the kernel runs).
-enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_COUNT };
+// TK_CHUNK tiles cover kKC levels each (the k-marching sound kernels)
+constexpr int kKC = 4;
+enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_COUNT };
 template <class T>
 struct Batch {
   const View<T>* views[2][2];   // device arrays, one view per member
   const int4* tiles[TK_COUNT];  // device tile tables
   int ntiles[TK_COUNT];
   int hstrip = 0;               // horizontal WAF as warp strips (tiles: member, block, level)
+  int kmarch = 0;               // k-marching sound kernels on TK_CHUNK tiles (bit mask as View::kmarch)
 };
 
 // launch counts per phase are returned by the launchers so the API can

@@ -184,10 +184,15 @@ int moloch_gpu_kernel_kinds(void);
 const char* moloch_gpu_kernel_name(int kind);
 
 /* Project-written autotuner.  Launch shapes that depend on the grid are
- * timed with CUDA events on the handle's stream and the fastest is kept:
- * choice[0] = levels per block of the horizontal WAF kernel (1, 2, 4, 8).
- * moloch_gpu_autotune runs advection() once per candidate and repeat, so it
- * advances the model state: call it on a scratch handle or before the
+ * timed with CUDA events on the handle's stream and the fastest is kept
+ * (moloch_gpu_tuning_count() slots):
+ *   choice[0] = horizontal WAF kernel: 1, 2, 4, 8 levels per 32x8 tile
+ *               block, or 16, 32, 64 rows per warp strip;
+ *   choice[1] = k-marching sound kernels (chunks of 4 levels per thread,
+ *               next level prefetched), bit mask: 1 divergence, 2 damping,
+ *               4 momentum; 0 = one level per thread.
+ * moloch_gpu_autotune runs advection() and sound() once per candidate and
+ * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the
  * caller and applied to new handles with moloch_gpu_set_tuning.  No
  * reference counterpart (the reference has no GPU launch shapes). */
@@ -211,7 +216,7 @@ typedef struct moloch_ensemble moloch_ensemble_t;
 int moloch_gpu_ensemble_create(int nmembers, moloch_handle_t* const* members, moloch_ensemble_t** out);
 int moloch_gpu_ensemble_run(moloch_ensemble_t* e, int nsteps, int use_graph);
 /* event-timed choice of the launch shapes over the whole ensemble (advances
- * the members' state); choice[0] = levels per horizontal WAF tile */
+ * the members' state); choice as for moloch_gpu_autotune */
 int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best_ms, int nchoice);
 int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int nchoice);
 long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);

@@ -71,15 +71,16 @@ def test_ensemble_autotune(gpu_lib, stream):
 
 
 def test_ensemble_strip_shape_matches_members(gpu_lib, stream):
-    """Ensemble with the warp-strip horizontal WAF against the same members
-    run alone with the tile kernel."""
+    """Ensemble with the warp-strip horizontal WAF and the k-marching sound
+    kernels against the same members run alone with the tile kernel and the
+    one-level-per-thread kernels."""
     ms = members(gpu_lib, "fp64", stream=stream.cuda_stream)
     solo = members(gpu_lib, "fp64", stream=stream.cuda_stream)
     e = gpu_lib.Ensemble(ms)
-    e.set_tuning([32])
+    e.set_tuning([32, 7])
     e.run(2, graph=True)
     for m in solo:
-        m.set_tuning([1])
+        m.set_tuning([1, 0])
         m.run(2, graph=True)
     for m, s in zip(ms, solo):
         for n in ("u", "v", "w", "pai", "t", "qv"):

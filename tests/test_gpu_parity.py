@@ -250,3 +250,23 @@ def test_horizontal_waf_strips_match_tiles(gpu_lib, mode, tol, shape):
     for n in PROG:
         e = rel_l2(b.get(n), a.get(n))
         assert e <= tol, (n, e)
+
+
+@pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
+@pytest.mark.parametrize("kz", [9, 13])
+def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz):
+    """The k-marching divergence/damping/momentum kernels (chunks of 4
+    levels, the next level prefetched) against the one-level-per-thread
+    kernels: bit for bit in the exact build; kz not a multiple of the chunk."""
+    a = gpu_lib.Moloch(45, 37, kz, mode=mode)
+    b = gpu_lib.Moloch(45, 37, kz, mode=mode)
+    for g in (a, b):
+        g.setup_idealized(hills=((400.0, 22.0, 18.0, 4.0),), u0=6.0, v0=-4.0)
+    a.set_tuning([1, 0])
+    b.set_tuning([1, 7])
+    for s in range(1, 4):
+        a.moloch(s)
+        b.moloch(s)
+    for n in PROG + ("s", "deltaw"):
+        e = rel_l2(b.get(n), a.get(n))
+        assert e <= tol, (n, e)
