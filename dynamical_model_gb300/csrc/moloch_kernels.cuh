@@ -447,7 +447,7 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
 }
 
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4) k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4) k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
   b_sound_column<T>(d, blockIdx.x, blockIdx.y, blockIdx.z, nsound, last, defer_pai);
 }
 
