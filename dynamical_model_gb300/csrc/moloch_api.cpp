@@ -1111,8 +1111,8 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 // horizontal WAF launch shape: 1..8 = levels per 32x8 tile block, >= 16 =
 // rows per warp strip
 static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
-// [0] horizontal WAF shape, [1] k-marching sound kernels (bit mask:
-// 1 divergence, 2 damping, 4 momentum)
+// [0] horizontal WAF shape, [1] sound kernel variants (bit mask:
+// 1 divergence, 2 damping, 4 momentum k-marching; 8 momentum warp strips)
 static const int kTuneCount = 2;
 
 int moloch_gpu_tuning_count(void) { return kTuneCount; }
@@ -1126,7 +1126,7 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     h->vf.hz_levels = choice[0];
   }
   if (n > 1) {
-    if (choice[1] < 0 || choice[1] > 7) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 15) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     h->vd.kmarch = choice[1];
     h->vf.kmarch = choice[1];
   }
@@ -1174,7 +1174,8 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   // three), timed on sound()
   double best1 = 1e30;
   int pick1 = h->elem == 8 ? h->vd.kmarch : h->vf.kmarch;
-  for (int cand = 0; cand < 8; ++cand) {
+  for (int cand = 0; cand < 16; ++cand) {
+    if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     h->vd.kmarch = cand;
     h->vf.kmarch = cand;
     float ms = 0.f, tot = 0.f;
@@ -1252,6 +1253,11 @@ void ens_tiles(moloch_ensemble* e) {
     for (int z = 0; z < (kz + kKC - 1) / kKC; ++z)
       for (int y = 0; y < (ni + 7) / 8; ++y)
         for (int x = 0; x < tj; ++x) e->tiles[TK_CHUNK].push_back(make_int4(q, x, y, z));
+    {
+      const int nstrips = ((nj + kMomJ - 1) / kMomJ) * ((ni + kMomR - 1) / kMomR);
+      for (int z = 0; z < kz; ++z)
+        for (int x = 0; x < (nstrips + 3) / 4; ++x) e->tiles[TK_MSTRIP].push_back(make_int4(q, x, z, 0));
+    }
     if (e->hz_levels >= 16) {  // warp strips: 4 strips of hz_levels rows per block, every level
       const int nstrips = ((nj + 27) / 28) * ((ni + e->hz_levels - 1) / e->hz_levels);
       for (int z = 0; z < kz; ++z)
@@ -1428,7 +1434,8 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   const PhaseFlags fl = flags_of(e->m[0]);
   double best1 = 1e30;
   int pick1 = e->kmarch;
-  for (int cand = 0; cand < 8; ++cand) {
+  for (int cand = 0; cand < 16; ++cand) {
+    if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     e->kmarch = cand;
     int rc = ens_build(e);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
@@ -1465,7 +1472,7 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
     e->hz_levels = choice[0];
   }
   if (nchoice > 1) {
-    if (choice[1] < 0 || choice[1] > 7) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 15) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     e->kmarch = choice[1];
   }
   return ens_build(e);

@@ -862,6 +862,119 @@ MOLOCH_KM_KERNELS(sound_damp)
 MOLOCH_KM_KERNELS(sound_momentum)
 #undef MOLOCH_KM_KERNELS
 
+
+// ---- momentum as warp strips (:730-837) -------------------------------------
+// One warp per strip of 30 output columns x R rows of one level (R =
+// d.hz_levels rows when the strips are chosen), lanes on columns j0-1 ..
+// j0+30.  West and east neighbours come from the lanes beside (shuffles),
+// the row below from the previous row kept in registers, the row above
+// (v at i+1) from the next row, which is loaded before the row is computed.
+// The stale-halo reads of the reference (edge buffers at j = 1, j = nj,
+// i = 1, i = ni) replace the neighbour values on those lanes and rows, as in
+// k_sound_momentum.
+template <class T>
+__device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx, const int k, const int R) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nj = d.nj, ni = d.ni, pl = d.pl;
+  const int nsj = (nj + kMomJ - 1) / kMomJ, nsi = (ni + R - 1) / R;
+  const int w = bx * (blockDim.x >> 5) + wid;
+  if (w >= nsj * nsi) return;  // whole warp
+  const int sj = w % nsj, si = w / nsj;
+  const int jl = sj * kMomJ - 1 + lane;
+  const int jj = wrapn(jl, nj);
+  const bool out_lane = lane >= 1 && lane <= kMomJ && jl < nj;
+  const int i_s = si * R, i_e = min(i_s + R, ni);
+  const size_t o = (size_t)k * pl, o1 = o + pl;
+  const T* __restrict__ u = d.ubuf[d.cur] + o;
+  const T* __restrict__ v = d.vbuf[d.cur] + o;
+  T* __restrict__ uo = d.ubuf[d.cur ^ 1] + o;
+  T* __restrict__ vo = d.vbuf[d.cur ^ 1] + o;
+  const T* __restrict__ tet = d.tetav + o;
+  const T* __restrict__ pai = d.pai + o;
+  const T* __restrict__ dw0 = d.deltaw + o;
+  const T* __restrict__ dw1 = d.deltaw + o1;
+  const T dts = d.dts, egdts = d.egdts, dtrdx = d.dtrdx, dtrdy = d.dtrdy;
+  const T hcpd = T(0.5) * T(kCpd);
+  const T gzh = d.gzitakh[k];
+  const bool rot = d.rotllr;
+  const int jm = wm1(jj, nj), jp = wp1(jj, nj);
+  // per-row inputs of this lane's column
+  struct Row { T u, v, t, p, d0, d1, vn, coru, corv, hx, hy, mu, mv; };
+  auto load = [&](int i, Row& x) {
+    const size_t c = (size_t)jj + (size_t)nj * wrapn(i, ni);
+    const size_t cn = (size_t)jj + (size_t)nj * wrapn(i + 1, ni);
+    x.u = u[c]; x.v = v[c]; x.t = tet[c]; x.p = pai[c]; x.d0 = dw0[c]; x.d1 = dw1[c];
+    x.vn = v[cn];
+    x.coru = d.coru[c]; x.corv = d.corv[c]; x.hx = d.hx[c]; x.hy = d.hy[c]; x.mu = d.mu[c];
+    x.mv = rot ? T(0) : d.mv[c];
+  };
+  // the row below the first row: u, tetav, pai, deltaw (k, k+1)
+  Row cur, nxt;
+  load(i_s - 1, cur);
+  T us = cur.u, ts = cur.t, ps = cur.p, ds0 = cur.d0, ds1 = cur.d1;
+  load(i_s, nxt);
+  for (int i = i_s; i < i_e; ++i) {
+    cur = nxt;
+    if (i + 1 < i_e) load(i + 1, nxt);
+    const int ii = i, ip = wp1(ii, ni), im = wm1(ii, ni);
+    // neighbours from the lanes beside
+    const T ue = __shfl_down_sync(0xffffffffu, cur.u, 1);
+    const T ues = __shfl_down_sync(0xffffffffu, us, 1);
+    const T vw = __shfl_up_sync(0xffffffffu, cur.v, 1);
+    const T vwn = __shfl_up_sync(0xffffffffu, cur.vn, 1);
+    const T tw = __shfl_up_sync(0xffffffffu, cur.t, 1);
+    const T pw = __shfl_up_sync(0xffffffffu, cur.p, 1);
+    const T dw0w = __shfl_up_sync(0xffffffffu, cur.d0, 1);
+    const T dw1w = __shfl_up_sync(0xffffffffu, cur.d1, 1);
+    if (out_lane) {
+      const T dw_c = cur.d0, dw_c1 = cur.d1;
+      const T tc = cur.t, pc = cur.p;
+      // Equation 17
+      {
+        const T zcx = dtrdx * cur.mu;
+        const T zfz = egdts + T(0.25) * (((dw0w + dw1w) + dw_c) + dw_c1);
+        const T zrom1u = hcpd * (tw + tc);
+        const T vdc = cur.v;
+        const T vdw = jj == 0 ? d.ev_j[ii + (size_t)ni * k] : vw;
+        const T vdwn = jj == 0 ? d.ev_j[ip + (size_t)ni * k] : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * k] : vwn);
+        const T vdn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * k] : cur.vn;
+        const T zcor1u = ((cur.coru * dts) * T(0.25)) * (((vdc + vdw) + vdwn) + vdn);
+        const T paw = jj == 0 ? d.ep_j[ii + (size_t)ni * k] : pw;
+        uo[(size_t)jj + (size_t)nj * ii] = ((cur.u + zcor1u) - (zfz * cur.hx) * gzh) - (zcx * zrom1u) * (pc - paw);
+      }
+      // Equation 18
+      {
+        const T zcy = rot ? dtrdy : dtrdy * cur.mv;
+        const T zfz = egdts + T(0.25) * (((ds0 + ds1) + dw_c) + dw_c1);
+        const T zrom1v = hcpd * (ts + tc);
+        const T udc = cur.u;
+        const T uds = ii == 0 ? d.eu_i[jj + (size_t)nj * k] : us;
+        const T ude = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * k] : ue;
+        const T udes = jj == nj - 1 ? d.eu_j[im + (size_t)ni * k] : (ii == 0 ? d.eu_i[jp + (size_t)nj * k] : ues);
+        const T zcor1v = ((cur.corv * dts) * T(0.25)) * (((udc + uds) + ude) + udes);
+        const T pas = ii == 0 ? d.ep_i[jj + (size_t)nj * k] : ps;
+        vo[(size_t)jj + (size_t)nj * ii] = ((cur.v - zcor1v) - (zfz * cur.hy) * gzh) - (zcy * zrom1v) * (pc - pas);
+      }
+    }
+    us = cur.u; ts = cur.t; ps = cur.p; ds0 = cur.d0; ds1 = cur.d1;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_momentum_strip(View<T> d, int R) {
+  b_momentum_strip<T>(d, blockIdx.x, blockIdx.y, R);
+}
+
+template <class T>
+__global__ void __launch_bounds__(128)
+    kb_momentum_strip(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int R) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_momentum_strip<T>(sv, t.y, t.z, R);
+}
+
 // ---- advection: staggered -> cross points (:1327-1341, :1389-1417) -----
 template <class T>
 __device__ __forceinline__ void b_stag_to_x(const View<T>& d, const int bx, const int by, const int bz) {
@@ -1566,7 +1679,10 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
-    if (d.kmarch & 4)
+    if (d.kmarch & 8) {
+      const int nstrips = ((d.nj + kMomJ - 1) / kMomJ) * ((d.ni + kMomR - 1) / kMomR);
+      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
+    } else if (d.kmarch & 4)
       MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum_km<T><<<kg, pb, 0, st>>>(d));
     else
       MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum<T><<<pg, pb, 0, st>>>(d));
@@ -1661,7 +1777,9 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
       } else {
         MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 0));
       }
-      if (b.kmarch & 4)
+      if (b.kmarch & 8)
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_momentum_strip<T><<<b.ntiles[TK_MSTRIP], 128, 0, st>>>(V(), b.tiles[TK_MSTRIP], kMomR));
+      else if (b.kmarch & 4)
         MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum_km<T><<<nkc, pb, 0, st>>>(V(), KC));
       else
         MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum<T><<<npt, pb, 0, st>>>(V(), PT));

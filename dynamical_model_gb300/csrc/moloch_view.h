@@ -107,7 +107,8 @@ struct View {
 
   // launch shape chosen by the autotuner: levels per k_waf_horizontal block
   int hz_levels;
-  int kmarch;      // k-marching sound kernels, bit mask: 1 divergence, 2 damping, 4 momentum
+  int kmarch;      // sound kernel variants, bit mask: 1 divergence, 2 damping, 4 momentum
+                   // k-marching; 8 momentum as warp strips
 
   // set when a learned surrogate stands in for sound(): the plain sound
   // kernels return at once while *sur_skip == 1 (the surrogate's cycle was
@@ -156,9 +157,12 @@ struct KernelTimer {
 // takes a 1-D grid that walks a tile table of (member, bx, by, bz) entries
 // and reads the member's view from views[cur][fcur] (the u/v buffer and
 // field-set parities the step is at when the kernel runs).
-// TK_CHUNK tiles cover kKC levels each (the k-marching sound kernels)
+// TK_CHUNK tiles cover kKC levels each (the k-marching sound kernels);
+// TK_MSTRIP tiles are blocks of 4 momentum warp strips (30 columns x kMomR
+// rows) of one level
 constexpr int kKC = 4;
-enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_COUNT };
+constexpr int kMomJ = 30, kMomR = 32;
+enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_COUNT };
 template <class T>
 struct Batch {
   const View<T>* views[2][2];   // device arrays, one view per member

@@ -188,9 +188,10 @@ const char* moloch_gpu_kernel_name(int kind);
  * (moloch_gpu_tuning_count() slots):
  *   choice[0] = horizontal WAF kernel: 1, 2, 4, 8 levels per 32x8 tile
  *               block, or 16, 32, 64 rows per warp strip;
- *   choice[1] = k-marching sound kernels (chunks of 4 levels per thread,
- *               next level prefetched), bit mask: 1 divergence, 2 damping,
- *               4 momentum; 0 = one level per thread.
+ *   choice[1] = sound kernel variants, bit mask: 1 divergence, 2 damping,
+ *               4 momentum as k-marching kernels (chunks of 4 levels per
+ *               thread, next level prefetched), 8 momentum as warp strips
+ *               (30 columns x 32 rows); 0 = one level per thread.
  * moloch_gpu_autotune runs advection() and sound() once per candidate and
  * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the

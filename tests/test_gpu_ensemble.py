@@ -77,7 +77,7 @@ def test_ensemble_strip_shape_matches_members(gpu_lib, stream):
     ms = members(gpu_lib, "fp64", stream=stream.cuda_stream)
     solo = members(gpu_lib, "fp64", stream=stream.cuda_stream)
     e = gpu_lib.Ensemble(ms)
-    e.set_tuning([32, 7])
+    e.set_tuning([32, 11])
     e.run(2, graph=True)
     for m in solo:
         m.set_tuning([1, 0])

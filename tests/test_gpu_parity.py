@@ -253,17 +253,20 @@ def test_horizontal_waf_strips_match_tiles(gpu_lib, mode, tol, shape):
 
 
 @pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
-@pytest.mark.parametrize("kz", [9, 13])
-def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz):
+@pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8)])
+def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz, variant):
     """The k-marching divergence/damping/momentum kernels (chunks of 4
-    levels, the next level prefetched) against the one-level-per-thread
-    kernels: bit for bit in the exact build; kz not a multiple of the chunk."""
+    levels, the next level prefetched) and the warp-strip momentum kernel
+    (30 columns x 32 rows, neighbours by shuffles, stale-halo edge buffers
+    on the boundary lanes and rows) against the one-level-per-thread
+    kernels: bit for bit in the exact build; kz not a multiple of the chunk,
+    jx and iy not multiples of the strip."""
     a = gpu_lib.Moloch(45, 37, kz, mode=mode)
     b = gpu_lib.Moloch(45, 37, kz, mode=mode)
     for g in (a, b):
         g.setup_idealized(hills=((400.0, 22.0, 18.0, 4.0),), u0=6.0, v0=-4.0)
     a.set_tuning([1, 0])
-    b.set_tuning([1, 7])
+    b.set_tuning([1, variant])
     for s in range(1, 4):
         a.moloch(s)
         b.moloch(s)
