@@ -61,6 +61,8 @@ __device__ __forceinline__ int wp1(int x, int n) { return x == n - 1 ? 0 : x + 1
 __device__ __forceinline__ int wm2(int x, int n) { int y = x - 2; return y < 0 ? y + n : y; }
 __device__ __forceinline__ int wp2(int x, int n) { int y = x + 2; return y >= n ? y - n : y; }
 __device__ __forceinline__ int wrapn(int x, int n) { int y = x % n; return y < 0 ? y + n : y; }
+// periodic index for -n <= x < 2n (no integer division)
+__device__ __forceinline__ int wrap2(int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
 
 __device__ __forceinline__ double dpow(double a, double b) { return pow(a, b); }
 __device__ __forceinline__ float dpow(float a, float b) { return powf(a, b); }
@@ -901,8 +903,8 @@ __device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx,
   // per-row inputs of this lane's column
   struct Row { T u, v, t, p, d0, d1, vn, coru, corv, hx, hy, mu, mv; };
   auto load = [&](int i, Row& x) {
-    const size_t c = (size_t)jj + (size_t)nj * wrapn(i, ni);
-    const size_t cn = (size_t)jj + (size_t)nj * wrapn(i + 1, ni);
+    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+    const size_t cn = (size_t)jj + (size_t)nj * wrap2(i + 1, ni);
     x.u = u[c]; x.v = v[c]; x.t = tet[c]; x.p = pai[c]; x.d0 = dw0[c]; x.d1 = dw1[c];
     x.vn = v[cn];
     x.coru = d.coru[c]; x.corv = d.corv[c]; x.hx = d.hx[c]; x.hy = d.hy[c]; x.mu = d.mu[c];
@@ -1335,7 +1337,7 @@ __device__ __forceinline__ void b_waf_hstrip(const View<T>& d, const int bx, con
   const T* __restrict__ ww_ = d.wafw + (size_t)k * pl;
   const T dtrdx = d.dtrdx_a, dtrdy = d.dtrdy_a;
   const bool rot = d.rotllr;
-  auto row = [&](int i) { return (size_t)j + (size_t)nj * wrapn(i, ni); };
+  auto row = [&](int i) { return (size_t)j + (size_t)nj * wrap2(i, ni); };
 
   for (int g0 = 0; g0 < kNumAdvected; g0 += G) {
     const int ng = min(G, kNumAdvected - g0);
