@@ -1038,6 +1038,22 @@ __device__ __forceinline__ T waf_vflux(T s_k1, T dtrdz, T xm, T x0, T x1, T x2) 
   const T zphi = (is + zamu * bb) - is * bb;
   return (T(0.5) * s_k1) * ((T(1) + zphi) * x1 + (T(1) - zphi) * x0);
 }
+// FP32 storage: the same flux, rearranged for fewer instructions (these
+// kernels are bound by the ALU pipe, not HBM): superbee as
+// max(sat(2r), min(r, 2)), phi = is + bb (zamu - is), and
+// (1+phi) x1 + (1-phi) x0 = (x1 + x0) - phi (x0 - x1)
+template <>
+__device__ __forceinline__ float waf_vflux<float>(float s_k1, float dtrdz, float xm, float x0, float x1, float x2) {
+  const float zamu = s_k1 * dtrdz;
+  const bool pos = zamu >= 0.f;
+  const float d = x0 - x1;
+  const float den = copysignf(fmaxf(fabsf(d), (float)kMinden), d);
+  const float r = __fdividef(pos ? x1 - x2 : xm - x0, den);
+  const float bb = fmaxf(__saturatef(2.f * r), fminf(r, 2.f));
+  const float is = pos ? 1.f : -1.f;
+  const float zphi = fmaf(bb, zamu - is, is);
+  return (0.5f * s_k1) * fmaf(-zphi, d, x1 + x0);
+}
 
 // One thread per column and field.  Both passes stream k in registers:
 // pass 1 yields wz1(t) at step t, pass 2 consumes it two levels later, so
@@ -1134,6 +1150,18 @@ __device__ __forceinline__ T waf_hflux(T zamu, T m2, T m1, T x0, T p1) {
   const T bb = superbee(rr);
   const T zphi = (is + zamu * bb) - is * bb;
   return (T(1) + zphi) * m1 + (T(1) - zphi) * x0;
+}
+// FP32 storage: rearranged as waf_vflux<float>
+template <>
+__device__ __forceinline__ float waf_hflux<float>(float zamu, float m2, float m1, float x0, float p1) {
+  const bool pos = zamu > 0.f;
+  const float d = x0 - m1;
+  const float den = copysignf(fmaxf(fabsf(d), (float)kMinden), d);
+  const float r = __fdividef(pos ? m1 - m2 : p1 - x0, den);
+  const float bb = fmaxf(__saturatef(2.f * r), fminf(r, 2.f));
+  const float is = pos ? 1.f : -1.f;
+  const float zphi = fmaf(bb, zamu - is, is);
+  return fmaf(zphi, -d, m1 + x0);
 }
 
 template <class T>
