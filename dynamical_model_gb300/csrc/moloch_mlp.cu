@@ -322,7 +322,7 @@ __device__ __forceinline__ float sur_field(const View<float>& d, int f, int j, i
 }
 
 // Features of ncols columns (cols == nullptr: all columns in order), one
-// block per 128 columns, one thread per column.  Feature index
+// block per 128 columns and 64-feature chunk, one thread per column.  Feature index
 // (f * kz + k) * 9 + nb: field f (u, v, w levels 2..kz+1, pai, tetav), level
 // k, neighbour nb = (di + 1) * 3 + (dj + 1) fastest, so that a 64-feature
 // chunk touches about 7 field planes.  For each chunk a table in shared
@@ -359,7 +359,8 @@ __global__ void __launch_bounds__(128) k_sur_features(View<float> d, const int* 
 #pragma unroll
     for (int nb = 0; nb < 9; ++nb) nbo[nb][t] = jj[nb % 3] + d.nj * ii[nb / 3];
   }
-  for (int f0 = 0; f0 < ldo; f0 += 64) {
+  {
+    const int f0 = blockIdx.y * 64;  // one 64-feature chunk per block
     if (t < 64) {
       const int fe = f0 + t;
       if (fe < nf) {
@@ -855,7 +856,8 @@ int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound) {
   const int n = v.nj * v.ni;
   k_sur_begin<<<1, 1, 0, st>>>(s->ctl, s->judge_every, s->jacc);
   const int* run = s->ctl + CTL_RUN;
-  k_sur_features<true><<<(n + 127) / 128, 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf, s->kin, run);
+  k_sur_features<true><<<dim3((n + 127) / 128, s->kin / 64), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
+                                                                          s->kin, run);
   forward(s, s->Xinf, n, s->Hinf, nullptr, s->Yinf, st, run);
   k_sur_check<<<grid1((size_t)n * s->nop), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold, s->ctl,
                                                           run);
@@ -1002,7 +1004,7 @@ int moloch_sur_collect(moloch_surrogate_t* s, moloch_handle_t* h, int nsteps, in
         SUR_TRY(cudaMemcpyAsync(s->cols, pick.data(), take * sizeof(int), cudaMemcpyHostToDevice, st));
         SUR_TRY(cudaStreamSynchronize(st));
         View<float>& v = *moloch_internal_viewf(h);
-        k_sur_features<false><<<(take + 127) / 128, 128, 0, st>>>(v, s->cols, take, nullptr, nullptr,
+        k_sur_features<false><<<dim3((take + 127) / 128, s->kin / 64), 128, 0, st>>>(v, s->cols, take, nullptr, nullptr,
                                                                    s->Xraw + (size_t)s->npairs * s->kin, s->kin,
                                                                    nullptr);
         k_sur_snapshot<<<take, 128, 0, st>>>(v, s->cols, take, s->snap);
@@ -1282,7 +1284,8 @@ int moloch_sur_profile(moloch_surrogate_t* s, moloch_handle_t* h, double* ms, in
   cudaEvent_t ev[7];
   for (auto& e : ev) SUR_TRY(cudaEventCreate(&e));
   cudaEventRecord(ev[0], st);
-  k_sur_features<true><<<(n + 127) / 128, 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf, s->kin, nullptr);
+  k_sur_features<true><<<dim3((n + 127) / 128, s->kin / 64), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
+                                                                          s->kin, nullptr);
   cudaEventRecord(ev[1], st);
   gemm(s->Xinf, s->kin, s->L[0].Wb, s->kin, nullptr, hid, s->Hinf[0], hid, s->L[0].b, n, hid, s->kin, ACT_SILU, st);
   cudaEventRecord(ev[2], st);
