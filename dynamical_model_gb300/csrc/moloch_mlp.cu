@@ -379,15 +379,19 @@ __global__ void __launch_bounds__(128) k_sur_features(View<float> d, const int* 
     }
     __syncthreads();
     if (cidx < ncols) {
-#pragma unroll 8
+      // all 64 loads of the chunk are issued before any is used (the plane
+      // data comes from HBM: the state is larger than L2)
+      float val[64];
+#pragma unroll
       for (int r = 0; r < 64; ++r) {
         const int nb = tnb[r];
-        float val = 0.f;
-        if (nb >= 0) {
-          val = __ldg(tptr[r] + nbo[nb][t]);
-          if (NORM) val = (val - tsub[r]) * tmul[r];
-        }
-        tile[t][r] = val;
+        val[r] = nb >= 0 ? __ldg(tptr[r] + nbo[nb < 0 ? 0 : nb][t]) : 0.f;
+      }
+#pragma unroll
+      for (int r = 0; r < 64; ++r) {
+        float x = val[r];
+        if (NORM && tnb[r] >= 0) x = (x - tsub[r]) * tmul[r];
+        tile[t][r] = x;
       }
     }
     __syncthreads();
