@@ -452,7 +452,7 @@ __global__ void k_sur_normalize(float* __restrict__ a, int n, int ld, int m, con
     float v = a[q];
     if (c < m) {
       const int s = c / group;
-      v = (v - mean[s]) / stdv[s];
+      v = stdv[s] > 0.f ? (v - mean[s]) / stdv[s] : 0.f;  // zero spread: the output is its mean
     } else {
       v = 0.f;
     }
@@ -1055,7 +1055,10 @@ int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long
     xm[q] = (float)mx;
     xd[q] = (float)(std::sqrt(vx) > 1e-12 * std::max(1.0, std::fabs(mx)) ? std::sqrt(vx) : 1.0);
     ym[q] = (float)my;
-    yd[q] = (float)(std::sqrt(vy) > 1e-30 ? std::sqrt(vy) : 1.0);
+    // an output that never changed in the training set (e.g. tetav at the
+    // levels where the acoustic cycle leaves it alone) gets scale 0: its
+    // prediction is its mean whatever the network says
+    yd[q] = (float)(std::sqrt(vy) > 1e-20 ? std::sqrt(vy) : 0.0);
   }
   SUR_TRY(cudaMemcpy(s->xmean, xm.data(), n5 * 4, cudaMemcpyHostToDevice));
   SUR_TRY(cudaMemcpy(s->xstd, xd.data(), n5 * 4, cudaMemcpyHostToDevice));
@@ -1063,6 +1066,10 @@ int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long
   SUR_TRY(cudaMemcpy(s->ystd, yd.data(), n5 * 4, cudaMemcpyHostToDevice));
   std::vector<float> env(s->nop, 1.f);  // largest |normalised target| per output
   for (int q = 0; q < n5; ++q) {
+    if (!(yd[q] > 0.f)) {  // scale-0 outputs are not checked
+      env[q] = 3.0e38f;
+      continue;
+    }
     double mx = 0.0;
     for (int p = 0; p < n; ++p) mx = std::max(mx, std::fabs((T[(size_t)p * s->nop + q] - ym[q]) / (double)yd[q]));
     env[q] = (float)std::max(mx, 1e-3);
