@@ -304,7 +304,10 @@ def ensemble_members(dm, stream, n=64, seed=2024):
     return out
 
 
-SUR = {"collect_steps": 4, "cols_per_cycle": 2048, "iters": 3000, "lr": 1e-3, "batch": 256,
+# surrogate training: pairs from the first collect_steps steps of a scratch
+# domain of the same workload (another seed), so the training window covers
+# the timed steps
+SUR = {"collect_steps": 16, "cols_per_cycle": 1024, "iters": 4000, "lr": 1e-3, "batch": 256,
        "threshold": 4.0, "judge_every": 6, "tol": 0.3}
 
 
