@@ -330,15 +330,18 @@ def train_surrogate(dm, mode, stream, jx, iy, kz, hills, cfg=SUR):
     return sur, info
 
 
-def surrogate_forced_error(dm, sur, stream, jx, iy, kz, hills, ref_fields, steps):
+def surrogate_forced_error(torch, dm, sur, stream, jx, iy, kz, hills, ref_fields, steps, tuning):
     """The surrogate committed on every cycle (no judge, no envelope check),
     from the same initial state as the FP64 reference: its error after
-    `steps` steps.  Shows what the judge protects against."""
+    `steps` steps and its time per step.  Shows what the judge protects
+    against and what a committed cycle costs."""
     d = dm.Moloch(jx, iy, kz, mode="fp32_mixed", stream=stream)
     d.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED, device=True)
+    d.set_tuning(tuning)
     sur.attach(d, threshold=1e30, judge_every=0)
-    d.run(steps, graph=True)
-    out = {"steps": steps,
+    d.run(2, graph=True)
+    ms, _ = time_steps(torch, d, torch.cuda.ExternalStream(stream), steps - 2)
+    out = {"steps": steps, "ms_per_step": ms / (steps - 2),
            "theta_rmse_K": rmse(d.get("t") / d.get("pai"), ref_fields["theta"]),
            "u_rmse_ms": rmse(d.get("u"), ref_fields["u"]),
            "v_rmse_ms": rmse(d.get("v"), ref_fields["v"])}
@@ -537,7 +540,7 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
     err_mix = errors(dmix)
     judge = sur.stats_counts()
     inference_ms = sur.profile(dsur)
-    forced = surrogate_forced_error(dm, sur, sptr, JX, IY, KZ, HILLS, ref, args.warmup + args.steps)
+    forced = surrogate_forced_error(torch, dm, sur, sptr, JX, IY, KZ, HILLS, ref, args.warmup + args.steps, tune_mix)
     sur.attach(dsur, threshold=SUR["threshold"], judge_every=SUR["judge_every"], tol=SUR["tol"])
 
     # ---- per-kernel CUDA-event profile of one step (roofline) ---------------

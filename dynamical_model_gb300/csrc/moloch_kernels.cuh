@@ -876,6 +876,7 @@ MOLOCH_KM_KERNELS(sound_momentum)
 // k_sound_momentum.
 template <class T>
 __device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx, const int k, const int R) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nj = d.nj, ni = d.ni, pl = d.pl;
   const int nsj = (nj + kMomJ - 1) / kMomJ, nsi = (ni + R - 1) / R;

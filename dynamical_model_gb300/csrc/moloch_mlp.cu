@@ -49,7 +49,8 @@ __device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x));
 __global__ void __launch_bounds__(kThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int boxB,
               float* __restrict__ C, int ldc, __nv_bfloat16* __restrict__ Cb, int ldcb,
-              const float* __restrict__ bias, int M, int N, int K, int act, const int* __restrict__ run) {
+              const float* __restrict__ bias, int M, int N, int K, int act, const int* __restrict__ run,
+              float* __restrict__ Ct, int ldct) {
   if (run && !*run) return;  // device-side skip (a captured step whose surrogate is off)
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full[kStages], empty[kStages], acc_full[2], acc_empty[2], done;
@@ -158,6 +159,10 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
             for (int e = 0; e < 4; ++e) cp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
           }
+          if (Ct) {  // transposed: the 32 lanes of a warp write 32 consecutive rows of C
+#pragma unroll
+            for (int e = 0; e < 16; ++e) Ct[(size_t)(n0 + c + e) * ldct + row] = v[e];
+          }
           if (Cb) {
             uint32_t pk[8];
 #pragma unroll
@@ -248,8 +253,8 @@ static void gemm_attr() {
 // checks shapes, builds the two maps and launches; MOLOCH_OK or an error code
 static int launch_gemm(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
                        const float* bias, int M, int N, int K, int act, cudaStream_t st,
-                       const int* run = nullptr) {
-  if (!A || !B || (!C && !Cb) || M <= 0 || N <= 0 || K <= 0) {
+                       const int* run = nullptr, float* Ct = nullptr, int ldct = 0) {
+  if (!A || !B || (!C && !Cb && !Ct) || M <= 0 || N <= 0 || K <= 0 || (Ct && ldct < M)) {
     moloch_internal_set_error("tc_gemm: bad arguments");
     return MOLOCH_ERR_ARG;
   }
@@ -268,7 +273,7 @@ static int launch_gemm(const void* A, int lda, const void* B, int ldb, float* C,
   }
   const int ntiles = ((M + kTileM - 1) / kTileM) * ((N + kTileN - 1) / kTileN);
   k_gemm_tc<<<std::min(ntiles, num_sms()), kThreads, kSmem, st>>>(ta, tb, boxB, C, ldc, (__nv_bfloat16*)Cb, ldcb,
-                                                                   bias, M, N, K, act, run);
+                                                                   bias, M, N, K, act, run, Ct, ldct);
   return MOLOCH_OK;
 }
 
@@ -577,21 +582,22 @@ __global__ void k_sur_begin(int* __restrict__ ctl, int judge_every, double* __re
 
 // every increment finite and within threshold x the envelope of the
 // training targets (per output, normalised units); tracks the largest ratio
+// (Y output-major: [outputs][n]; grid.y = output, grid.x strides over columns)
 __global__ void k_sur_check(const float* __restrict__ Y, int n, int ld, int m, const float* __restrict__ env,
                             float threshold, int* __restrict__ ctl, const int* __restrict__ run) {
   if (run && !*run) return;
-  const size_t tot = (size_t)n * ld;
+  const int o = blockIdx.y;
+  const float lim = threshold * env[o];
+  const float rcp_env = 1.0f / env[o];
+  const float* __restrict__ yo = Y + (size_t)o * n;
   int b = 0;
   float rmax = 0.f;
-  for (size_t q = blockIdx.x * (size_t)blockDim.x + threadIdx.x; q < tot; q += (size_t)gridDim.x * blockDim.x) {
-    const int c = (int)(q % ld);
-    if (c < m) {
-      const float r = fabsf(Y[q]) / env[c];
-      if (!(r <= threshold)) b = 1;  // also catches NaN
-      rmax = r == r ? fmaxf(rmax, r) : __int_as_float(0x7f800000);
-    }
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
+    const float y = fabsf(yo[c]);
+    if (!(y <= lim)) b = 1;  // also catches NaN
+    rmax = y == y ? fmaxf(rmax, y * rcp_env) : __int_as_float(0x7f800000);
   }
-  for (int o = 16; o > 0; o >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+  for (int q = 16; q > 0; q >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, q));
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(&ctl[CTL_BAD], 1);
   if ((threadIdx.x & 31) == 0) atomicMax(&ctl[CTL_MAXRATIO], __float_as_int(rmax));
 }
@@ -634,7 +640,7 @@ __global__ void __launch_bounds__(256) k_sur_judge(View<float> d, const int* __r
     for (int f = 0; f < 5; ++f) {
       const int o = f * d.kz + k;
       const float act = post[f][q] - snap[(size_t)f * n + q];
-      const float pred = Y[c * ld + o] * ystd[o] + ymean[o];
+      const float pred = Y[(size_t)o * ld + c] * ystd[o] + ymean[o];  // output-major
       const float e = pred - act;
       acc[2 * f] += (double)e * e;
       acc[2 * f + 1] += (double)act * act;
@@ -701,7 +707,8 @@ __global__ void __launch_bounds__(256) k_sur_vvel(View<float> d, const float* __
   const float* __restrict__ u = d.ubuf[d.cur];
   const float* __restrict__ v = d.vbuf[d.cur];
   const float fr = (float)(nsound - 1) / (float)nsound;
-  auto inc = [&](size_t col, int f, int k) { const int q = f * kz + k; return Y[col * ld + q] * ystd[q] + ymean[q]; };
+  // Y output-major: output q of column col at Y[q * ld + col] (ld = columns)
+  auto inc = [&](size_t col, int f, int k) { const int q = f * kz + k; return Y[(size_t)q * ld + col] * ystd[q] + ymean[q]; };
   auto ul = [&](size_t col, int k) { return u[col + k * pl] + fr * inc(col, 0, k); };
   auto vl = [&](size_t col, int k) { return v[col + k * pl] + fr * inc(col, 1, k); };
   const float hx0 = d.hx[c], hx1 = d.hx[ce], hy0 = d.hy[c], hy1 = d.hy[cn];
@@ -728,12 +735,12 @@ __global__ void __launch_bounds__(256) k_sur_apply(View<float> d, const float* _
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl, c = jj + (size_t)nj * ii;
-  const float* __restrict__ yr = Y + c * ld;
+  const float* __restrict__ yr = Y + c;  // output-major: output q at yr[q * ld]
   const float* u = d.ubuf[d.cur];
   const float* v = d.vbuf[d.cur];
   float* uo = d.ubuf[d.cur ^ (nsound & 1)];
   float* vo = d.vbuf[d.cur ^ (nsound & 1)];
-  auto inc = [&](int f, int k) { const int q = f * kz + k; return yr[q] * ystd[q] + ymean[q]; };
+  auto inc = [&](int f, int k) { const int q = f * kz + k; return yr[(size_t)q * ld] * ystd[q] + ymean[q]; };
   for (int k = 0; k < kz; ++k) {
     const size_t q = c + (size_t)k * pl;
     uo[q] = u[q] + inc(0, k);
@@ -787,8 +794,9 @@ static double u01h(uint64_t& st) { return (double)(sm64(st) >> 11) * (1.0 / 9007
   } while (0)
 
 static int gemm(const void* A, int lda, const void* B, int ldb, float* C, int ldc, void* Cb, int ldcb,
-                const float* bias, int M, int N, int K, int act, cudaStream_t st, const int* run = nullptr) {
-  launch_gemm(A, lda, B, ldb, C, ldc, Cb, ldcb, bias, M, N, K, act, st, run);
+                const float* bias, int M, int N, int K, int act, cudaStream_t st, const int* run = nullptr,
+                float* Ct = nullptr, int ldct = 0) {
+  launch_gemm(A, lda, B, ldb, C, ldc, Cb, ldcb, bias, M, N, K, act, st, run, Ct, ldct);
   return 1;
 }
 
@@ -802,13 +810,14 @@ static int transpose(const void* in, int rows, int cols, int ld_in, void* out, i
 }
 
 // forward of n rows: X -> H[0..2] (BF16, SiLU) -> Y (FP32); Z (pre-activations) optional
+// Y [n][nop] row-major, or (Y == nullptr) Yt [nop][n] output-major
 static int forward(Surrogate* s, const void* X, int n, void* const* H, float* const* Z, float* Y, cudaStream_t st,
-                   const int* run = nullptr) {
+                   const int* run = nullptr, float* Yt = nullptr) {
   const int hid = s->hid;
   gemm(X, s->kin, s->L[0].Wb, s->kin, Z ? Z[0] : nullptr, hid, H[0], hid, s->L[0].b, n, hid, s->kin, ACT_SILU, st, run);
   gemm(H[0], hid, s->L[1].Wb, hid, Z ? Z[1] : nullptr, hid, H[1], hid, s->L[1].b, n, hid, hid, ACT_SILU, st, run);
   gemm(H[1], hid, s->L[2].Wb, hid, Z ? Z[2] : nullptr, hid, H[2], hid, s->L[2].b, n, hid, hid, ACT_SILU, st, run);
-  gemm(H[2], hid, s->L[3].Wb, hid, Y, s->nop, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st, run);
+  gemm(H[2], hid, s->L[3].Wb, hid, Y, s->nop, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st, run, Yt, n);
   return 4;
 }
 
@@ -862,20 +871,20 @@ int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound) {
   const int* run = s->ctl + CTL_RUN;
   k_sur_features<true><<<dim3((n + 127) / 128, s->kin / 64), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
                                                                           s->kin, run);
-  forward(s, s->Xinf, n, s->Hinf, nullptr, s->Yinf, st, run);
-  k_sur_check<<<grid1((size_t)n * s->nop), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold, s->ctl,
-                                                          run);
+  forward(s, s->Xinf, n, s->Hinf, nullptr, nullptr, st, run, s->Yinf);  // Yinf output-major
+  k_sur_check<<<dim3((n + 2047) / 2048, s->nout), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
+                                                                 s->ctl, run);
   k_sur_decide<<<1, 1, 0, st>>>(s->ctl, s->counts);
   k_sur_judge_snapshot<<<grid1((size_t)5 * n * v.kz), 256, 0, st>>>(v, s->ctl, s->jsnap);
   const dim3 cg((v.nj + 31) / 32, (v.ni + 7) / 8);
-  k_sur_vvel<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, s->nop, s->ymean, s->ystd, s->ctl, nsound);
-  k_sur_apply<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, s->nop, s->ymean, s->ystd, s->ctl, nsound);
+  k_sur_vvel<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, n, s->ymean, s->ystd, s->ctl, nsound);
+  k_sur_apply<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, n, s->ymean, s->ystd, s->ctl, nsound);
   return 11;
 }
 
 int sur_after(Surrogate* s, View<float>& v, cudaStream_t st) {
   const size_t n = (size_t)v.nj * v.ni * v.kz;
-  k_sur_judge<<<grid1(n), 256, 0, st>>>(v, s->ctl, s->jsnap, s->Yinf, s->nop, s->ymean, s->ystd, s->jacc);
+  k_sur_judge<<<grid1(n), 256, 0, st>>>(v, s->ctl, s->jsnap, s->Yinf, v.nj * v.ni, s->ymean, s->ystd, s->jacc);
   k_sur_verdict<<<1, 1, 0, st>>>(s->ctl, s->jacc, s->tol, s->judge_every, s->max_interval, s->counts);
   return 2;
 }
@@ -1304,13 +1313,14 @@ int moloch_sur_profile(moloch_surrogate_t* s, moloch_handle_t* h, double* ms, in
   cudaEventRecord(ev[3], st);
   gemm(s->Hinf[1], hid, s->L[2].Wb, hid, nullptr, hid, s->Hinf[2], hid, s->L[2].b, n, hid, hid, ACT_SILU, st);
   cudaEventRecord(ev[4], st);
-  gemm(s->Hinf[2], hid, s->L[3].Wb, hid, s->Yinf, s->nop, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st);
+  gemm(s->Hinf[2], hid, s->L[3].Wb, hid, nullptr, 0, nullptr, 0, s->L[3].b, n, s->nop, hid, ACT_NONE, st, nullptr,
+       s->Yinf, n);
   cudaEventRecord(ev[5], st);
   // the check writes slots CTL_BAD and CTL_MAXRATIO of the block it is
   // given: point it at the unused upper half of the control block
   static_assert(16 + CTL_MAXRATIO < CTL_COUNT, "control block too small");
-  k_sur_check<<<grid1((size_t)n * s->nop), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
-                                                          s->ctl + 16, nullptr);
+  k_sur_check<<<dim3((n + 2047) / 2048, s->nout), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
+                                                                 s->ctl + 16, nullptr);
   cudaEventRecord(ev[6], st);
   SUR_TRY(cudaEventSynchronize(ev[6]));
   SUR_TRY(cudaGetLastError());

@@ -63,11 +63,15 @@ def _state(g):
     return {f: g.get(f) for f in STATE}
 
 
-@pytest.mark.parametrize("jx,iy,kz", [(24, 20, 8), (37, 29, 12)])
-def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz):
+@pytest.mark.parametrize("jx,iy,kz,tuning", [(24, 20, 8, [1, 0]), (37, 29, 12, [1, 0]), (37, 29, 12, [32, 11]),
+                                             (24, 20, 8, [16, 7])])
+def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz, tuning):
+    """tuning: the plain kernel variants that must all stand aside on a
+    committed cycle (one level per thread, strips, k-marching)."""
     from oracle import mlp_oracle as mo
     g = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     g.setup_idealized(hills=((400.0, jx / 2, iy / 2, 3.0),), u0=5.0, v0=-3.0)
+    g.set_tuning(tuning)
     g.phase(0)
     pre = _state(g)
     sur = gpu_lib.Surrogate(kz, capacity=256, batch=128, seed=5)
