@@ -93,8 +93,8 @@ class ClockSampler:
 
     def start(self):
         try:
-            self.out = open(os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv"), "w") \
-                if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else None
+            path = os.environ.get("MOLOCH_CLOCKS_CSV")  # optional copy of the raw samples
+            self.out = open(path, "w") if path else None
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
