@@ -64,10 +64,10 @@ ALG_WORDS = {
 # from an ncu capture of the kernel, and the grid points of that capture;
 # scaled by the point count to the benchmarked size (traffic grows in
 # proportion: one pass over each array per launch)
-NCU_TRAFFIC = {"k_sound_column": (338.1e6, 256 * 256 * 60)}
+NCU_TRAFFIC = {"k_sound_column": (842.8e6, 384 * 384 * 60)}
 # sm__pipe_fp64_cycles_active (% of peak, active) from the same capture
-NCU_FP64_PIPE = {"k_sound_column": {"pipe_fp64_active_pct": 48.9, "capture": "256x256x60",
-                                    "fp64_pipe_instructions_per_level": 10}}
+NCU_FP64_PIPE = {"k_sound_column": {"pipe_fp64_active_pct": 35.7, "capture": "384x384x60",
+                                    "fp64_operations_per_level": 4}}
 # whole-step algorithmic words per grid point of the fused design target
 # (pre-diag 11 + 3 sound cycles x 91 + 3 advection steps x 23 + post-diag 11)
 B_ALG_WORDS = 364
@@ -561,10 +561,10 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
                 "traffic": (NCU_TRAFFIC[tname][0] * gp / NCU_TRAFFIC[tname][1]) if tname in NCU_TRAFFIC else None,
-                "traffic_note": "ncu dram bytes of one launch at 256x256x60, scaled by grid points",
-                # second roof of the top kernel: its FP64 pivot recurrence (10
-                # FP64-pipe instructions per level) keeps the FP64 pipe this
-                # busy in the ncu capture of the same kernel
+                "traffic_note": "ncu dram bytes of one launch at 384x384x60, scaled by grid points",
+                # second roof of the top kernel: its FP64 pivot recurrence (4
+                # FP64 operations per level) keeps the FP64 pipe this busy in
+                # the ncu capture of the same kernel
                 "fp64_pipe": NCU_FP64_PIPE.get(tname),
                 "step_alg_GBps": B_ALG_WORDS * esz * value_mix / n_dom / 1e9}
     kernels = {k: {"ms": round(v[0], 4), "launches": v[1],

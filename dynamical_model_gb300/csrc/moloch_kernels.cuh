@@ -275,19 +275,31 @@ __global__ void __launch_bounds__(kPtBX* kPtBY)
 }
 
 
-// Reciprocal of a Thomas pivot.  FP64 build: the IEEE quotient, as the
-// reference.  FP32-storage build: an FP32 estimate refined by one FP64
-// Newton step (relative error ~1e-14) -- the pivot stays FP64 while the
-// FP64 pipe, 1/64 of the FP32 rate on GB300, does 2 FMAs instead of a
-// full division.
-template <class T> __device__ __forceinline__ double pivot_rcp(double den);
-template <> __device__ __forceinline__ double pivot_rcp<double>(double den) { return 1.0 / den; }
-template <> __device__ __forceinline__ double pivot_rcp<float>(double den) {
-  float x = (float)den, r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-  double r0 = (double)r;
-  double e = fma(-den, r0, 1.0);
-  return fma(r0, e, r0);
+// Exact FP32 -> FP64 widening on the integer pipe.  GB300 executes F2F
+// conversions on its FP64 pipe (1/64 of the FP32 rate); these few integer
+// operations do not touch it.  Zeros, normal values of either sign,
+// infinities and NaNs convert exactly; FP32 subnormals become zero of the
+// same sign.
+__device__ __forceinline__ double widen_f32(float x) {
+  const unsigned b = __float_as_uint(x);
+  const unsigned ex = b & 0x7f800000u, sg = b & 0x80000000u;
+  unsigned hi = (((b & 0x7fffffffu) >> 3) + 0x38000000u) | sg;  // exponent rebiased by 1023 - 127
+  unsigned lo = b << 29;
+  if (ex == 0u) { hi = sg; lo = 0u; }
+  if (ex == 0x7f800000u) hi |= 0x7ff00000u;
+  return __hiloint2double((int)hi, (int)lo);
+}
+
+// FP64 -> FP32 by truncation on the integer pipe: sign and exponent exact,
+// mantissa cut to 23 bits (relative error < 2^-23).  Magnitudes below the
+// FP32 normal range become zero, above it infinity; NaNs stay NaN.
+__device__ __forceinline__ float narrow_trunc(double x) {
+  const unsigned hi = (unsigned)__double2hiint(x), lo = (unsigned)__double2loint(x);
+  const unsigned ax = hi & 0x7fffffffu;
+  unsigned m = (__funnelshift_l(lo, hi, 3) - (896u << 23)) & 0x7fffffffu;  // exponent rebiased by 127 - 1023
+  if (ax < 0x38100000u) m = 0u;
+  if (ax >= 0x47f00000u) m = (ax > 0x7ff00000u || (ax == 0x7ff00000u && lo != 0u)) ? 0x7fc00000u : 0x7f800000u;
+  return __uint_as_float(m | (hi & 0x80000000u));
 }
 
 // ---- sound: implicit w (Thomas, :634-686) + Exner/theta (:690-728) -----
@@ -295,7 +307,13 @@ template <> __device__ __forceinline__ double pivot_rcp<float>(double den) {
 // mode, stash of the FP64 down-sweep values, then back-substitution fused
 // with the Exner/theta/pai update of the level above it.
 // defer_pai: leave zdiv2b final and pai to k_pai_update (divergence filter on).
-template <class T>
+// PD: levels loaded ahead of the level computed, in both sweeps (a register
+// ring of PD level records).  The kernels use PD = 1: 64 registers (FP32),
+// 8 blocks per SM, no spills.  A ring of 3 levels at 4 blocks per SM (so
+// that the back-substitution finds more of the down-sweep's levels in L2)
+// measured 13 % slower at 512 x 512 x 60: fewer columns in flight cost more
+// bandwidth than the extra L2 hits saved.
+template <class T, int PD>
 __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, const int by, const int bz, int nsound, int last, int defer_pai) {
   if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int jj = bx * kColBX + threadIdx.x;
@@ -337,22 +355,33 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
   ST* __restrict__ WWs = reinterpret_cast<ST*>(d.wwkw) + c;
   const T wsurf = W[(size_t)kz * pl];  // w(kz+1) from k_sound_div
   ST wkp1 = (ST)wsurf;
-  double wwp1 = 0.0;  // wwkw(kz+1) = 0
+  double wwp1 = 0.0;  // wwkw(kz+1) = 0 (FP64 storage)
+  double cwp1 = 1.0;  // 1 - wwkw(kz+1) (FP32 storage)
+  // level kk of the down-sweep reads w, fmzf, qv, ffilt at kk and tetav,
+  // pai, qsat, zdiv2b, fmz, t at kk-1 (carried as the next level's kk values)
+  struct Dn { T wk, fz, qv, ff, tkm, pkm, qskm, zdkm, fkm, tm; };
+  auto load_dn = [&](int kk, Dn& x) {
+    const size_t on = (size_t)kk * pl, onm = on - pl;
+    x.wk = W[on]; x.fz = FMZF[on]; x.qv = QV[on]; x.ff = FF[kk];
+    x.tkm = TET[onm]; x.pkm = PAI[onm]; x.qskm = QSAT[onm]; x.zdkm = ZD[onm];
+    x.fkm = FMZ[onm]; x.tm = TT[onm];
+  };
   size_t o = (size_t)(kz - 1) * pl;
   T zd_k = ZD[o], tk = TET[o], pk = PAI[o], fk = FMZ[o], qsk = QSAT[o];
-  T n_wk = W[o], n_fz = FMZF[o], n_qv = QV[o], n_ff = FF[kz - 1];
-  T n_tkm = TET[o - pl], n_pkm = PAI[o - pl], n_qskm = QSAT[o - pl], n_zdkm = ZD[o - pl];
-  T n_fkm = FMZ[o - pl], n_tm = TT[o - pl];
-  for (int kk = kz - 1; kk >= 1; --kk) {
+  Dn dring[PD];
+#pragma unroll
+  for (int u = 0; u < PD; ++u)
+    if (kz - 1 - u >= 1) load_dn(kz - 1 - u, dring[u]);
+  for (int base = kz - 1; base >= 1; base -= PD) {
+#pragma unroll
+  for (int u = 0; u < PD; ++u) {
+    const int kk = base - u;
+    if (kk < 1) break;
     o = (size_t)kk * pl;
-    const T wk = n_wk, fz = n_fz, qvk = n_qv, ff = n_ff, tkm = n_tkm, pkm = n_pkm;
-    const T qskm = n_qskm, zd_km = n_zdkm, fkm = n_fkm, tm = n_tm;
-    if (kk > 1) {
-      const size_t on = o - pl, onm = on - pl;
-      n_wk = W[on]; n_fz = FMZF[on]; n_qv = QV[on]; n_ff = FF[kk - 1];
-      n_tkm = TET[onm]; n_pkm = PAI[onm]; n_qskm = QSAT[onm]; n_zdkm = ZD[onm];
-      n_fkm = FMZ[onm]; n_tm = TT[onm];
-    }
+    const Dn cur = dring[u];
+    if (kk - PD >= 1) load_dn(kk - PD, dring[u]);
+    const T wk = cur.wk, fz = cur.fz, qvk = cur.qv, ff = cur.ff, tkm = cur.tkm, pkm = cur.pkm;
+    const T qskm = cur.qskm, zd_km = cur.zdkm, fkm = cur.fkm, tm = cur.tm;
     T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
     zrom1w = zrom1w - (((((T(kCpd) * wk) * fz) * fz) * ns) * dtrdz) * (tkm - tk);
     if (qvk > T(0.96) * qsk && wk > T(0.1)) {
@@ -365,25 +394,34 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * (pkm * zd_km - pk * zd_k);
     const T zu_t = ((zcs2 * fkm) * zrom1w) * pkm + ff;
     const T zd_t = ((zcs2 * fk) * zrom1w) * pk + ff;
-    const double zu = (double)zu_t;
-    const double zdd = (double)zd_t;
-    const double den = ((1.0 + zdd) + zu) - zdd * wwp1;
     ST wpk;
     double wwk;
     if constexpr (kF32) {
-      // FP32 estimate r of 1/den, one FP64 Newton step for the pivot
-      // (relative error ~1e-14); the FP32 right-hand side and the stash use
-      // r itself, so no FP64 result has to be converted back (the FP64
-      // pipe is 1/64 of the FP32 rate on GB300 and converts count there)
+      // The pivot recurrence in FP64, written for the complement
+      // c = 1 - wwkw: den = (1 + zd c(k+1)) + zu, c(k) = (1 + zd c(k+1)) / den
+      // -- the reference's den = ((1 + zd) + zu) - zd wwkw(k+1) and
+      // wwkw(k) = zu / den without the cancellation of zd against
+      // zd wwkw(k+1).  Four FP64 operations a level: the quotient starts
+      // from the FP32 estimate q0 = tt r (r the FP32 estimate of 1/den) and
+      // takes one correction, r times the FP64 residual tt - den q0
+      // (relative error ~2e-13); the widenings and narrowings run on the
+      // integer pipe.  The FP32 right-hand side and the stash use r itself.
+      const double zu = widen_f32(zu_t), zdd = widen_f32(zd_t);
+      const double tt = fma(zdd, cwp1, 1.0);
+      const double den = tt + zu;
       float r;
-      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"((float)den));
-      const double r0 = (double)r;
-      const double zrapp = fma(r0, fma(-den, r0, 1.0), r0);
-      wwk = zrapp * zu;
+      asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(narrow_trunc(den)));
+      const double q0 = widen_f32(narrow_trunc(tt) * r);
+      const double rem = fma(-den, q0, tt);
+      cwp1 = q0 + widen_f32(r * narrow_trunc(rem));
+      wwk = 0.0;
       wpk = r * (zwexpl + zd_t * wkp1);
       WWs[o] = r * zu_t;
     } else {
-      const double zrapp = pivot_rcp<T>(den);
+      const double zu = (double)zu_t;
+      const double zdd = (double)zd_t;
+      const double den = ((1.0 + zdd) + zu) - zdd * wwp1;
+      const double zrapp = 1.0 / den;
       wwk = zrapp * zu;
       wpk = zrapp * ((double)zwexpl + zdd * wkp1);
       WWs[o] = (ST)wwk;
@@ -392,10 +430,11 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     wkp1 = wpk; wwp1 = wwk;
     zd_k = zd_km; tk = tkm; pk = pkm; fk = fkm; qsk = qskm;
   }
+  }
 
   // (c) back-substitution (:681-686) fused with the Exner/theta update of
   // the level above (:690-728); w(1) = 0 always (init_moloch :260-262).
-  // Level kk is solved while level kk-1 is finalized; loads run one ahead.
+  // Level kk is solved while level kk-1 is finalized; loads run PD ahead.
   const T rdrcv = T(kRdrcv);
   ST wlo_d = 0;
   T wlo = T(0);
@@ -425,32 +464,46 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     }
     if (last) S[q] = m == 0 ? T(0) : (wl + f.s) * f.fmzf;  // complete Equation 10 (:843-849)
   };
-  Fin fin = load_fin(0);
-  ST n_wp = WPs[pl], n_ww = WWs[pl];
-  T n_wold = W[pl];
-  for (int kk = 1; kk < kz; ++kk) {
-    const size_t q = (size_t)kk * pl;
-    const ST wpk = n_wp, wwk = n_ww;
-    const T wold = n_wold;
-    const Fin cur = fin;
-    fin = load_fin(kk);  // level kk is finalized in the next iteration
-    if (kk + 1 < kz) {
-      n_wp = WPs[q + pl]; n_ww = WWs[q + pl]; n_wold = W[q + pl];
+  // record m = 1 .. kz: the stash and old w of level m (m < kz) and the
+  // finalize inputs of level m-1
+  struct Bk { ST wp, ww; T wold; Fin f; };
+  auto load_bk = [&](int m, Bk& x) {
+    x.f = load_fin(m - 1);
+    if (m < kz) {
+      const size_t q = (size_t)m * pl;
+      x.wp = WPs[q]; x.ww = WWs[q]; x.wold = W[q];
     }
-    wlo_d = wpk + wwk * wlo_d;
-    const T wn = (T)wlo_d;
-    DW[q] = (-wold) + wn;
-    W[q] = wn;
-    finalize(kk - 1, cur, wlo, wn);
-    wlo = wn;
+  };
+  Bk bring[PD];
+#pragma unroll
+  for (int u = 0; u < PD; ++u)
+    if (1 + u <= kz) load_bk(1 + u, bring[u]);
+  for (int base = 1; base <= kz; base += PD) {
+#pragma unroll
+  for (int u = 0; u < PD; ++u) {
+    const int kk = base + u;
+    if (kk > kz) break;
+    const Bk cur = bring[u];
+    if (kk + PD <= kz) load_bk(kk + PD, bring[u]);
+    if (kk < kz) {
+      const size_t q = (size_t)kk * pl;
+      wlo_d = cur.wp + cur.ww * wlo_d;
+      const T wn = (T)wlo_d;
+      DW[q] = (-cur.wold) + wn;
+      W[q] = wn;
+      finalize(kk - 1, cur.f, wlo, wn);
+      wlo = wn;
+    } else {
+      finalize(kz - 1, cur.f, wlo, wsurf);
+    }
   }
-  finalize(kz - 1, fin, wlo, wsurf);
+  }
   if (last) S[(size_t)kz * pl] = T(0);
 }
 
 template <class T>
 __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4) k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
-  b_sound_column<T>(d, blockIdx.x, blockIdx.y, blockIdx.z, nsound, last, defer_pai);
+  b_sound_column<T, 1>(d, blockIdx.x, blockIdx.y, blockIdx.z, nsound, last, defer_pai);
 }
 
 template <class T>
@@ -460,8 +513,9 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
   const int4 t = tiles[blockIdx.x];
   copy_view(&sv, views + t.x);
   __syncthreads();
-  b_sound_column<T>(sv, t.y, t.z, t.w, nsound, last, defer_pai);
+  b_sound_column<T, 1>(sv, t.y, t.z, t.w, nsound, last, defer_pai);
 }
+
 
 
 // ---- 5-point Laplacian filter of one field, out of place ----------------

@@ -99,6 +99,19 @@ def test_options(oracle_mod, gpu_lib, opts):
     compare(o, g, PROG + DIAG, 1e-12)
 
 
+@pytest.mark.parametrize("variant", [7, 11])
+def test_divfilter_with_sound_variants(oracle_mod, gpu_lib, variant):
+    """The divergence filter path (the column kernel leaves zdiv2b and pai to
+    the filter kernels) with the k-marching and warp-strip sound kernels,
+    against the oracle."""
+    o, g = pair(oracle_mod, gpu_lib, 19, 16, 10, hills=((300.0, 9.0, 8.0, 3.0),), divfilter=True)
+    g.set_tuning([1, variant])
+    for s in range(1, 4):
+        o.step(s)
+        g.moloch(s)
+    compare(o, g, PROG + DIAG, 1e-12)
+
+
 def test_hill_and_wind(oracle_mod, gpu_lib):
     """Gaussian hill (500 m, radius 20 gp as in the 512 x 512 x 60 workload,
     scaled to the grid) and a 7 m/s background wind."""
