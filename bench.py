@@ -52,6 +52,7 @@ ALG_WORDS = {
     "k_prediag": 13,          # r: pai t q(5) | w: p qsat tvirt qwltot qwitot tetav
     "k_sound_div": 7,         # r: u v fmz rfw rfs | w: s zdiv2a
     "k_sound_damp": 8,        # r: zdiv2a u v fmz s | w: u v zdiv2b
+    "k_sound_divdamp": 9,     # r: u v fmz rfw rfs | w: u v s zdiv2b (fused div + damp)
     "k_sound_column": 16,     # r: w fmzf qv tetav pai qsat t zdiv2b fmz qc qwltot qwitot | w: w deltaw tetav pai
     "k_sound_momentum": 7,    # r: u v deltaw tetav pai | w: u v
     "k_stag_to_x": 6,         # r: u v w | w: ux vx wx

@@ -580,7 +580,10 @@ int launch_phase(moloch_handle* h, View<T>& v, int phase) {
   }
   if constexpr (sizeof(T) == sizeof(float)) {
     if (phase == 1 && h->sur) {
-      n = moloch::mlp::sur_cycle(h->sur, v, h->stream, fl.nsound);
+      // parity of the u/v buffer flips of the plain loop, which a committed
+      // cycle's u, v must land on
+      const int flips = fl.nsound * ((v.kmarch & 16) ? 2 : 1);
+      n = moloch::mlp::sur_cycle(h->sur, v, h->stream, fl.nsound, flips & 1);
       n += kfast::launch_sound<T>(v, h->stream, fl);
       return n + moloch::mlp::sur_after(h->sur, v, h->stream);
     }
@@ -1064,7 +1067,7 @@ long long moloch_gpu_kernel_count(moloch_handle_t* h) { return h ? h->kernels : 
 static const char* const kKindNames[KK_COUNT] = {
     "k_prediag", "k_sound_div", "k_sound_damp", "k_sound_column", "k_lap_filter", "k_pai_update",
     "k_sound_momentum", "k_stag_to_x", "k_waf_vertical", "k_waf_horizontal", "k_stag_from_x",
-    "k_filter_increment", "k_postdiag", "k_diag"};
+    "k_filter_increment", "k_postdiag", "k_diag", "k_sound_divdamp"};
 
 int moloch_gpu_kernel_kinds(void) { return KK_COUNT; }
 
@@ -1112,7 +1115,8 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 // rows per warp strip
 static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
 // [0] horizontal WAF shape, [1] sound kernel variants (bit mask:
-// 1 divergence, 2 damping, 4 momentum k-marching; 8 momentum warp strips)
+// 1 divergence, 2 damping, 4 momentum k-marching; 8 momentum warp strips;
+// 16 divergence and damping fused in warp strips, which overrides 1 and 2)
 static const int kTuneCount = 2;
 
 int moloch_gpu_tuning_count(void) { return kTuneCount; }
@@ -1126,7 +1130,7 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     h->vf.hz_levels = choice[0];
   }
   if (n > 1) {
-    if (choice[1] < 0 || choice[1] > 15) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 31) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     h->vd.kmarch = choice[1];
     h->vf.kmarch = choice[1];
   }
@@ -1174,8 +1178,9 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   // three), timed on sound()
   double best1 = 1e30;
   int pick1 = h->elem == 8 ? h->vd.kmarch : h->vf.kmarch;
-  for (int cand = 0; cand < 16; ++cand) {
+  for (int cand = 0; cand < 32; ++cand) {
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
+    if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both
     h->vd.kmarch = cand;
     h->vf.kmarch = cand;
     float ms = 0.f, tot = 0.f;
@@ -1257,6 +1262,9 @@ void ens_tiles(moloch_ensemble* e) {
       const int nstrips = ((nj + kMomJ - 1) / kMomJ) * ((ni + kMomR - 1) / kMomR);
       for (int z = 0; z < kz; ++z)
         for (int x = 0; x < (nstrips + 3) / 4; ++x) e->tiles[TK_MSTRIP].push_back(make_int4(q, x, z, 0));
+      const int ndstrips = ((nj + kDDJ - 1) / kDDJ) * ((ni + kDDR - 1) / kDDR);
+      for (int z = 0; z < kz; ++z)
+        for (int x = 0; x < (ndstrips + 3) / 4; ++x) e->tiles[TK_DSTRIP].push_back(make_int4(q, x, z, 0));
     }
     if (e->hz_levels >= 16) {  // warp strips: 4 strips of hz_levels rows per block, every level
       const int nstrips = ((nj + 27) / 28) * ((ni + e->hz_levels - 1) / e->hz_levels);
@@ -1434,8 +1442,9 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   const PhaseFlags fl = flags_of(e->m[0]);
   double best1 = 1e30;
   int pick1 = e->kmarch;
-  for (int cand = 0; cand < 16; ++cand) {
+  for (int cand = 0; cand < 32; ++cand) {
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
+    if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both
     e->kmarch = cand;
     int rc = ens_build(e);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
@@ -1472,7 +1481,7 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
     e->hz_levels = choice[0];
   }
   if (nchoice > 1) {
-    if (choice[1] < 0 || choice[1] > 15) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 31) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     e->kmarch = choice[1];
   }
   return ens_build(e);

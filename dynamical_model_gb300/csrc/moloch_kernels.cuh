@@ -1032,6 +1032,180 @@ __global__ void __launch_bounds__(128)
   b_momentum_strip<T>(sv, t.y, t.z, R);
 }
 
+// ---- divergence + divdamp as warp strips (:514-597, :853-895, :627-630) ---
+// The work of k_sound_div and k_sound_damp in one pass.  One warp per strip
+// of kDDJ output columns x R rows of one level k, lanes on columns
+// j0-1 .. j0+30.  For each row the lane's point gets s(k) and s(k+1)
+// (Equation 10, or the surface values when k is the lowest level) and the
+// horizontal divergence zdiv2a (Equation 16) from the pre-damping u, v of
+// the current buffer: east neighbours from the lane beside (shuffles),
+// north neighbours from the next row, whose v-part is loaded two rows
+// ahead.  The damping of row i then takes zdiv2a of the lanes beside and of
+// rows i-1, i+1 from registers.  Damped u, v go to the other buffer
+// (ubuf[cur^1]) -- the caller flips cur -- so no strip ever reads a value
+// another strip has damped; zdiv2a never goes to memory.  The boundary
+// lanes and rows store the pre-damping edge values the momentum step reads
+// as the stale ud/vd halo (:730-735), as k_sound_div does.
+template <class T>
+__device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, const int k, const int R) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int nj = d.nj, ni = d.ni, kz = d.kz;
+  const size_t pl = d.pl;
+  const int nsj = (nj + kDDJ - 1) / kDDJ, nsi = (ni + R - 1) / R;
+  const int w = bx * (blockDim.x >> 5) + wid;
+  if (w >= nsj * nsi) return;  // whole warp
+  const int sj = w % nsj, si = w / nsj;
+  const int jl = sj * kDDJ - 1 + lane;
+  const int jj = wrapn(jl, nj);
+  const bool out_lane = lane >= 1 && lane <= kDDJ && jl < nj;
+  const int i_s = si * R, i_e = min(i_s + R, ni);
+  const size_t o = (size_t)k * pl;
+  const bool has_up = k > 0, has_dn = k < kz - 1;  // levels k-1 and k+1 exist
+  const T* __restrict__ u = d.ubuf[d.cur] + o;
+  const T* __restrict__ v = d.vbuf[d.cur] + o;
+  T* __restrict__ uo = d.ubuf[d.cur ^ 1] + o;
+  T* __restrict__ vo = d.vbuf[d.cur ^ 1] + o;
+  const T* __restrict__ rfw = d.rfw + o;
+  const T* __restrict__ rfs = d.rfs + o;
+  const T* __restrict__ fmz = d.fmz + o;
+  const bool rot = d.rotllr;
+  const T dtrdx = d.dtrdx, dtrdy = d.dtrdy, dtrdz = d.dtrdz, ddamp2 = d.ddamp2;
+  const T cd = d.cdamp[k];
+  const T gzk = has_up ? d.gzitak[k] : T(0), gzk1 = has_dn ? d.gzitak[k + 1] : T(0);
+  // u-part and v-part of a row of this lane's column
+  struct Ur { T uk, um, up, rfw, fmz, hx, mx, rmu, mu, mv, s0; };
+  struct Vr { T vk, vm, vp, rfs, rmv, hy; };
+  auto load_u = [&](int i, Ur& x) {
+    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+    x.uk = u[c];
+    x.um = has_up ? u[c - pl] : T(0);
+    x.up = has_dn ? u[c + pl] : T(0);
+    x.rfw = rfw[c]; x.fmz = fmz[c]; x.hx = d.hx[c]; x.mu = d.mu[c];
+    x.mx = rot ? d.mx[c] : d.mx2[c];
+    x.rmu = rot ? T(0) : d.rmu[c];
+    x.mv = rot ? T(0) : d.mv[c];
+    x.s0 = has_up ? T(0) : d.s[c];  // s at the top level is never computed here
+  };
+  auto load_v = [&](int i, Vr& x) {
+    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+    x.vk = v[c];
+    x.vm = has_up ? v[c - pl] : T(0);
+    x.vp = has_dn ? v[c + pl] : T(0);
+    x.rfs = rfs[c]; x.rmv = d.rmv[c]; x.hy = d.hy[c];
+  };
+  // zdiv2a, s(k), s(k+1) of a row from its u-part and the v-parts of the
+  // row and the row after (expressions of k_sound_div)
+  struct Zr { T z, sk, sk1, ws; };
+  auto row_terms = [&](const Ur& a, const Vr& b, const Vr& bn) {
+    const T uk_e = __shfl_down_sync(0xffffffffu, a.uk, 1);
+    const T um_e = __shfl_down_sync(0xffffffffu, a.um, 1);
+    const T up_e = __shfl_down_sync(0xffffffffu, a.up, 1);
+    const T rfw_e = __shfl_down_sync(0xffffffffu, a.rfw, 1);
+    const T hx_e = __shfl_down_sync(0xffffffffu, a.hx, 1);
+    const T rmu_e = __shfl_down_sync(0xffffffffu, a.rmu, 1);
+    Zr r;
+    if (has_up) {
+      const T zuh = (a.uk + a.um) * a.hx + (uk_e + um_e) * hx_e;
+      const T zvh = (b.vk + b.vm) * b.hy + (bn.vk + bn.vm) * bn.hy;
+      r.sk = -((T(0.25) * (zuh + zvh)) * gzk);
+    } else {
+      r.sk = a.s0;
+    }
+    if (has_dn) {
+      const T zuh = (a.up + a.uk) * a.hx + (up_e + uk_e) * hx_e;
+      const T zvh = (b.vp + b.vk) * b.hy + (bn.vp + bn.vk) * bn.hy;
+      r.sk1 = -((T(0.25) * (zuh + zvh)) * gzk1);
+      r.ws = T(0);
+    } else {  // surface w(kz+1) and s(kz+1) (:536-549)
+      const T zuh = a.uk * a.hx + uk_e * hx_e;
+      const T zvh = b.vk * b.hy + bn.vk * bn.hy;
+      r.ws = T(0.5) * (zuh + zvh);
+      r.sk1 = -r.ws;
+    }
+    if (rot) {
+      const T zum = (dtrdx * a.uk) * a.rfw;
+      const T zup = (dtrdx * uk_e) * rfw_e;
+      const T zvm = ((dtrdy * b.vk) * b.rfs) * b.rmv;
+      const T zvp = ((dtrdy * bn.vk) * bn.rfs) * bn.rmv;
+      r.z = (a.fmz * a.mx) * ((zup - zum) + (zvp - zvm));
+    } else {
+      const T zum = ((dtrdx * a.uk) * a.rmu) * a.rfw;
+      const T zup = ((dtrdx * uk_e) * rmu_e) * rfw_e;
+      const T zvm = ((dtrdy * b.vk) * b.rmv) * b.rfs;
+      const T zvp = ((dtrdy * bn.vk) * bn.rmv) * bn.rfs;
+      r.z = (a.mx * a.fmz) * ((zup - zum) + (zvp - zvm));
+    }
+    return r;
+  };
+  // prologue: zdiv2a of row i_s-1, all terms of row i_s
+  Ur ua, ub, un;
+  Vr va, vb, vc, vn;
+  load_u(i_s - 1, ua); load_v(i_s - 1, va); load_v(i_s, vb);
+  load_u(i_s, ub); load_v(i_s + 1, vc);
+  const T z_first = row_terms(ua, va, vb).z;
+  T z_prev = z_first;
+  Zr zcur = row_terms(ub, vb, vc);
+  Ur ucur = ub;
+  Vr vcur = vb;
+  if (i_s + 1 <= i_e) { load_u(i_s + 1, un); load_v(i_s + 2, vn); }
+  for (int i = i_s; i < i_e; ++i) {
+    // in registers: z(i-1); row i (ucur, vcur, zcur); v-part of row i+1 (vc);
+    // in flight: u-part of row i+1 (un), v-part of row i+2 (vn)
+    const Ur unext = un;
+    const Vr vnext = vn;
+    if (i + 2 <= i_e) { load_u(i + 2, un); load_v(i + 3, vn); }
+    const Zr znext = row_terms(unext, vc, vnext);  // row i+1
+    const T zc = zcur.z;
+    const T zw = __shfl_up_sync(0xffffffffu, zc, 1);
+    const T ze = __shfl_down_sync(0xffffffffu, zc, 1);
+    const T zs = z_prev, zn = znext.z;
+    if (out_lane) {
+      const int ii = i;
+      const size_t c = (size_t)jj + (size_t)nj * ii;
+      const T u0 = ucur.uk, v0 = vcur.vk;
+      if (has_up) d.s[o + c] = zcur.sk;
+      if (!has_dn) {
+        d.w[c + (size_t)kz * pl] = zcur.ws;
+        d.s[c + (size_t)kz * pl] = -zcur.ws;
+      }
+      if (jj == 0) d.eu_j[ii + (size_t)ni * k] = u0;
+      if (ii == ni - 1) d.eu_i[jj + (size_t)nj * k] = u0;
+      if (jj == nj - 1) d.ev_j[ii + (size_t)ni * k] = v0;
+      if (ii == 0) d.ev_i[jj + (size_t)nj * k] = v0;
+      uo[c] = u0 + ((cd * ucur.mu) * (zc - zw));
+      if (rot)
+        vo[c] = v0 + cd * (zc - zs);
+      else
+        vo[c] = v0 + ((cd * ucur.mv) * (zc - zs));
+      const T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
+      T zd = zc + ddamp2 * p2d;
+      zd = zd + (ucur.fmz * dtrdz) * (zcur.sk - zcur.sk1);
+      d.zdiv2b[o + c] = zd;
+    }
+    z_prev = zc;
+    zcur = znext;
+    ucur = unext;
+    vcur = vc;
+    vc = vnext;
+  }
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_divdamp_strip(View<T> d, int R) {
+  b_divdamp_strip<T>(d, blockIdx.x, blockIdx.y, R);
+}
+
+template <class T>
+__global__ void __launch_bounds__(128)
+    kb_divdamp_strip(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int R) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_divdamp_strip<T>(sv, t.y, t.z, R);
+}
+
 // ---- advection: staggered -> cross points (:1327-1341, :1389-1417) -----
 template <class T>
 __device__ __forceinline__ void b_stag_to_x(const View<T>& d, const int bx, const int by, const int bz) {
@@ -1737,7 +1911,8 @@ int launch_prediag(const View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   return 1;
 }
 
-// one sound() call: nsound substeps; flips d.cur once per substep
+// one sound() call: nsound substeps; flips d.cur once per substep, twice
+// with the fused divergence/damping kernel (kmarch bit 16)
 template <class T>
 int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   int n = 0;
@@ -1746,15 +1921,22 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   const dim3 kg = pt_grid(d.nj, d.ni, (d.kz + kKC - 1) / kKC);  // k-marching: chunks of kKC levels
   for (int ns = 1; ns <= fl.nsound; ++ns) {
     const int last = ns == fl.nsound;
-    if (d.kmarch & 1)
-      MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div_km<T><<<kg, pb, 0, st>>>(d));
-    else
-      MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div<T><<<pg, pb, 0, st>>>(d));
-    if (d.kmarch & 2)
-      MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp_km<T><<<kg, pb, 0, st>>>(d));
-    else
-      MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp<T><<<pg, pb, 0, st>>>(d));
-    n += 2;
+    if (d.kmarch & 16) {
+      const int nstrips = ((d.nj + kDDJ - 1) / kDDJ) * ((d.ni + kDDR - 1) / kDDR);
+      MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
+      d.cur ^= 1;  // the damped u, v are in the other buffer
+      ++n;
+    } else {
+      if (d.kmarch & 1)
+        MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div_km<T><<<kg, pb, 0, st>>>(d));
+      else
+        MOLOCH_LAUNCH(KK_SOUND_DIV, st, k_sound_div<T><<<pg, pb, 0, st>>>(d));
+      if (d.kmarch & 2)
+        MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp_km<T><<<kg, pb, 0, st>>>(d));
+      else
+        MOLOCH_LAUNCH(KK_SOUND_DAMP, st, k_sound_damp<T><<<pg, pb, 0, st>>>(d));
+      n += 2;
+    }
     if (fl.divfilter) {
       MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 1));
       MOLOCH_LAUNCH(KK_LAP_FILTER, st, k_lap_filter<T><<<pg, pb, 0, st>>>(d));
@@ -1846,14 +2028,20 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
   for (int a = 0; a < fl.nadv; ++a) {
     for (int ns = 1; ns <= fl.nsound; ++ns) {
       const int last = ns == fl.nsound;
-      if (b.kmarch & 1)
-        MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div_km<T><<<nkc, pb, 0, st>>>(V(), KC));
-      else
-        MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div<T><<<npt, pb, 0, st>>>(V(), PT));
-      if (b.kmarch & 2)
-        MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp_km<T><<<nkc, pb, 0, st>>>(V(), KC));
-      else
-        MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp<T><<<npt, pb, 0, st>>>(V(), PT));
+      if (b.kmarch & 16) {
+        MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, kb_divdamp_strip<T><<<b.ntiles[TK_DSTRIP], 128, 0, st>>>(V(), b.tiles[TK_DSTRIP], kDDR));
+        cur ^= 1;  // the damped u, v are in the other buffer
+        --n;
+      } else {
+        if (b.kmarch & 1)
+          MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div_km<T><<<nkc, pb, 0, st>>>(V(), KC));
+        else
+          MOLOCH_LAUNCH(KK_SOUND_DIV, st, kb_sound_div<T><<<npt, pb, 0, st>>>(V(), PT));
+        if (b.kmarch & 2)
+          MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp_km<T><<<nkc, pb, 0, st>>>(V(), KC));
+        else
+          MOLOCH_LAUNCH(KK_SOUND_DAMP, st, kb_sound_damp<T><<<npt, pb, 0, st>>>(V(), PT));
+      }
       if (fl.divfilter) {
         MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 1));
         MOLOCH_LAUNCH(KK_LAP_FILTER, st, kb_lap_filter<T><<<npt, pb, 0, st>>>(V(), PT));

@@ -725,11 +725,11 @@ __global__ void __launch_bounds__(256) k_sur_vvel(View<float> d, const float* __
 }
 
 // Accepted cycle, part 2: state += denormalised increments, column by
-// column; u, v go to the buffer the plain loop leaves them in after nsound
-// substeps.
+// column; u, v go to the buffer the plain loop leaves them in (outpar: the
+// parity of its buffer flips over the cycle).
 __global__ void __launch_bounds__(256) k_sur_apply(View<float> d, const float* __restrict__ Y, int ld,
                                                    const float* __restrict__ ymean, const float* __restrict__ ystd,
-                                                   const int* __restrict__ ctl, int nsound) {
+                                                   const int* __restrict__ ctl, int outpar) {
   if (!ctl[CTL_FLAG]) return;
   const int jj = blockIdx.x * 32 + threadIdx.x, ii = blockIdx.y * 8 + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
@@ -738,8 +738,8 @@ __global__ void __launch_bounds__(256) k_sur_apply(View<float> d, const float* _
   const float* __restrict__ yr = Y + c;  // output-major: output q at yr[q * ld]
   const float* u = d.ubuf[d.cur];
   const float* v = d.vbuf[d.cur];
-  float* uo = d.ubuf[d.cur ^ (nsound & 1)];
-  float* vo = d.vbuf[d.cur ^ (nsound & 1)];
+  float* uo = d.ubuf[d.cur ^ outpar];
+  float* vo = d.vbuf[d.cur ^ outpar];
   auto inc = [&](int f, int k) { const int q = f * kz + k; return yr[(size_t)q * ld] * ystd[q] + ymean[q]; };
   for (int k = 0; k < kz; ++k) {
     const size_t q = c + (size_t)k * pl;
@@ -865,7 +865,7 @@ static void adam_all(Surrogate* s, float lr, int t, cudaStream_t st) {
   }
 }
 
-int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound) {
+int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound, int outpar) {
   const int n = v.nj * v.ni;
   k_sur_begin<<<1, 1, 0, st>>>(s->ctl, s->judge_every, s->jacc);
   const int* run = s->ctl + CTL_RUN;
@@ -878,7 +878,7 @@ int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound) {
   k_sur_judge_snapshot<<<grid1((size_t)5 * n * v.kz), 256, 0, st>>>(v, s->ctl, s->jsnap);
   const dim3 cg((v.nj + 31) / 32, (v.ni + 7) / 8);
   k_sur_vvel<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, n, s->ymean, s->ystd, s->ctl, nsound);
-  k_sur_apply<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, n, s->ymean, s->ystd, s->ctl, nsound);
+  k_sur_apply<<<cg, dim3(32, 8), 0, st>>>(v, s->Yinf, n, s->ymean, s->ystd, s->ctl, outpar);
   return 11;
 }
 

@@ -60,7 +60,7 @@ struct Surrogate {
 
 // one surrogate cycle before sound(): features, MLP, check, decision,
 // commit (the plain substeps then skip); returns the kernel count
-int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound);
+int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound, int outpar);
 // after sound(): the judge's comparison on judge cycles
 int sur_after(Surrogate* s, View<float>& v, cudaStream_t st);
 

@@ -135,7 +135,7 @@ struct View {
 enum KernelKind {
   KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_DAMP, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE,
   KK_SOUND_MOMENTUM, KK_STAG_TO_X, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
-  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_COUNT
+  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_COUNT
 };
 
 // Optional event recorder: when a launcher is given one, it records a CUDA
@@ -159,10 +159,12 @@ struct KernelTimer {
 // field-set parities the step is at when the kernel runs).
 // TK_CHUNK tiles cover kKC levels each (the k-marching sound kernels);
 // TK_MSTRIP tiles are blocks of 4 momentum warp strips (30 columns x kMomR
-// rows) of one level
+// rows) of one level; TK_DSTRIP tiles blocks of 4 divergence/damping warp
+// strips (29 columns x kDDR rows)
 constexpr int kKC = 4;
 constexpr int kMomJ = 30, kMomR = 32;
-enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_COUNT };
+constexpr int kDDJ = 29, kDDR = 32;
+enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_DSTRIP, TK_COUNT };
 template <class T>
 struct Batch {
   const View<T>* views[2][2];   // device arrays, one view per member

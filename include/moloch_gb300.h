@@ -191,7 +191,9 @@ const char* moloch_gpu_kernel_name(int kind);
  *   choice[1] = sound kernel variants, bit mask: 1 divergence, 2 damping,
  *               4 momentum as k-marching kernels (chunks of 4 levels per
  *               thread, next level prefetched), 8 momentum as warp strips
- *               (30 columns x 32 rows); 0 = one level per thread.
+ *               (30 columns x 32 rows), 16 divergence and damping fused in
+ *               one warp-strip kernel (29 columns x 32 rows; overrides 1
+ *               and 2); 0 = one level per thread.
  * moloch_gpu_autotune runs advection() and sound() once per candidate and
  * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the

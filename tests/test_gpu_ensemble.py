@@ -70,11 +70,12 @@ def test_ensemble_autotune(gpu_lib, stream):
         m.close()
 
 
-@pytest.mark.parametrize("variant", [11, 7])
+@pytest.mark.parametrize("variant", [11, 7, 24])
 def test_ensemble_strip_shape_matches_members(gpu_lib, stream, variant):
-    """Ensemble with the warp-strip horizontal WAF and the k-marching or
-    warp-strip sound kernels against the same members run alone with the
-    tile kernel and the one-level-per-thread kernels.
+    """Ensemble with the warp-strip horizontal WAF and the k-marching,
+    warp-strip or fused divergence/damping sound kernels against the same
+    members run alone with the tile kernel and the one-level-per-thread
+    kernels.
     Different kernels contract different multiply-adds in the FP64 build,
     so the bound is 1e-12 rather than the 1e-13 of identical kernels."""
     ms = members(gpu_lib, "fp64", stream=stream.cuda_stream)

@@ -99,12 +99,15 @@ def test_options(oracle_mod, gpu_lib, opts):
     compare(o, g, PROG + DIAG, 1e-12)
 
 
-@pytest.mark.parametrize("variant", [7, 11])
-def test_divfilter_with_sound_variants(oracle_mod, gpu_lib, variant):
+@pytest.mark.parametrize("opts", [dict(divfilter=True), dict(rotllr=False),
+                                  dict(divfilter=True, filterpai=True, filtertheta=True, rotllr=False)])
+@pytest.mark.parametrize("variant", [7, 11, 24])
+def test_options_with_sound_variants(oracle_mod, gpu_lib, variant, opts):
     """The divergence filter path (the column kernel leaves zdiv2b and pai to
-    the filter kernels) with the k-marching and warp-strip sound kernels,
-    against the oracle."""
-    o, g = pair(oracle_mod, gpu_lib, 19, 16, 10, hills=((300.0, 9.0, 8.0, 3.0),), divfilter=True)
+    the filter kernels) and the non-rotated map factors with the k-marching,
+    warp-strip and fused divergence/damping sound kernels, against the
+    oracle."""
+    o, g = pair(oracle_mod, gpu_lib, 19, 16, 10, hills=((300.0, 9.0, 8.0, 3.0),), **opts)
     g.set_tuning([1, variant])
     for s in range(1, 4):
         o.step(s)
@@ -266,14 +269,16 @@ def test_horizontal_waf_strips_match_tiles(gpu_lib, mode, tol, shape):
 
 
 @pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
-@pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8)])
+@pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8), (9, 16), (13, 24), (10, 20)])
 def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz, variant):
     """The k-marching divergence/damping/momentum kernels (chunks of 4
-    levels, the next level prefetched) and the warp-strip momentum kernel
+    levels, the next level prefetched), the warp-strip momentum kernel
     (30 columns x 32 rows, neighbours by shuffles, stale-halo edge buffers
-    on the boundary lanes and rows) against the one-level-per-thread
-    kernels: bit for bit in the exact build; kz not a multiple of the chunk,
-    jx and iy not multiples of the strip."""
+    on the boundary lanes and rows) and the fused divergence/damping strips
+    (variant bit 16: 29 columns x 32 rows, damped u, v to the other buffer)
+    against the one-level-per-thread kernels: bit for bit in the exact
+    build; kz not a multiple of the chunk, jx and iy not multiples of the
+    strips."""
     a = gpu_lib.Moloch(45, 37, kz, mode=mode)
     b = gpu_lib.Moloch(45, 37, kz, mode=mode)
     for g in (a, b):

@@ -64,10 +64,11 @@ def _state(g):
 
 
 @pytest.mark.parametrize("jx,iy,kz,tuning", [(24, 20, 8, [1, 0]), (37, 29, 12, [1, 0]), (37, 29, 12, [32, 11]),
-                                             (24, 20, 8, [16, 7])])
+                                             (24, 20, 8, [16, 7]), (37, 29, 12, [32, 24])])
 def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz, tuning):
     """tuning: the plain kernel variants that must all stand aside on a
-    committed cycle (one level per thread, strips, k-marching)."""
+    committed cycle (one level per thread, strips, k-marching, the fused
+    divergence/damping strips, which flip the u/v buffers twice a substep)."""
     from oracle import mlp_oracle as mo
     g = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     g.setup_idealized(hills=((400.0, jx / 2, iy / 2, 3.0),), u0=5.0, v0=-3.0)
@@ -105,12 +106,14 @@ def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz, tuning):
     g.close()
 
 
-def test_sur_fallback_is_bit_identical(gpu_lib):
+@pytest.mark.parametrize("tuning", [[1, 0], [32, 24]])
+def test_sur_fallback_is_bit_identical(gpu_lib, tuning):
     jx, iy, kz = 32, 24, 10
     a = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     b = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     for g in (a, b):
         g.setup_idealized(hills=((300.0, 16.0, 12.0, 3.0),), u0=4.0)
+        g.set_tuning(tuning)
     sur = gpu_lib.Surrogate(kz, capacity=256, batch=128)
     _random_params(sur, np.random.default_rng(2))
     sur.set_stats(np.zeros((5, kz)), np.ones((5, kz)), np.zeros((5, kz)), np.ones((5, kz)))
