@@ -118,6 +118,8 @@ _PROTOS = {
     "moloch_sur_collect": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                           ctypes.c_ulonglong]),
     "moloch_sur_pairs": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_sur_pair_data": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                            ctypes.c_void_p]),
     "moloch_sur_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double, ctypes.c_ulonglong]),
     "moloch_sur_train": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_float, ctypes.c_ulonglong,
                                         ctypes.POINTER(ctypes.c_float), ctypes.POINTER(ctypes.c_float)]),
@@ -414,6 +416,17 @@ class Surrogate:
     def collect(self, model, nsteps, cols_per_cycle=512, seed=3):
         _check(self.L.moloch_sur_collect(self.h, model.h, nsteps, cols_per_cycle, seed))
         return self.L.moloch_sur_pairs(self.h)
+
+    def pair_data(self, first=0, count=None):
+        """Collected pairs as (X [count][45 kz] raw features, T [count][5 kz]
+        raw increments), in collection order."""
+        d = self.dims()
+        if count is None:
+            count = d["pairs"] - first
+        X = np.empty((count, d["nin"]), np.float32)
+        T = np.empty((count, d["nout"]), np.float32)
+        _check(self.L.moloch_sur_pair_data(self.h, first, count, X.ctypes.data, T.ctypes.data))
+        return X, T
 
     def prepare(self, val_fraction=0.1, seed=5):
         _check(self.L.moloch_sur_prepare(self.h, val_fraction, seed))

@@ -31,21 +31,27 @@ constexpr int kStages = 4;
 constexpr int kAStage = kTileM * kChunkK * 2;   // 16 KB
 constexpr int kBStage = kTileN * kChunkK * 2;   // 32 KB
 constexpr int kSmem = kStages * (kAStage + kBStage) + 1024;  // + alignment slack
-constexpr int kThreads = 192;  // loader warp, MMA warp, four epilogue warps
+constexpr int kThreads = 320;  // loader warp, MMA warp, eight epilogue warps
+constexpr int kEpiThreads = 256;
 
 enum Act { ACT_NONE = 0, ACT_SILU = 1 };
 
 static __device__ int g_tc_error;  // set when a bounded wait gives up
 
-__device__ __forceinline__ float silu(float x) { return x / (1.0f + __expf(-x)); }
+// x * sigmoid(x) with the fast reciprocal divide (relative error ~1e-7,
+// far below the BF16 rounding of the stored activation); exp(-x) = inf
+// for very negative x gives 0
+__device__ __forceinline__ float silu(float x) { return __fdividef(x, 1.0f + __expf(-x)); }
 
-// Persistent CTA (one per SM), six warps: warp 0 issues the TMA loads of
+// Persistent CTA (one per SM), ten warps: warp 0 issues the TMA loads of
 // 64-wide K chunks of A and B (128-byte swizzle) into a kStages-deep ring of
 // shared-memory stages, warp 1 issues the 128 x N x 16 MMAs of each chunk
-// and commits them to the stage's "empty" barrier, and warps 2-5 drain the
-// accumulator of the previous tile from TMEM (tcgen05.ld, one 32-lane
-// quarter per warp) while the next tile accumulates: two accumulators of
-// 256 columns each are double-buffered in the 512 TMEM columns.
+// and commits them to the stage's "empty" barrier, and warps 2-9 drain the
+// accumulator of the previous tile from TMEM (tcgen05.ld; two warps per
+// 32-lane quarter, taking alternate 32-column groups) while the next tile
+// accumulates: two accumulators of 256 columns each are double-buffered in
+// the 512 TMEM columns.  The epilogue is latency-bound per warp (bias,
+// SiLU, BF16 packing, row stores), so it gets two warps per quarter.
 __global__ void __launch_bounds__(kThreads, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB, int boxB,
               float* __restrict__ C, int ldc, __nv_bfloat16* __restrict__ Cb, int ldcb,
@@ -68,7 +74,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     for (int b = 0; b < 2; ++b) {
       tc::mbar_init(&acc_full[b], 1);
-      tc::mbar_init(&acc_empty[b], 128);
+      tc::mbar_init(&acc_empty[b], kEpiThreads);
     }
     tc::mbar_init(&done, 1);
     s_fail = 0;
@@ -134,9 +140,11 @@ __global__ void __launch_bounds__(kThreads, 1)
     }
     tc::mma_commit(&done);  // arrives once every MMA issued above has completed
   } else if (warp >= 2) {
-    // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31
-    const int q = warp & 3;
+    // ---- epilogue: warp w reads TMEM lanes 32*(w%4) .. +31 and the
+    // 32-column groups h, h+2, h+4, ... of the tile (h = (w-2)/4)
+    const int q = warp & 3, h = (warp - 2) >> 2;
     const uint32_t lrow = (uint32_t)(q * 32) << 16;
+    const bool bias4 = bias && ((reinterpret_cast<uintptr_t>(bias) & 15) == 0);
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
       const int b = lt & 1;
@@ -148,36 +156,57 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int m0 = (t % nm) * kTileM, n0 = (t / nm) * kTileN;
       const int nt = min(kTileN, N - n0);
       const int row = m0 + q * 32 + lane;
-      for (int c = 0; c < nt; c += 16) {
-        float v[16];
-        tc::tmem_ld16(tbase + lrow + (uint32_t)(b * kTileN + c), v);
+      for (int c = 32 * h; c < nt; c += 64) {
+        float v[32];
+        const int w = min(32, nt - c);  // 32, or 16 at the end of a 16-wide tile
+        if (w == 32)
+          tc::tmem_ld32(tbase + lrow + (uint32_t)(b * kTileN + c), v);
+        else
+          tc::tmem_ld16(tbase + lrow + (uint32_t)(b * kTileN + c), v);
         if (row < M) {
-#pragma unroll
-          for (int e = 0; e < 16; ++e) v[e] += bias ? bias[n0 + c + e] : 0.f;
-          if (C) {
-            float4* cp = reinterpret_cast<float4*>(C + (size_t)row * ldc + n0 + c);
-#pragma unroll
-            for (int e = 0; e < 4; ++e) cp[e] = make_float4(v[4 * e], v[4 * e + 1], v[4 * e + 2], v[4 * e + 3]);
-          }
-          if (Ct) {  // transposed: the 32 lanes of a warp write 32 consecutive rows of C
-#pragma unroll
-            for (int e = 0; e < 16; ++e) Ct[(size_t)(n0 + c + e) * ldct + row] = v[e];
-          }
-          if (Cb) {
-            uint32_t pk[8];
+          if (bias4) {
 #pragma unroll
             for (int e = 0; e < 8; ++e) {
-              float x0 = v[2 * e], x1 = v[2 * e + 1];
-              if (act == ACT_SILU) {
-                x0 = silu(x0);
-                x1 = silu(x1);
+              if (4 * e < w) {
+                const float4 bb = *reinterpret_cast<const float4*>(bias + n0 + c + 4 * e);
+                v[4 * e] += bb.x; v[4 * e + 1] += bb.y; v[4 * e + 2] += bb.z; v[4 * e + 3] += bb.w;
               }
-              const __nv_bfloat162 b2 = __floats2bfloat162_rn(x0, x1);
-              pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
             }
-            uint4* bp = reinterpret_cast<uint4*>(Cb + (size_t)row * ldcb + n0 + c);
-            bp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
-            bp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+          } else if (bias) {
+#pragma unroll
+            for (int e = 0; e < 32; ++e)
+              if (e < w) v[e] += bias[n0 + c + e];
+          }
+#pragma unroll
+          for (int g = 0; g < 2; ++g) {  // two 16-column halves
+            if (16 * g >= w) break;
+            const float* vg = v + 16 * g;
+            const int cg = c + 16 * g;
+            if (C) {
+              float4* cp = reinterpret_cast<float4*>(C + (size_t)row * ldc + n0 + cg);
+#pragma unroll
+              for (int e = 0; e < 4; ++e) cp[e] = make_float4(vg[4 * e], vg[4 * e + 1], vg[4 * e + 2], vg[4 * e + 3]);
+            }
+            if (Ct) {  // transposed: the 32 lanes of a warp write 32 consecutive rows of C
+#pragma unroll
+              for (int e = 0; e < 16; ++e) Ct[(size_t)(n0 + cg + e) * ldct + row] = vg[e];
+            }
+            if (Cb) {
+              uint32_t pk[8];
+#pragma unroll
+              for (int e = 0; e < 8; ++e) {
+                float x0 = vg[2 * e], x1 = vg[2 * e + 1];
+                if (act == ACT_SILU) {
+                  x0 = silu(x0);
+                  x1 = silu(x1);
+                }
+                const __nv_bfloat162 b2 = __floats2bfloat162_rn(x0, x1);
+                pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
+              }
+              uint4* bp = reinterpret_cast<uint4*>(Cb + (size_t)row * ldcb + n0 + cg);
+              bp[0] = make_uint4(pk[0], pk[1], pk[2], pk[3]);
+              bp[1] = make_uint4(pk[4], pk[5], pk[6], pk[7]);
+            }
           }
         }
       }
@@ -326,101 +355,134 @@ __device__ __forceinline__ float sur_field(const View<float>& d, int f, int j, i
   }
 }
 
-// Features of ncols columns (cols == nullptr: all columns in order), one
-// block per 128 columns and 64-feature chunk, one thread per column.  Feature index
-// (f * kz + k) * 9 + nb: field f (u, v, w levels 2..kz+1, pai, tetav), level
-// k, neighbour nb = (di + 1) * 3 + (dj + 1) fastest, so that a 64-feature
-// chunk touches about 7 field planes.  For each chunk a table in shared
-// memory gives every feature's plane, neighbour slot and normalisation; each
-// thread gathers its column's 64 values (consecutive threads read
-// consecutive j: coalesced, and the 9 neighbours hit L1), and the chunk
-// is transposed through shared memory so that 8 threads write one column's
-// 128-byte (BF16) or 256-byte (FP32) row segment together.  NORM: normalise
-// with the dataset statistics and write BF16; else write raw FP32.
+// Features of ncols columns (cols == nullptr: all columns in order).  Feature
+// index (f * kz + k) * 9 + nb: field f (u, v, w levels 2..kz+1, pai,
+// tetav), level k, neighbour nb = (di + 1) * 3 + (dj + 1) fastest.  Work
+// items of 128 columns x one 64-feature chunk (ldo / 64 chunks per column),
+// one thread per column, blocks looping over the items.  A chunk starting
+// at feature f0 covers at most 8 field planes, and where each of its 64
+// features sits (plane, neighbour) depends only on f0 % 9: one fully
+// unrolled body per value of f0 % 9 keeps the plane pointers, the nine
+// neighbour offsets and the 64 values in registers, all 64 loads issued
+// before any is used (the planes come from HBM; the 9 neighbours of
+// consecutive columns hit L1).  The 128 rows of the item are staged in
+// shared memory and leave as whole 128-byte (BF16) or 256-byte (FP32) row
+// segments, 8 or 16 threads per row.  NORM: normalise with the dataset
+// statistics and write BF16; else write raw FP32.
+// row strides of the staging tile, in 32-bit words: 144 B (BF16 rows of
+// 64 features + 16 B) and 272 B (FP32 rows + 16 B), so that the eight
+// 16-byte stores of a quarter warp land in distinct banks
+constexpr int kStageBf = 36, kStageF32 = 68;
+
+template <bool NORM, int OFF>
+__device__ __forceinline__ void feature_item(const float* const (&pp)[8], const float (&sub)[8],
+                                             const float (&mul)[8], const int (&nbo)[9], bool valid, int np_rel,
+                                             uint32_t* stage_row) {
+  float val[64];
+#pragma unroll
+  for (int r = 0; r < 64; ++r) {
+    const int pr = (OFF + r) / 9, nb = (OFF + r) % 9;
+    val[r] = (valid && pr < np_rel) ? __ldg(pp[pr] + nbo[nb]) : 0.f;
+  }
+  if (!valid) return;
+  if (NORM) {
+    uint32_t pk[32];
+#pragma unroll
+    for (int e = 0; e < 32; ++e) {
+      const int r0 = 2 * e, r1 = 2 * e + 1;
+      const int p0 = (OFF + r0) / 9, p1 = (OFF + r1) / 9;
+      const float x0 = p0 < np_rel ? (val[r0] - sub[p0]) * mul[p0] : 0.f;
+      const float x1 = p1 < np_rel ? (val[r1] - sub[p1]) * mul[p1] : 0.f;
+      const __nv_bfloat162 b2 = __floats2bfloat162_rn(x0, x1);
+      pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
+    }
+    uint4* dst = reinterpret_cast<uint4*>(stage_row);
+#pragma unroll
+    for (int e = 0; e < 8; ++e) dst[e] = make_uint4(pk[4 * e], pk[4 * e + 1], pk[4 * e + 2], pk[4 * e + 3]);
+  } else {
+    float4* dst = reinterpret_cast<float4*>(stage_row);
+#pragma unroll
+    for (int e = 0; e < 16; ++e) dst[e] = make_float4(val[4 * e], val[4 * e + 1], val[4 * e + 2], val[4 * e + 3]);
+  }
+}
+
 template <bool NORM>
 __global__ void __launch_bounds__(128) k_sur_features(View<float> d, const int* __restrict__ cols, int ncols,
                                                       const float* __restrict__ xmean, const float* __restrict__ xstd,
                                                       void* out, int ldo, const int* __restrict__ run) {
   if (run && !*run) return;
-  __shared__ int nbo[9][128];                 // neighbour column offsets
-  __shared__ const float* tptr[64];           // field plane of each feature of the chunk
-  __shared__ int tnb[64];                     // neighbour slot (-1: padding)
-  __shared__ float tsub[64], tmul[64];        // normalisation
-  __shared__ float tile[128][65];             // [column][feature]
+  __shared__ __align__(16) uint32_t stage[128 * kStageF32];  // the item's 128 output rows
   const int t = threadIdx.x;
-  const int c0 = blockIdx.x * 128;
-  const int kz = d.kz, nf = 45 * kz;
-  const int cidx = c0 + t;
-  {
-    int j = 0, i = 0;
-    if (cidx < ncols) {
-      const int col = cols ? cols[cidx] : cidx;
-      j = col % d.nj;
-      i = col / d.nj;
-    }
-    const int jm = j == 0 ? d.nj - 1 : j - 1, jp = j == d.nj - 1 ? 0 : j + 1;
-    const int im = i == 0 ? d.ni - 1 : i - 1, ip = i == d.ni - 1 ? 0 : i + 1;
-    const int jj[3] = {jm, j, jp}, ii[3] = {im, i, ip};
+  const int kz = d.kz, np = 5 * kz;  // field planes
+  const int srow = NORM ? kStageBf : kStageF32;
+  const int ntile = (ncols + 127) / 128, items = ntile * (ldo / 64);
+  // work items (column tile, 64-feature chunk), the column tile fastest
+  for (int item = blockIdx.x; item < items; item += gridDim.x) {
+    const int c0 = (item % ntile) * 128;
+    const int cidx = c0 + t;
+    const int f0 = (item / ntile) * 64;
+    const bool valid = cidx < ncols;
+    int nbo[9];
+    {
+      int j = 0, i = 0;
+      if (valid) {
+        const int col = cols ? cols[cidx] : cidx;
+        j = col % d.nj;
+        i = col / d.nj;
+      }
+      const int jm = j == 0 ? d.nj - 1 : j - 1, jp = j == d.nj - 1 ? 0 : j + 1;
+      const int im = i == 0 ? d.ni - 1 : i - 1, ip = i == d.ni - 1 ? 0 : i + 1;
+      const int jj[3] = {jm, j, jp}, ii[3] = {im, i, ip};
 #pragma unroll
-    for (int nb = 0; nb < 9; ++nb) nbo[nb][t] = jj[nb % 3] + d.nj * ii[nb / 3];
-  }
-  {
-    const int f0 = blockIdx.y * 64;  // one 64-feature chunk per block
-    if (t < 64) {
-      const int fe = f0 + t;
-      if (fe < nf) {
-        const int plane = fe / 9, k = plane % kz, fld = plane / kz;
-        const float* base = fld == 0 ? d.ubuf[d.cur] : fld == 1 ? d.vbuf[d.cur] : fld == 2 ? d.w + d.pl
-                          : fld == 3 ? d.pai : d.tetav;
-        tptr[t] = base + (size_t)k * d.pl;
-        tnb[t] = fe - 9 * plane;
-        if (NORM) {
-          tsub[t] = xmean[plane];
-          tmul[t] = 1.0f / xstd[plane];
-        }
+      for (int nb = 0; nb < 9; ++nb) nbo[nb] = jj[nb % 3] + d.nj * ii[nb / 3];
+    }
+    const int p0 = f0 / 9, off = f0 - 9 * p0;
+    const int np_rel = np - p0;  // planes of this chunk that exist (the rest is padding)
+    const float* pp[8];
+    float sub[8], mul[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int plane = p0 + q < np ? p0 + q : np - 1;
+      const int fld = plane / kz, k = plane - fld * kz;
+      const float* b = fld == 0 ? d.ubuf[d.cur] : fld == 1 ? d.vbuf[d.cur] : fld == 2 ? d.w + d.pl
+                     : fld == 3 ? d.pai : d.tetav;
+      pp[q] = b + (size_t)k * d.pl;
+      if (NORM) {
+        sub[q] = xmean[plane];
+        mul[q] = 1.0f / xstd[plane];
       } else {
-        tnb[t] = -1;
+        sub[q] = 0.f;
+        mul[q] = 1.f;
       }
     }
-    __syncthreads();
-    if (cidx < ncols) {
-      // all 64 loads of the chunk are issued before any is used (the plane
-      // data comes from HBM: the state is larger than L2)
-      float val[64];
-#pragma unroll
-      for (int r = 0; r < 64; ++r) {
-        const int nb = tnb[r];
-        val[r] = nb >= 0 ? __ldg(tptr[r] + nbo[nb < 0 ? 0 : nb][t]) : 0.f;
-      }
-#pragma unroll
-      for (int r = 0; r < 64; ++r) {
-        float x = val[r];
-        if (NORM && tnb[r] >= 0) x = (x - tsub[r]) * tmul[r];
-        tile[t][r] = x;
-      }
+    uint32_t* const row = stage + t * srow;
+    switch (off) {
+      case 0: feature_item<NORM, 0>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 1: feature_item<NORM, 1>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 2: feature_item<NORM, 2>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 3: feature_item<NORM, 3>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 4: feature_item<NORM, 4>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 5: feature_item<NORM, 5>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 6: feature_item<NORM, 6>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      case 7: feature_item<NORM, 7>(pp, sub, mul, nbo, valid, np_rel, row); break;
+      default: feature_item<NORM, 8>(pp, sub, mul, nbo, valid, np_rel, row); break;
     }
     __syncthreads();
-    // write: 8 (BF16) or 16 (FP32) threads per column row segment
+    // the staged rows leave as whole 128-byte (BF16) / 256-byte (FP32)
+    // segments, 16 bytes per thread, 8 or 16 threads per row
     if (NORM) {
       for (int q = t; q < 128 * 8; q += 128) {
-        const int cc = q >> 3, part = q & 7;
-        if (c0 + cc < ncols && f0 + part * 8 < ldo) {
-          uint32_t pk[4];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const __nv_bfloat162 b2 = __floats2bfloat162_rn(tile[cc][part * 8 + 2 * e], tile[cc][part * 8 + 2 * e + 1]);
-            pk[e] = *reinterpret_cast<const uint32_t*>(&b2);
-          }
-          *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) + (size_t)(c0 + cc) * ldo + f0 + part * 8) =
-              make_uint4(pk[0], pk[1], pk[2], pk[3]);
-        }
+        const int rr = q >> 3, part = q & 7;
+        if (c0 + rr < ncols)
+          *reinterpret_cast<uint4*>(reinterpret_cast<__nv_bfloat16*>(out) + (size_t)(c0 + rr) * ldo + f0 + part * 8) =
+              *reinterpret_cast<const uint4*>(stage + rr * kStageBf + part * 4);
       }
     } else {
       for (int q = t; q < 128 * 16; q += 128) {
-        const int cc = q >> 4, part = q & 15;
-        if (c0 + cc < ncols && f0 + part * 4 < ldo)
-          *reinterpret_cast<float4*>(reinterpret_cast<float*>(out) + (size_t)(c0 + cc) * ldo + f0 + part * 4) =
-              make_float4(tile[cc][part * 4], tile[cc][part * 4 + 1], tile[cc][part * 4 + 2], tile[cc][part * 4 + 3]);
+        const int rr = q >> 4, part = q & 15;
+        if (c0 + rr < ncols)
+          *reinterpret_cast<uint4*>(reinterpret_cast<float*>(out) + (size_t)(c0 + rr) * ldo + f0 + part * 4) =
+              *reinterpret_cast<const uint4*>(stage + rr * kStageF32 + part * 4);
       }
     }
     __syncthreads();
@@ -582,20 +644,32 @@ __global__ void k_sur_begin(int* __restrict__ ctl, int judge_every, double* __re
 
 // every increment finite and within threshold x the envelope of the
 // training targets (per output, normalised units); tracks the largest ratio
-// (Y output-major: [outputs][n]; grid.y = output, grid.x strides over columns)
+// (Y output-major: [outputs][n]; grid.y strides over outputs, grid.x over
+// columns: a small fixed grid, so that a cycle without inference pays for
+// few empty blocks)
 __global__ void k_sur_check(const float* __restrict__ Y, int n, int ld, int m, const float* __restrict__ env,
                             float threshold, int* __restrict__ ctl, const int* __restrict__ run) {
   if (run && !*run) return;
-  const int o = blockIdx.y;
-  const float lim = threshold * env[o];
-  const float rcp_env = 1.0f / env[o];
-  const float* __restrict__ yo = Y + (size_t)o * n;
   int b = 0;
   float rmax = 0.f;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < n; c += gridDim.x * blockDim.x) {
-    const float y = fabsf(yo[c]);
-    if (!(y <= lim)) b = 1;  // also catches NaN
-    rmax = y == y ? fmaxf(rmax, y * rcp_env) : __int_as_float(0x7f800000);
+  for (int o = blockIdx.y; o < m; o += gridDim.y) {
+    const float lim = threshold * env[o];
+    const float rcp_env = 1.0f / env[o];
+    const float* __restrict__ yo = Y + (size_t)o * n;
+    const int stride = gridDim.x * blockDim.x;
+    int c = blockIdx.x * blockDim.x + threadIdx.x;
+    auto take = [&](float y) {
+      if (!(y <= lim)) b = 1;  // also catches NaN
+      rmax = y == y ? fmaxf(rmax, y * rcp_env) : __int_as_float(0x7f800000);
+    };
+    for (; c + 7 * stride < n; c += 8 * stride) {  // eight independent loads in flight
+      float y[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) y[u] = fabsf(yo[c + u * stride]);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) take(y[u]);
+    }
+    for (; c < n; c += stride) take(fabsf(yo[c]));
   }
   for (int q = 16; q > 0; q >>= 1) rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, q));
   if (__any_sync(0xffffffffu, b) && (threadIdx.x & 31) == 0) atomicOr(&ctl[CTL_BAD], 1);
@@ -801,6 +875,15 @@ static int gemm(const void* A, int lda, const void* B, int ldb, float* C, int ld
 }
 
 static int grid1(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
+// k_sur_check: at most 16 x 38 blocks of 256 threads
+static dim3 check_grid(int n, int m) { return dim3(std::min((n + 2047) / 2048, 16), std::min(m, 38)); }
+// k_sur_features: work items of 128 columns x 64 features, one wave of
+// blocks of 128 threads (5 per SM at 92 registers, 34 KB of shared memory)
+// looping over the items
+static dim3 feature_grid(int ncols, int kin) {
+  const long items = (long)((ncols + 127) / 128) * (kin / 64);
+  return dim3((unsigned)std::min<long>(items, 152 * 5));
+}
 
 static int transpose(const void* in, int rows, int cols, int ld_in, void* out, int ld_out, cudaStream_t st) {
   dim3 g((cols + 31) / 32, (rows + 31) / 32);
@@ -869,10 +952,10 @@ int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound, int out
   const int n = v.nj * v.ni;
   k_sur_begin<<<1, 1, 0, st>>>(s->ctl, s->judge_every, s->jacc);
   const int* run = s->ctl + CTL_RUN;
-  k_sur_features<true><<<dim3((n + 127) / 128, s->kin / 64), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
+  k_sur_features<true><<<feature_grid(n, s->kin), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
                                                                           s->kin, run);
   forward(s, s->Xinf, n, s->Hinf, nullptr, nullptr, st, run, s->Yinf);  // Yinf output-major
-  k_sur_check<<<dim3((n + 2047) / 2048, s->nout), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
+  k_sur_check<<<check_grid(n, s->nout), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
                                                                  s->ctl, run);
   k_sur_decide<<<1, 1, 0, st>>>(s->ctl, s->counts);
   k_sur_judge_snapshot<<<grid1((size_t)5 * n * v.kz), 256, 0, st>>>(v, s->ctl, s->jsnap);
@@ -1017,7 +1100,7 @@ int moloch_sur_collect(moloch_surrogate_t* s, moloch_handle_t* h, int nsteps, in
         SUR_TRY(cudaMemcpyAsync(s->cols, pick.data(), take * sizeof(int), cudaMemcpyHostToDevice, st));
         SUR_TRY(cudaStreamSynchronize(st));
         View<float>& v = *moloch_internal_viewf(h);
-        k_sur_features<false><<<dim3((take + 127) / 128, s->kin / 64), 128, 0, st>>>(v, s->cols, take, nullptr, nullptr,
+        k_sur_features<false><<<feature_grid(take, s->kin), 128, 0, st>>>(v, s->cols, take, nullptr, nullptr,
                                                                    s->Xraw + (size_t)s->npairs * s->kin, s->kin,
                                                                    nullptr);
         k_sur_snapshot<<<take, 128, 0, st>>>(v, s->cols, take, s->snap);
@@ -1038,6 +1121,19 @@ int moloch_sur_collect(moloch_surrogate_t* s, moloch_handle_t* h, int nsteps, in
 }
 
 int moloch_sur_pairs(moloch_surrogate_t* s) { return s ? s->npairs : -1; }
+
+int moloch_sur_pair_data(moloch_surrogate_t* s, int first, int count, float* X, float* T) {
+  if (!s || first < 0 || count < 0 || first + count > s->npairs || (count && (!X || !T))) {
+    moloch_internal_set_error("sur_pair_data: bad arguments");
+    return MOLOCH_ERR_ARG;
+  }
+  if (!count) return MOLOCH_OK;
+  SUR_TRY(cudaMemcpy2D(X, (size_t)s->nin * 4, s->Xraw + (size_t)first * s->kin, (size_t)s->kin * 4,
+                       (size_t)s->nin * 4, count, cudaMemcpyDeviceToHost));
+  SUR_TRY(cudaMemcpy2D(T, (size_t)s->nout * 4, s->T + (size_t)first * s->nop, (size_t)s->nop * 4,
+                       (size_t)s->nout * 4, count, cudaMemcpyDeviceToHost));
+  return MOLOCH_OK;
+}
 
 // normalisation statistics, normalised BF16 features, shuffle, split
 int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long long seed) {
@@ -1304,7 +1400,7 @@ int moloch_sur_profile(moloch_surrogate_t* s, moloch_handle_t* h, double* ms, in
   cudaEvent_t ev[7];
   for (auto& e : ev) SUR_TRY(cudaEventCreate(&e));
   cudaEventRecord(ev[0], st);
-  k_sur_features<true><<<dim3((n + 127) / 128, s->kin / 64), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
+  k_sur_features<true><<<feature_grid(n, s->kin), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
                                                                           s->kin, nullptr);
   cudaEventRecord(ev[1], st);
   gemm(s->Xinf, s->kin, s->L[0].Wb, s->kin, nullptr, hid, s->Hinf[0], hid, s->L[0].b, n, hid, s->kin, ACT_SILU, st);
@@ -1319,7 +1415,7 @@ int moloch_sur_profile(moloch_surrogate_t* s, moloch_handle_t* h, double* ms, in
   // the check writes slots CTL_BAD and CTL_MAXRATIO of the block it is
   // given: point it at the unused upper half of the control block
   static_assert(16 + CTL_MAXRATIO < CTL_COUNT, "control block too small");
-  k_sur_check<<<dim3((n + 2047) / 2048, s->nout), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
+  k_sur_check<<<check_grid(n, s->nout), 256, 0, st>>>(s->Yinf, n, s->nop, s->nout, s->env, s->threshold,
                                                                  s->ctl + 16, nullptr);
   cudaEventRecord(ev[6], st);
   SUR_TRY(cudaEventSynchronize(ev[6]));

@@ -281,6 +281,11 @@ int moloch_sur_create(int kz, int capacity, int batch, unsigned long long seed, 
 int moloch_sur_collect(moloch_surrogate_t* s, moloch_handle_t* h, int nsteps, int cols_per_cycle,
                        unsigned long long seed);
 int moloch_sur_pairs(moloch_surrogate_t* s);
+/* copy collected pairs first .. first+count-1 to the host: X [count][45*kz]
+ * raw FP32 features, T [count][5*kz] raw increments (output index
+ * f*kz + k), in collection order (before moloch_sur_prepare shuffles its
+ * normalised copies) */
+int moloch_sur_pair_data(moloch_surrogate_t* s, int first, int count, float* X, float* T);
 int moloch_sur_prepare(moloch_surrogate_t* s, double val_fraction, unsigned long long seed);
 int moloch_sur_train(moloch_surrogate_t* s, int iters, float lr, unsigned long long seed, float* train_loss,
                      float* val_loss);

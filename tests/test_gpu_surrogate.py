@@ -106,6 +106,52 @@ def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz, tuning):
     g.close()
 
 
+def _splitmix(seed, n):
+    """The collector's column sampler: splitmix64 draws."""
+    m = (1 << 64) - 1
+    st, out = seed, []
+    for _ in range(n):
+        st = (st + 0x9E3779B97F4A7C15) & m
+        z = st
+        z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+        z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+        out.append(z ^ (z >> 31))
+    return out
+
+
+@pytest.mark.parametrize("tuning", [[1, 0], [32, 24]])
+def test_sur_collected_pairs_match_oracle(gpu_lib, tuning):
+    """Training pairs of the first collected cycle against the feature
+    layout of the oracle and the increments of a twin domain run through
+    the same phases: bit for bit (the features are copies of state values,
+    the increments one FP32 subtraction)."""
+    from oracle import mlp_oracle as mo
+    jx, iy, kz, take, seed = 37, 29, 8, 96, 11
+    a = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    b = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    for g in (a, b):
+        g.setup_idealized(hills=((400.0, jx / 2, iy / 2, 3.0),), u0=5.0, v0=-3.0)
+        g.set_tuning(tuning)
+    sur = gpu_lib.Surrogate(kz, capacity=1024, batch=128)
+    n = sur.collect(a, 1, cols_per_cycle=take, seed=seed)
+    assert n == take * a.params.mo_nadv
+    X, T = sur.pair_data(0, take)
+    b.phase(0)
+    pre = _state(b)
+    b.phase(1)
+    post = _state(b)
+    cols = np.array([z % (jx * iy) for z in _splitmix(seed, take)])
+    assert np.array_equal(X, mo.features(pre)[cols].astype(np.float32))
+    def lv(st, f):  # the field's kz levels as FP32 (w: levels 2..kz+1)
+        return (st[f][1:kz + 1] if f == "w" else st[f]).astype(np.float32)
+    inc = np.stack([lv(post, f) - lv(pre, f) for f in STATE])  # [5][kz][iy][jx], FP32 differences
+    want = inc.reshape(5 * kz, iy * jx)[:, cols].T
+    assert np.array_equal(T, want)
+    sur.close()
+    a.close()
+    b.close()
+
+
 @pytest.mark.parametrize("tuning", [[1, 0], [32, 24]])
 def test_sur_fallback_is_bit_identical(gpu_lib, tuning):
     jx, iy, kz = 32, 24, 10
