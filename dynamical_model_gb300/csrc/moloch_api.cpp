@@ -270,6 +270,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.cur = 0;
   v.hz_levels = 1;
   v.kmarch = 0;
+  v.vfields = 1;
   v.sur_skip = nullptr;
   return off + 256;
 }
@@ -1116,8 +1117,11 @@ int moloch_gpu_profile_step(moloch_handle_t* h, double* ms_by_kind, int* launche
 static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
 // [0] horizontal WAF shape, [1] sound kernel variants (bit mask:
 // 1 divergence, 2 damping, 4 momentum k-marching; 8 momentum warp strips;
-// 16 divergence and damping fused in warp strips, which overrides 1 and 2)
-static const int kTuneCount = 2;
+// 16 divergence and damping fused in warp strips, which overrides 1 and 2),
+// [2] advected fields per thread of the vertical WAF (1, 2, 5, 10)
+static const int kTuneCount = 3;
+static const int kVFieldCandidates[4] = {1, 2, 5, 10};
+static bool valid_vfields(int f) { return f == 1 || f == 2 || f == 5 || f == 10; }
 
 int moloch_gpu_tuning_count(void) { return kTuneCount; }
 
@@ -1133,6 +1137,11 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     if (choice[1] < 0 || choice[1] > 31) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     h->vd.kmarch = choice[1];
     h->vf.kmarch = choice[1];
+  }
+  if (n > 2) {
+    if (!valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
+    h->vd.vfields = choice[2];
+    h->vf.vfields = choice[2];
   }
   for (int q = 0; q < 2; ++q) {  // launch shapes are baked into captured graphs
     if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
@@ -1198,11 +1207,35 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
     }
     if (tot < best1) { best1 = tot; pick1 = cand; }
   }
+  h->vd.kmarch = pick1;
+  h->vf.kmarch = pick1;
+  // vertical WAF: fields per thread, timed on advection()
+  double best2 = 1e30;
+  int pick2 = h->elem == 8 ? h->vd.vfields : h->vf.vfields;
+  for (int cand : kVFieldCandidates) {
+    h->vd.vfields = cand;
+    h->vf.vfields = cand;
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, h->stream);
+      int nk = h->elem == 8 ? launch_phase(h, h->vd, 2) : launch_phase(h, h->vf, 2);
+      h->kernels += nk;
+      cudaEventRecord(e1, h->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best2) { best2 = tot; pick2 = cand; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   choice[0] = pick;
   choice[1] = pick1;
-  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1 / 2.0; }
+  choice[2] = pick2;
+  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1 / 2.0; best_ms[2] = best2 / 2.0; }
   return moloch_gpu_set_tuning(h, choice, kTuneCount);
 }
 
@@ -1221,6 +1254,7 @@ struct moloch_ensemble {
   cudaGraphExec_t gexec[2] = {nullptr, nullptr};
   int hz_levels = 4;
   int kmarch = 0;
+  int vfields = 1;
   int cur = 0, fcur = 0;
   long long kernels = 0;
   int kernels_per_step = 0;
@@ -1254,7 +1288,7 @@ void ens_tiles(moloch_ensemble* e) {
     for (int y = 0; y < (ni + 3) / 4; ++y)
       for (int x = 0; x < tj; ++x) e->tiles[TK_COLUMN].push_back(make_int4(q, x, y, 0));
     for (int y = 0; y < (ni + 3) / 4; ++y)
-      for (int x = 0; x < tj * kNumAdvected; ++x) e->tiles[TK_VERTICAL].push_back(make_int4(q, x, y, 0));
+      for (int x = 0; x < tj * (kNumAdvected / e->vfields); ++x) e->tiles[TK_VERTICAL].push_back(make_int4(q, x, y, 0));
     for (int z = 0; z < (kz + kKC - 1) / kKC; ++z)
       for (int y = 0; y < (ni + 7) / 8; ++y)
         for (int x = 0; x < tj; ++x) e->tiles[TK_CHUNK].push_back(make_int4(q, x, y, z));
@@ -1296,6 +1330,7 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
         v.cur = cur;
         v.fcur = fc;
         v.hz_levels = e->hz_levels >= 16 ? e->hz_levels : std::min(e->hz_levels, v.kz);
+        v.vfields = e->vfields;
         v.bind_fields();
         hv[(size_t)(cur * 2 + fc) * n + q] = v;
       }
@@ -1310,6 +1345,7 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     b.ntiles[t] = (int)e->tiles[t].size();
     b.hstrip = e->hz_levels >= 16;
     b.kmarch = e->kmarch;
+    b.vfields = e->vfields;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
   return MOLOCH_OK;
@@ -1463,12 +1499,36 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
     }
     if (tot < best1) { best1 = tot; pick1 = cand; }
   }
+  e->kmarch = pick1;
+  // vertical WAF: fields per thread, timed on advection()
+  double best2 = 1e30;
+  int pick2 = e->vfields;
+  for (int cand : kVFieldCandidates) {
+    e->vfields = cand;
+    int rc = ens_build(e);
+    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, e->stream);
+      e->kernels += e->elem == 8 ? kfast::blaunch_advection(e->bd, e->stream, e->cur, e->fcur)
+                                 : kfast::blaunch_advection(e->bf, e->stream, e->cur, e->fcur);
+      cudaEventRecord(e1, e->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "ensemble autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best2) { best2 = tot; pick2 = cand; }
+  }
+  e->vfields = pick2;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  e->kmarch = pick1;
   choice[0] = pick;
   choice[1] = pick1;
-  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; }
+  choice[2] = pick2;
+  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; }
   ens_sync_members(e);
   return ens_build(e);
 }
@@ -1483,6 +1543,10 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
   if (nchoice > 1) {
     if (choice[1] < 0 || choice[1] > 31) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     e->kmarch = choice[1];
+  }
+  if (nchoice > 2) {
+    if (!valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
+    e->vfields = choice[2];
   }
   return ens_build(e);
 }

@@ -1284,74 +1284,100 @@ __device__ __forceinline__ float waf_vflux<float>(float s_k1, float dtrdz, float
   return (0.5f * s_k1) * fmaf(-zphi, d, x1 + x0);
 }
 
-// One thread per column and field.  Both passes stream k in registers:
-// pass 1 yields wz1(t) at step t, pass 2 consumes it two levels later, so
-// the intermediate field never leaves the SM.  The grid puts the field
-// index fastest, so the ten fields of one column tile run together and
-// share the s / metric loads through L2.
-template <class T>
+// One thread per column and F fields (F = 1, 2, 5 or 10: the tuned
+// View::vfields).  Both passes stream k in registers: pass 1 yields wz1(t)
+// at step t, pass 2 consumes it two levels later, so the intermediate field
+// never leaves the SM.  The fields of a thread share the loads of s, wafu,
+// wafd and the velocity-only terms of the fluxes (Courant number, its sign,
+// s/2, the metric term of the update), which the compiler computes once.
+// The grid puts the field group fastest, so the groups of one column tile
+// run together and share the s / metric loads through L2.
+template <class T, int F>
 __device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, const int by, const int bz) {
-  const int f = bx % kNumAdvected;
-  const int tj = bx / kNumAdvected;
+  constexpr int NG = kNumAdvected / F;
+  const int g = bx % NG;
+  const int tj = bx / NG;
   const int jj = tj * kColBX + threadIdx.x;
   const int ii = by * kColBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
   const size_t c = jj + (size_t)nj * ii;
-  const T* __restrict__ src = d.fset[d.fcur][f];
-  T* __restrict__ wz = d.wz + (size_t)f * pl * kz;
+  const T* src[F];
+  T* wz[F];
+#pragma unroll
+  for (int u = 0; u < F; ++u) {
+    src[u] = d.fset[d.fcur][g * F + u];
+    wz[u] = d.wz + (size_t)(g * F + u) * pl * kz;
+  }
   const T* __restrict__ s = d.s;
   const T* __restrict__ wafu = d.wafu;
   const T* __restrict__ wafd = d.wafd;
   const T dtrdz = d.dtrdz_a;
-  T xa = src[c], xb = xa, xc = src[c + pl];  // pass-1 window x(t-1), x(t), x(t+1)
-  T wfw1 = T(0), wfw2 = T(0);                // wfw1(t), wfw2(m)
-  T y0 = T(0), y1 = T(0), y2 = T(0), y3 = T(0);  // wz1(t-3 .. t)
+  T xa[F], xb[F], xc[F];               // pass-1 window x(t-1), x(t), x(t+1)
+  T wfw1[F], wfw2[F];                  // wfw1(t), wfw2(m)
+  T y0[F], y1[F], y2[F], y3[F];        // wz1(t-3 .. t)
+#pragma unroll
+  for (int u = 0; u < F; ++u) {
+    xa[u] = src[u][c]; xb[u] = xa[u]; xc[u] = src[u][c + pl];
+    wfw1[u] = T(0); wfw2[u] = T(0);
+    y0[u] = T(0); y1[u] = T(0); y2[u] = T(0); y3[u] = T(0);
+  }
   T sA = T(0), sB = T(0), sC = s[c], sD;    // s(t-2 .. t+1)
   T uA = T(0), uB = T(0), dA = T(0), dB = T(0);  // wafu/wafd at t-2, t-1
-  for (int t = 1; t <= kz + 2; ++t) {
-    T w1 = y3, uC = T(0), dC = T(0);
+  // one step t of both passes; FAST: 4 <= t <= kz-2, where no boundary
+  // case applies (t2 = t+2, both fluxes exist, ym = y0), so the tests drop
+  auto step = [&](const int t, auto fast) {
+    constexpr bool FAST = decltype(fast)::value;
+    T uC = T(0), dC = T(0);
     sD = T(0);
-    if (t <= kz) {
-      const size_t o = (size_t)(t - 1) * pl;
-      sD = s[c + (size_t)t * pl];
-      const int t2 = t + 2 <= kz ? t + 2 : kz;
-      const T xd = src[c + (size_t)(t2 - 1) * pl];
-      uC = wafu[c + o];
-      dC = wafd[c + o];
-      const T wfw1n = t <= kz - 1 ? waf_vflux(sD, dtrdz, xa, xb, xc, xd) : T(0);
-      w1 = ((xb - wfw1 * uC) + wfw1n * dC) + (sC * uC - sD * dC) * xb;
-      xa = xb; xb = xc; xc = xd; wfw1 = wfw1n;
-    }
-    y0 = y1; y1 = y2; y2 = y3; y3 = w1;  // for t > kz, wz1 stays clamped at wz1(kz)
     const int m = t - 2;
-    if (m >= 1) {
-      const T ym = m == 1 ? y1 : y0;
-      const T wfw2n = m <= kz - 1 ? waf_vflux(sB, dtrdz, ym, y1, y2, y3) : T(0);
-      wz[c + (size_t)(m - 1) * pl] = ((y1 - wfw2 * uA) + wfw2n * dA) + (sA * uA - sB * dA) * y1;
-      wfw2 = wfw2n;
+    if (FAST || t <= kz) {
+      sD = s[c + (size_t)t * pl];
+      uC = wafu[c + (size_t)(t - 1) * pl];
+      dC = wafd[c + (size_t)(t - 1) * pl];
+    }
+    const int t2 = FAST ? t + 2 : (t + 2 <= kz ? t + 2 : kz);
+#pragma unroll
+    for (int u = 0; u < F; ++u) {
+      T w1 = y3[u];
+      if (FAST || t <= kz) {
+        const T xd = src[u][c + (size_t)(t2 - 1) * pl];
+        const T wfw1n = (FAST || t <= kz - 1) ? waf_vflux(sD, dtrdz, xa[u], xb[u], xc[u], xd) : T(0);
+        w1 = ((xb[u] - wfw1[u] * uC) + wfw1n * dC) + (sC * uC - sD * dC) * xb[u];
+        xa[u] = xb[u]; xb[u] = xc[u]; xc[u] = xd; wfw1[u] = wfw1n;
+      }
+      y0[u] = y1[u]; y1[u] = y2[u]; y2[u] = y3[u]; y3[u] = w1;  // for t > kz, wz1 stays clamped at wz1(kz)
+      if (FAST || m >= 1) {
+        const T ym = (!FAST && m == 1) ? y1[u] : y0[u];
+        const T wfw2n = (FAST || m <= kz - 1) ? waf_vflux(sB, dtrdz, ym, y1[u], y2[u], y3[u]) : T(0);
+        wz[u][c + (size_t)(m - 1) * pl] = ((y1[u] - wfw2[u] * uA) + wfw2n * dA) + (sA * uA - sB * dA) * y1[u];
+        wfw2[u] = wfw2n;
+      }
     }
     sA = sB; sB = sC; sC = sD;
     uA = uB; uB = uC; dA = dB; dB = dC;
-  }
+  };
+  const int tf = kz - 2 >= 4 ? kz - 2 : 3;  // last step of the fast range
+  for (int t = 1; t <= 3; ++t) step(t, std::false_type());
+  for (int t = 4; t <= tf; ++t) step(t, std::true_type());
+  for (int t = tf + 1; t <= kz + 2; ++t) step(t, std::false_type());
 }
 
-template <class T>
+template <class T, int F>
 __global__ void __launch_bounds__(kColBX* kColBY) k_waf_vertical(View<T> d) {
-  b_waf_vertical<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
+  b_waf_vertical<T, F>(d, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
-template <class T>
+template <class T, int F>
 __global__ void __launch_bounds__(kColBX* kColBY)
     kb_waf_vertical(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
   __shared__ View<T> sv;
   const int4 t = tiles[blockIdx.x];
   copy_view(&sv, views + t.x);
   __syncthreads();
-  b_waf_vertical<T>(sv, t.y, t.z, t.w);
+  b_waf_vertical<T, F>(sv, t.y, t.z, t.w);
 }
-
 
 // ---- advection: meridional + zonal WAF (:1075-1187) ----------------------
 // Block = 32 (j) x 8 (i) output points of kHzLevels consecutive levels, ten
@@ -1959,14 +1985,40 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   return n;
 }
 
+// launch of the vertical WAF with the View's fields per thread
+template <class T>
+void launch_waf_vertical(const View<T>& d, cudaStream_t st) {
+  const int ng = kNumAdvected / d.vfields;
+  const dim3 vg(((d.nj + kColBX - 1) / kColBX) * ng, (d.ni + kColBY - 1) / kColBY), vb(kColBX, kColBY);
+  switch (d.vfields) {
+    case 2: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T, 2><<<vg, vb, 0, st>>>(d)); break;
+    case 5: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T, 5><<<vg, vb, 0, st>>>(d)); break;
+    case 10: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T, 10><<<vg, vb, 0, st>>>(d)); break;
+    default: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T, 1><<<vg, vb, 0, st>>>(d)); break;
+  }
+}
+
+template <class T>
+void blaunch_waf_vertical(const Batch<T>& b, const View<T>* views, cudaStream_t st) {
+  const int n = b.ntiles[TK_VERTICAL];
+  const int4* tl = b.tiles[TK_VERTICAL];
+  const dim3 vb(kColBX, kColBY);
+  switch (b.vfields) {
+    case 2: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T, 2><<<n, vb, 0, st>>>(views, tl)); break;
+    case 5: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T, 5><<<n, vb, 0, st>>>(views, tl)); break;
+    case 10: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T, 10><<<n, vb, 0, st>>>(views, tl)); break;
+    default: MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T, 1><<<n, vb, 0, st>>>(views, tl)); break;
+  }
+}
+
+
 // one advection() call; the advected fields move to the other buffer set
 template <class T>
 int launch_advection(View<T>& d, cudaStream_t st) {
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
-  const dim3 vg(((d.nj + kColBX - 1) / kColBX) * kNumAdvected, (d.ni + kColBY - 1) / kColBY);
   const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, (d.kz + d.hz_levels - 1) / d.hz_levels);
   MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pg, pb, 0, st>>>(d));
-  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, k_waf_vertical<T><<<vg, dim3(kColBX, kColBY), 0, st>>>(d));
+  launch_waf_vertical<T>(d, st);
   if (d.hz_levels >= 16) {  // warp strips of hz_levels rows
     const int nstrips = ((d.nj + kStripJ - 1) / kStripJ) * ((d.ni + d.hz_levels - 1) / d.hz_levels);
     MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_hstrip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d));
@@ -2017,12 +2069,11 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
   auto V = [&]() { return b.views[cur][fcur]; };
   const int4* PT = b.tiles[TK_POINT];
   const int4* CO = b.tiles[TK_COLUMN];
-  const int4* VE = b.tiles[TK_VERTICAL];
   const int4* HZ = b.tiles[TK_HORIZONTAL];
   const int4* KC = b.tiles[TK_CHUNK];
   const int nkc = b.ntiles[TK_CHUNK];
   const int npt = b.ntiles[TK_POINT], nco = b.ntiles[TK_COLUMN];
-  const int nve = b.ntiles[TK_VERTICAL], nhz = b.ntiles[TK_HORIZONTAL];
+  const int nhz = b.ntiles[TK_HORIZONTAL];
   MOLOCH_LAUNCH(KK_PREDIAG, st, kb_prediag<T><<<npt, pb, 0, st>>>(V(), PT, fl.filterpai, fl.filtertheta));
   ++n;
   for (int a = 0; a < fl.nadv; ++a) {
@@ -2060,7 +2111,7 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
       cur ^= 1;
     }
     MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<npt, pb, 0, st>>>(V(), PT));
-    MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T><<<nve, cb, 0, st>>>(V(), VE));
+    blaunch_waf_vertical<T>(b, V(), st);
     if (b.hstrip)
       MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_hstrip<T><<<nhz, 128, 0, st>>>(V(), HZ));
     else
@@ -2079,7 +2130,7 @@ template <class T>
 int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur) {
   const dim3 pb(kPtBX, kPtBY), cb(kColBX, kColBY), hb(32, 8);
   MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
-  MOLOCH_LAUNCH(KK_WAF_VERTICAL, st, kb_waf_vertical<T><<<b.ntiles[TK_VERTICAL], cb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_VERTICAL]));
+  blaunch_waf_vertical<T>(b, b.views[cur][fcur], st);
   if (b.hstrip)
     MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_hstrip<T><<<b.ntiles[TK_HORIZONTAL], 128, 0, st>>>(b.views[cur][fcur], b.tiles[TK_HORIZONTAL]));
   else

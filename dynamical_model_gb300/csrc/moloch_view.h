@@ -108,7 +108,8 @@ struct View {
   // launch shape chosen by the autotuner: levels per k_waf_horizontal block
   int hz_levels;
   int kmarch;      // sound kernel variants, bit mask: 1 divergence, 2 damping, 4 momentum
-                   // k-marching; 8 momentum as warp strips
+                   // k-marching; 8 momentum as warp strips; 16 divergence + damping fused
+  int vfields;     // advected fields per thread of k_waf_vertical: 1, 2, 5 or 10
 
   // set when a learned surrogate stands in for sound(): the plain sound
   // kernels return at once while *sur_skip == 1 (the surrogate's cycle was
@@ -172,6 +173,7 @@ struct Batch {
   int ntiles[TK_COUNT];
   int hstrip = 0;               // horizontal WAF as warp strips (tiles: member, block, level)
   int kmarch = 0;               // k-marching sound kernels on TK_CHUNK tiles (bit mask as View::kmarch)
+  int vfields = 1;              // fields per thread of the vertical WAF (TK_VERTICAL tiles follow it)
 };
 
 // launch counts per phase are returned by the launchers so the API can

@@ -193,7 +193,10 @@ const char* moloch_gpu_kernel_name(int kind);
  *               thread, next level prefetched), 8 momentum as warp strips
  *               (30 columns x 32 rows), 16 divergence and damping fused in
  *               one warp-strip kernel (29 columns x 32 rows; overrides 1
- *               and 2); 0 = one level per thread.
+ *               and 2); 0 = one level per thread;
+ *   choice[2] = advected fields per thread of the vertical WAF kernel:
+ *               1, 2, 5 or 10 (the fields of a thread share the velocity
+ *               loads and terms).
  * moloch_gpu_autotune runs advection() and sound() once per candidate and
  * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the

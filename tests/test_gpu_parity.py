@@ -269,6 +269,26 @@ def test_horizontal_waf_strips_match_tiles(gpu_lib, mode, tol, shape):
 
 
 @pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
+@pytest.mark.parametrize("fields", [2, 5, 10])
+def test_vertical_waf_fields_per_thread_match(gpu_lib, mode, tol, fields):
+    """The vertical WAF kernel with 2, 5 or 10 advected fields per thread
+    (shared velocity loads and terms) against one field per thread: the
+    same arithmetic per field, bit for bit in the exact build."""
+    a = gpu_lib.Moloch(45, 37, 11, mode=mode)
+    b = gpu_lib.Moloch(45, 37, 11, mode=mode)
+    for g in (a, b):
+        g.setup_idealized(hills=((400.0, 22.0, 18.0, 4.0),), u0=6.0, v0=-4.0)
+    a.set_tuning([1, 0, 1])
+    b.set_tuning([1, 0, fields])
+    for s in range(1, 4):
+        a.moloch(s)
+        b.moloch(s)
+    for n in PROG:
+        e = rel_l2(b.get(n), a.get(n))
+        assert e <= tol, (n, e)
+
+
+@pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
 @pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8), (9, 16), (13, 24), (10, 20)])
 def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz, variant):
     """The k-marching divergence/damping/momentum kernels (chunks of 4
