@@ -920,16 +920,37 @@ MOLOCH_KM_KERNELS(sound_momentum)
 
 
 // ---- momentum as warp strips (:730-837) -------------------------------------
-// One warp per strip of 30 output columns x R rows of one level (R =
-// d.hz_levels rows when the strips are chosen), lanes on columns j0-1 ..
-// j0+30.  West and east neighbours come from the lanes beside (shuffles),
-// the row below from the previous row kept in registers, the row above
-// (v at i+1) from the next row, which is loaded before the row is computed.
-// The stale-halo reads of the reference (edge buffers at j = 1, j = nj,
-// i = 1, i = ni) replace the neighbour values on those lanes and rows, as in
-// k_sound_momentum.
+// asynchronous global -> shared copies (cp.async, one element per lane)
 template <class T>
-__device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx, const int k, const int R) {
+__device__ __forceinline__ void cp_async_elem(T* dst_smem, const T* src) {
+  const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem));
+  if constexpr (sizeof(T) == 4)
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+// One warp per strip of 30 output columns x R rows of one level, lanes on
+// columns j0-1 .. j0+30.  West and east neighbours come from the lanes
+// beside (shuffles), the row below and the row above (v at i+1) from a ring
+// of kMomS row slots in shared memory: the six state arrays of a row (u, v,
+// tetav, pai, deltaw at k and k+1) are copied there with cp.async
+// kMomS - 3 rows ahead of the row computed, each lane copying and later
+// reading only its own column, so the pipeline needs no warp barrier and
+// holds no registers; the 2-D metric fields come one row ahead in
+// registers.  The stale-halo reads of the reference (edge buffers at
+// j = 1, j = nj, i = 1, i = ni) replace the neighbour values on those lanes
+// and rows, as in k_sound_momentum.
+constexpr int kMomS = 6;  // row slots: rows i-1, i, i+1 and three in flight
+template <class T>
+using MomRing = T[4][kMomS][6][32];  // [warp][slot][array][lane]
+
+template <class T>
+__device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx, const int k, const int R,
+                                                 MomRing<T>& ring) {
   if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nj = d.nj, ni = d.ni, pl = d.pl;
@@ -955,81 +976,124 @@ __device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx,
   const T gzh = d.gzitakh[k];
   const bool rot = d.rotllr;
   const int jm = wm1(jj, nj), jp = wp1(jj, nj);
-  // per-row inputs of this lane's column
-  struct Row { T u, v, t, p, d0, d1, vn, coru, corv, hx, hy, mu, mv; };
-  auto load = [&](int i, Row& x) {
+  T(*const rg)[6][32] = ring[wid];
+  // rows i_s-1 .. i_e stream through the slots in order; the slot indices
+  // rotate by one per row
+  auto nxt = [](int q) { return q + 1 == kMomS ? 0 : q + 1; };
+  auto issue = [&](int r, int q) {  // copies of row r into slot q (nothing past i_e); one group either way
+    if (r <= i_e) {
+      const size_t c = (size_t)jj + (size_t)nj * wrap2(r, ni);
+      T(*const sl)[32] = rg[q];
+      cp_async_elem(&sl[0][lane], u + c);
+      cp_async_elem(&sl[1][lane], v + c);
+      cp_async_elem(&sl[2][lane], tet + c);
+      cp_async_elem(&sl[3][lane], pai + c);
+      cp_async_elem(&sl[4][lane], dw0 + c);
+      cp_async_elem(&sl[5][lane], dw1 + c);
+    }
+    cp_async_commit();
+  };
+  // 2-D fields of a row, one row ahead in registers
+  struct Row2 { T coru, corv, hx, hy, mu, mv; };
+  auto load2 = [&](int i, Row2& x) {
     const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
-    const size_t cn = (size_t)jj + (size_t)nj * wrap2(i + 1, ni);
-    x.u = u[c]; x.v = v[c]; x.t = tet[c]; x.p = pai[c]; x.d0 = dw0[c]; x.d1 = dw1[c];
-    x.vn = v[cn];
     x.coru = d.coru[c]; x.corv = d.corv[c]; x.hx = d.hx[c]; x.hy = d.hy[c]; x.mu = d.mu[c];
     x.mv = rot ? T(0) : d.mv[c];
   };
-  // the row below the first row: u, tetav, pai, deltaw (k, k+1)
-  Row cur, nxt;
-  load(i_s - 1, cur);
-  T us = cur.u, ts = cur.t, ps = cur.p, ds0 = cur.d0, ds1 = cur.d1;
-  load(i_s, nxt);
-  for (int i = i_s; i < i_e; ++i) {
-    cur = nxt;
-    if (i + 1 < i_e) load(i + 1, nxt);
-    const int ii = i, ip = wp1(ii, ni), im = wm1(ii, ni);
+  for (int r = i_s - 1, q = 0; r <= i_s + kMomS - 3; ++r, ++q) issue(r, q);
+  Row2 c2, n2;
+  load2(i_s, n2);
+  // slots of rows i-1, i, i+1 and of the row issued next (i + kMomS - 2)
+  int qb = 0, qc = 1, qn = 2, qi = kMomS - 1;
+  // a strip that touches none of the domain edges (j = 1, nj; i = 1, ni)
+  // never reads the stale-halo edge buffers: its rows run a copy of the
+  // step without those tests
+  const bool interior = sj != 0 && sj != nsj - 1 && i_s != 0 && i_e != ni;
+  auto row = [&](const int i, auto edge) {
+    constexpr bool EDGE = decltype(edge)::value;
+    issue(i + kMomS - 2, qi);        // into the slot of row i-2
+    cp_async_wait<kMomS - 3>();      // rows up to i+1 have landed
+    c2 = n2;
+    if (i + 1 < i_e) load2(i + 1, n2);
+    const T(*const sb)[32] = rg[qb];
+    const T(*const sc)[32] = rg[qc];
+    const T(*const sn)[32] = rg[qn];
+    const T cu = sc[0][lane], cv = sc[1][lane], ct = sc[2][lane], cp = sc[3][lane];
+    const T cd0 = sc[4][lane], cd1 = sc[5][lane];
+    const T us = sb[0][lane], ts = sb[2][lane], ps = sb[3][lane], ds0 = sb[4][lane], ds1 = sb[5][lane];
+    const T vn = sn[1][lane];
+    const int ii = i;
     // neighbours from the lanes beside
-    const T ue = __shfl_down_sync(0xffffffffu, cur.u, 1);
+    const T ue = __shfl_down_sync(0xffffffffu, cu, 1);
     const T ues = __shfl_down_sync(0xffffffffu, us, 1);
-    const T vw = __shfl_up_sync(0xffffffffu, cur.v, 1);
-    const T vwn = __shfl_up_sync(0xffffffffu, cur.vn, 1);
-    const T tw = __shfl_up_sync(0xffffffffu, cur.t, 1);
-    const T pw = __shfl_up_sync(0xffffffffu, cur.p, 1);
-    const T dw0w = __shfl_up_sync(0xffffffffu, cur.d0, 1);
-    const T dw1w = __shfl_up_sync(0xffffffffu, cur.d1, 1);
+    const T vw = __shfl_up_sync(0xffffffffu, cv, 1);
+    const T vwn = __shfl_up_sync(0xffffffffu, vn, 1);
+    const T tw = __shfl_up_sync(0xffffffffu, ct, 1);
+    const T pw = __shfl_up_sync(0xffffffffu, cp, 1);
+    const T dw0w = __shfl_up_sync(0xffffffffu, cd0, 1);
+    const T dw1w = __shfl_up_sync(0xffffffffu, cd1, 1);
     if (out_lane) {
-      const T dw_c = cur.d0, dw_c1 = cur.d1;
-      const T tc = cur.t, pc = cur.p;
+      const T dw_c = cd0, dw_c1 = cd1;
+      const T tc = ct, pc = cp;
       // Equation 17
       {
-        const T zcx = dtrdx * cur.mu;
+        const T zcx = dtrdx * c2.mu;
         const T zfz = egdts + T(0.25) * (((dw0w + dw1w) + dw_c) + dw_c1);
         const T zrom1u = hcpd * (tw + tc);
-        const T vdc = cur.v;
-        const T vdw = jj == 0 ? d.ev_j[ii + (size_t)ni * k] : vw;
-        const T vdwn = jj == 0 ? d.ev_j[ip + (size_t)ni * k] : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * k] : vwn);
-        const T vdn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * k] : cur.vn;
-        const T zcor1u = ((cur.coru * dts) * T(0.25)) * (((vdc + vdw) + vdwn) + vdn);
-        const T paw = jj == 0 ? d.ep_j[ii + (size_t)ni * k] : pw;
-        uo[(size_t)jj + (size_t)nj * ii] = ((cur.u + zcor1u) - (zfz * cur.hx) * gzh) - (zcx * zrom1u) * (pc - paw);
+        const T vdc = cv;
+        T vdw = vw, vdwn = vwn, vdn = vn, paw = pw;
+        if (EDGE) {
+          const int ip = wp1(ii, ni);
+          vdw = jj == 0 ? d.ev_j[ii + (size_t)ni * k] : vw;
+          vdwn = jj == 0 ? d.ev_j[ip + (size_t)ni * k] : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * k] : vwn);
+          vdn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * k] : vn;
+          paw = jj == 0 ? d.ep_j[ii + (size_t)ni * k] : pw;
+        }
+        const T zcor1u = ((c2.coru * dts) * T(0.25)) * (((vdc + vdw) + vdwn) + vdn);
+        uo[(size_t)jj + (size_t)nj * ii] = ((cu + zcor1u) - (zfz * c2.hx) * gzh) - (zcx * zrom1u) * (pc - paw);
       }
       // Equation 18
       {
-        const T zcy = rot ? dtrdy : dtrdy * cur.mv;
+        const T zcy = rot ? dtrdy : dtrdy * c2.mv;
         const T zfz = egdts + T(0.25) * (((ds0 + ds1) + dw_c) + dw_c1);
         const T zrom1v = hcpd * (ts + tc);
-        const T udc = cur.u;
-        const T uds = ii == 0 ? d.eu_i[jj + (size_t)nj * k] : us;
-        const T ude = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * k] : ue;
-        const T udes = jj == nj - 1 ? d.eu_j[im + (size_t)ni * k] : (ii == 0 ? d.eu_i[jp + (size_t)nj * k] : ues);
-        const T zcor1v = ((cur.corv * dts) * T(0.25)) * (((udc + uds) + ude) + udes);
-        const T pas = ii == 0 ? d.ep_i[jj + (size_t)nj * k] : ps;
-        vo[(size_t)jj + (size_t)nj * ii] = ((cur.v - zcor1v) - (zfz * cur.hy) * gzh) - (zcy * zrom1v) * (pc - pas);
+        const T udc = cu;
+        T uds = us, ude = ue, udes = ues, pas = ps;
+        if (EDGE) {
+          const int im = wm1(ii, ni);
+          uds = ii == 0 ? d.eu_i[jj + (size_t)nj * k] : us;
+          ude = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * k] : ue;
+          udes = jj == nj - 1 ? d.eu_j[im + (size_t)ni * k] : (ii == 0 ? d.eu_i[jp + (size_t)nj * k] : ues);
+          pas = ii == 0 ? d.ep_i[jj + (size_t)nj * k] : ps;
+        }
+        const T zcor1v = ((c2.corv * dts) * T(0.25)) * (((udc + uds) + ude) + udes);
+        vo[(size_t)jj + (size_t)nj * ii] = ((cv - zcor1v) - (zfz * c2.hy) * gzh) - (zcy * zrom1v) * (pc - pas);
       }
     }
-    us = cur.u; ts = cur.t; ps = cur.p; ds0 = cur.d0; ds1 = cur.d1;
-  }
+    qb = qc; qc = qn; qn = nxt(qn); qi = nxt(qi);
+  };
+  if (interior)
+    for (int i = i_s; i < i_e; ++i) row(i, std::false_type());
+  else
+    for (int i = i_s; i < i_e; ++i) row(i, std::true_type());
+  cp_async_wait<0>();  // no copy outlives the kernel
 }
 
 template <class T>
-__global__ void __launch_bounds__(128) k_momentum_strip(View<T> d, int R) {
-  b_momentum_strip<T>(d, blockIdx.x, blockIdx.y, R);
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_momentum_strip(View<T> d, int R) {
+  __shared__ __align__(16) MomRing<T> ring;
+  b_momentum_strip<T>(d, blockIdx.x, blockIdx.y, R, ring);
 }
 
 template <class T>
 __global__ void __launch_bounds__(128)
     kb_momentum_strip(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int R) {
   __shared__ View<T> sv;
+  __shared__ __align__(16) MomRing<T> ring;
   const int4 t = tiles[blockIdx.x];
   copy_view(&sv, views + t.x);
   __syncthreads();
-  b_momentum_strip<T>(sv, t.y, t.z, R);
+  b_momentum_strip<T>(sv, t.y, t.z, R, ring);
 }
 
 // ---- divergence + divdamp as warp strips (:514-597, :853-895, :627-630) ---
