@@ -88,6 +88,7 @@ _PROTOS = {
     "moloch_gpu_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_kernel_kinds": (ctypes.c_int, []),
+    "moloch_gpu_host_direct": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "moloch_gpu_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
     "moloch_gpu_tuning_count": (ctypes.c_int, []),
     "moloch_gpu_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
@@ -287,6 +288,19 @@ class Moloch:
     @property
     def stream(self):
         return self.L.moloch_gpu_stream(self.h)
+
+    @property
+    def host_direct(self):
+        """True when uploads read the host arrays with a kernel through the
+        host page tables (see moloch_gpu_host_direct)."""
+        rc = self.L.moloch_gpu_host_direct(self.h, -1)
+        _check(min(rc, 0))
+        return bool(rc)
+
+    @host_direct.setter
+    def host_direct(self, enable):
+        rc = self.L.moloch_gpu_host_direct(self.h, 1 if enable else 0)
+        _check(min(rc, 0))
 
     @property
     def kernel_count(self):

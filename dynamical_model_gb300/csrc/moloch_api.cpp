@@ -203,6 +203,10 @@ struct moloch_handle {
   // host copies of the static inputs (dense interiors)
   std::vector<double> zeta, fmz, fmzf, msfx, msfu, msfv, hx, hy, ulat, vlat, zita, zitah;
   unsigned uploaded = 0;  // bit per field id
+  // uploads of prognostic fields by kernels that read the caller's host
+  // arrays through the host page tables (-1: not decided yet, 0: pinned
+  // staging and host threads, 1: direct)
+  int host_direct = -1;
   // attached acoustic-cycle surrogate (FP32 storage only): each sound()
   // call first runs the surrogate; the plain substeps skip on acceptance
   moloch::mlp::Surrogate* sur = nullptr;
@@ -392,6 +396,40 @@ int download_streamed(moloch_handle* h, const T* src, const FieldShape& s, int n
       }
     });
   }
+  return MOLOCH_OK;
+}
+
+// Direct uploads need the device to read pageable host memory through the
+// host page tables (NVLink-C2C on GB300).  Downloads and the output path
+// stay staged: a kernel writing into host pages the caller has not touched
+// yet (a fresh array) takes a page fault per page (measured 32 ms for a
+// 125 MB field against 4 ms staged), and the output copy overlaps the next
+// steps anyway.
+bool use_direct(moloch_handle* h) {
+  if (h->host_direct < 0) {
+    int dev = 0, pma = 0, pt = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev);
+    cudaDeviceGetAttribute(&pt, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev);
+    h->host_direct = (pma && pt) ? 1 : 0;
+  }
+  return h->host_direct == 1;
+}
+
+// interior of a Fortran-layout field into the dense device copy, read by a
+// kernel straight from the caller's array; returns when the kernel is done
+// (the caller may change the array afterwards)
+template <class T>
+int upload_direct(moloch_handle* h, T* dst, const double* base, const FieldShape& s, int nj, int ni, int nk,
+                  int level4) {
+  const long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1;
+  const long n3 = s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1;
+  const long A = (long)level4 * n1 * n2 * n3 + (s.ndim >= 3 ? (1 - s.lb[2]) * n1 * n2 : 0) +
+                 (s.ndim >= 2 ? (1 - s.lb[1]) * n1 : 0) + (1 - s.lb[0]);
+  const long P = s.ndim >= 3 ? n1 * n2 : 0, Rw = s.ndim >= 2 ? n1 : 0;
+  moloch::init::launch_upload_direct<T>(dst, base, A, P, Rw, nj, ni, nk, h->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
   return MOLOCH_OK;
 }
 
@@ -757,27 +795,41 @@ int moloch_gpu_upload(moloch_handle_t* h, int field, const double* host_base, co
     if (h->initialized) h->initialized = false;  // statics changed: init again
     return MOLOCH_OK;
   }
+  const bool direct = use_direct(h);
+  auto up = [&](int f, int level4) -> int {
+    if (h->elem == 8) {
+      double* p = field_ptr(h->vd, f);
+      if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", f);
+      return direct ? upload_direct<double>(h, p, host_base, s, nj, ni, nk, level4)
+                    : upload_streamed<double>(h, p, host_base, s, nj, ni, nk, level4);
+    }
+    float* p = field_ptr(h->vf, f);
+    if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", f);
+    return direct ? upload_direct<float>(h, p, host_base, s, nj, ni, nk, level4)
+                  : upload_streamed<float>(h, p, host_base, s, nj, ni, nk, level4);
+  };
   if (field == MOLOCH_F_QX) {
     for (int n = 0; n < 5; ++n) {
-      int rc = h->elem == 8 ? upload_streamed<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), host_base, s, nj, ni, nk, n)
-                            : upload_streamed<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), host_base, s, nj, ni, nk, n);
+      int rc = up(MOLOCH_F_QV + n, n);
       if (rc) return rc;
       h->uploaded |= 1u << (MOLOCH_F_QV + n);
     }
     return MOLOCH_OK;
   }
-  int rc;
-  if (h->elem == 8) {
-    double* p = field_ptr(h->vd, field);
-    if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", field);
-    rc = upload_streamed<double>(h, p, host_base, s, nj, ni, nk, 0);
-  } else {
-    float* p = field_ptr(h->vf, field);
-    if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", field);
-    rc = upload_streamed<float>(h, p, host_base, s, nj, ni, nk, 0);
-  }
+  const int rc = up(field, 0);
   if (!rc) h->uploaded |= 1u << field;
   return rc;
+}
+
+int moloch_gpu_host_direct(moloch_handle_t* h, int enable) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  if (enable >= 0) {
+    h->host_direct = -1;
+    const bool can = use_direct(h);
+    h->host_direct = (enable && can) ? 1 : 0;
+  }
+  return use_direct(h) ? 1 : 0;
 }
 
 int moloch_gpu_init(moloch_handle_t* h) {
@@ -896,18 +948,18 @@ int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base, const 
     scatter_periodic(*st, s, nj, ni, nk, 0, host_base);
     return MOLOCH_OK;
   }
+  auto down = [&](int f, int k, int level4) -> int {
+    return h->elem == 8 ? download_streamed<double>(h, field_ptr(h->vd, f), s, nj, ni, k, level4, host_base)
+                        : download_streamed<float>(h, field_ptr(h->vf, f), s, nj, ni, k, level4, host_base);
+  };
   if (field == MOLOCH_F_QX) {
     for (int n = 0; n < 5; ++n) {
-      int rc = h->elem == 8
-                   ? download_streamed<double>(h, field_ptr(h->vd, MOLOCH_F_QV + n), s, nj, ni, kz, n, host_base)
-                   : download_streamed<float>(h, field_ptr(h->vf, MOLOCH_F_QV + n), s, nj, ni, kz, n, host_base);
+      int rc = down(MOLOCH_F_QV + n, kz, n);
       if (rc) return rc;
     }
     return MOLOCH_OK;
   }
-  int rc = h->elem == 8 ? download_streamed<double>(h, field_ptr(h->vd, field), s, nj, ni, nk, 0, host_base)
-                        : download_streamed<float>(h, field_ptr(h->vf, field), s, nj, ni, nk, 0, host_base);
-  return rc;
+  return down(field, nk, 0);
 }
 
 // Output path (the fields the reference driver writes every iout steps,
@@ -949,9 +1001,9 @@ int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb
     if (t_host && (t_lb[d] != st.lb[d] || t_ub[d] != st.ub[d])) return fail(MOLOCH_ERR_BOUNDS, "output t bounds");
   for (int d = 0; d < sp.ndim; ++d)
     if (ps_host && (ps_lb[d] != sp.lb[d] || ps_ub[d] != sp.ub[d])) return fail(MOLOCH_ERR_BOUNDS, "output ps bounds");
+  const size_t pl = (size_t)nj * ni, n3 = pl * kz;
   CUDA_TRY(cudaEventSynchronize(h->out_done));
   h->out_pending = false;
-  const size_t pl = (size_t)nj * ni, n3 = pl * kz;
   auto scatter = [&](const FieldShape& s, int nk, size_t off, double* base) {
     const long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ub[1] - s.lb[1] + 1;
     const int i1 = s.lb[1], nrow_i = s.ub[1] - s.lb[1] + 1;

@@ -12,6 +12,7 @@
 // state t, pai, qv written directly in the bulk type.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "moloch_constants.h"
@@ -181,6 +182,32 @@ int launch_fill(T* p, size_t n, double value, cudaStream_t st) {
   k_fill<T><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(p, n, (T)value);
   return 1;
 }
+
+// ---- direct host uploads ------------------------------------------------------
+// One thread per element, grid-stride; consecutive threads take consecutive
+// j, so the host array is read in whole rows.  Bound by the host link (about
+// 200 GB/s on GB300), not by the SMs.
+template <class T>
+__global__ void k_upload_direct(T* __restrict__ dst, const double* __restrict__ src, long A, long P, long Rw, int nj,
+                                int ni, size_t n) {
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = e / (size_t)nj;
+    const int j = (int)(e - r * nj);
+    const long kk = (long)(r / (size_t)ni), i = (long)(r - (size_t)kk * ni);
+    dst[e] = (T)src[A + kk * P + i * Rw + j];
+  }
+}
+
+template <class T>
+int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st) {
+  const size_t n = (size_t)nj * ni * nk;
+  const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
+  k_upload_direct<T><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(dst, src, A, P, Rw, nj, ni, n);
+  return 1;
+}
+
+template int launch_upload_direct<double>(double*, const double*, long, long, long, int, int, int, cudaStream_t);
+template int launch_upload_direct<float>(float*, const double*, long, long, long, int, int, int, cudaStream_t);
 
 template int launch_fill<double>(double*, size_t, double, cudaStream_t);
 template int launch_fill<float>(float*, size_t, double, cudaStream_t);

@@ -42,5 +42,12 @@ int launch_ideal(const IdealArgs& a, const double* zita, const double* zitah, do
                  double* fmzf, double* hx, double* hy, double* ulat, double* vlat, T* t, T* pai, T* qv,
                  cudaStream_t st);
 template <class T> int launch_fill(T* p, size_t n, double value, cudaStream_t st);
+
+// Direct host uploads: a kernel that reads the caller's host array through
+// the host page tables (NVLink-C2C; the device reports pageable memory
+// access): dst[(kk*ni + i)*nj + j] = src[A + kk*P + i*Rw + j], the interior
+// of a Fortran-layout array (0-based kk < nk, i < ni, j < nj) in the bulk type.
+template <class T>
+int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st);
 }  // namespace init
 }  // namespace moloch

@@ -147,6 +147,20 @@ int moloch_gpu_run(moloch_handle_t* h, int nsteps, int use_graph);
 int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base,
                         const int* lb, const int* ub);
 
+/* How moloch_gpu_upload moves prognostic fields from the caller's host
+ * arrays to the device.  Direct (1): a kernel reads the host array itself
+ * through the host page tables (NVLink-C2C on GB300, about 185 GB/s: 0.7 ms
+ * for a 512x512x60 FP64 field against 1.8 ms staged), gathering the
+ * interior and converting to the bulk type on the device; the upload
+ * returns once the kernel is done.  Staged (0): host threads convert level
+ * chunks into pinned staging that cudaMemcpyAsync moves.  Direct is the
+ * default where the device reports pageable memory access with host page
+ * tables.  Downloads and the output path are always staged (a kernel
+ * writing into host pages not yet touched takes a page fault per page).
+ * enable: 1 use direct when supported, 0 staged, -1 only query.  Returns
+ * the mode in effect (0 or 1) or a negative error. */
+int moloch_gpu_host_direct(moloch_handle_t* h, int enable);
+
 /* Output path (nompi/regcm_dynamical_core.F90:203-216 writes t and ps
  * every iout steps).  output_start snapshots t and ps on the device in
  * stream order (after the steps already issued) and starts their copy to

@@ -172,9 +172,14 @@ def test_cfl_violation_is_reported(gpu_lib):
     assert ei.value.code == 4
 
 
-def test_upload_download_roundtrip_and_bounds(gpu_lib):
+@pytest.mark.parametrize("direct", [True, False])
+def test_upload_download_roundtrip_and_bounds(gpu_lib, direct):
+    """Host arrays with halo rings through upload and download, with direct
+    (a kernel reading the host arrays) and staged uploads."""
     g = gpu_lib.Moloch(12, 10, 6)
     g.setup_idealized()
+    g.host_direct = direct
+    assert g.host_direct == direct or not direct
     rng = np.random.default_rng(0)
     for name in ("u", "v", "w", "pai", "t", "qv", "qc", "qi", "qr", "qs"):
         a = g.download(name)
@@ -217,6 +222,34 @@ def test_output_path_overlaps_steps(gpu_lib, mode):
         assert np.array_equal(a.get(n), b.get(n)), n
     with pytest.raises(gpu_lib.MolochError):
         a.output_finish()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
+def test_direct_and_staged_transfers_agree(gpu_lib, mode):
+    """Uploads through the direct path (a kernel reading the host arrays)
+    and the staged path give identical device states: identical downloads
+    (halo rings included) and identical steps afterwards."""
+    if not gpu_lib.Moloch(8, 8, 4).host_direct:
+        pytest.skip("device without pageable host memory access")
+    a = gpu_lib.Moloch(37, 29, 9, mode=mode)
+    b = gpu_lib.Moloch(37, 29, 9, mode=mode)
+    for g in (a, b):
+        g.setup_idealized(hills=((300.0, 18.0, 14.0, 4.0),), u0=3.0)
+        g.run(2, graph=True)
+    a.host_direct = True
+    b.host_direct = False
+    names = ("u", "v", "w", "pai", "t", "qx", "ps", "tetav", "p", "rho", "qsat")
+    for n in names:
+        da, db = a.download(n), b.download(n)
+        assert np.array_equal(da, db), n
+    for n in ("u", "v", "w", "pai", "t", "qx"):
+        host = a.download(n) * (1.0 + 1e-3)  # a state the device does not hold yet
+        a.upload(n, host)
+        b.upload(n, host)
+    for g in (a, b):
+        g.run(1, graph=True)
+    for n in names:
+        assert np.array_equal(a.download(n), b.download(n)), n
 
 
 @pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
