@@ -266,9 +266,21 @@ def e2e_steps(torch, dm, d, stream, steps):
     loop does it: every step uploads the prognostic state (u, v, w, pai, t,
     qx), runs one moloch() call and reads back the output fields t and ps
     (the fields the reference driver writes, regcm_dynamical_core.F90:203-216)
-    with the asynchronous output path, whose copy overlaps the next step."""
+    with the asynchronous output path, whose copy overlaps the next step.
+    The host arrays are registered (pinned) once before the loop, as a
+    driver does with its module arrays: each upload is then a DMA that
+    overlaps the step still running."""
     names_in = ("u", "v", "w", "pai", "t", "qx")
     host = {n: d.download(n) for n in names_in}
+    for n in names_in:
+        d.host_register(host[n])
+    # one untimed iteration: the upload staging buffers are allocated on
+    # first use
+    for n in names_in:
+        d.upload(n, host[n])
+    d.moloch(1)
+    d.output_start()
+    d.output_finish()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     d.sync()
@@ -286,6 +298,8 @@ def e2e_steps(torch, dm, d, stream, steps):
     e1.record(stream)
     e1.synchronize()
     wall = time.perf_counter() - t0
+    for n in names_in:
+        d.host_unregister(host[n])
     h2d = sum(host[n].nbytes for n in names_in)
     d2h = out[0].nbytes + out[1].nbytes
     return max(e0.elapsed_time(e1), 1e3 * wall), h2d, d2h
@@ -581,8 +595,8 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
         ms_e2e = reduce_max(dist, ms_e2e, device)
         e2e = {"value": n_dom * gp * n_e2e / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": n_e2e,
-               "path": "moloch_gpu_upload(u,v,w,pai,t,qx) + moloch_gpu_step + moloch_gpu_output_start/finish(t,ps), "
-                       "FP64 host arrays, FP32 + surrogate handle"}
+               "path": "moloch_gpu_upload(u,v,w,pai,t,qx) from registered (pinned) FP64 host arrays + "
+                       "moloch_gpu_step + moloch_gpu_output_start/finish(t,ps), FP32 + surrogate handle"}
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:

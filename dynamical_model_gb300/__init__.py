@@ -89,6 +89,8 @@ _PROTOS = {
                                                ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_kernel_kinds": (ctypes.c_int, []),
     "moloch_gpu_host_direct": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "moloch_gpu_host_register": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t]),
+    "moloch_gpu_host_unregister": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "moloch_gpu_kernel_name": (ctypes.c_char_p, [ctypes.c_int]),
     "moloch_gpu_tuning_count": (ctypes.c_int, []),
     "moloch_gpu_autotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
@@ -219,6 +221,7 @@ class Moloch:
         _check(self.L.moloch_gpu_create(ctypes.byref(self.grid), ctypes.byref(self.params),
                                         ctypes.c_void_p(stream) if stream else None, ctypes.byref(h)))
         self.h = h
+        self._pinned = {}  # registered host arrays, kept alive while pinned
 
     # -- init_moloch ----------------------------------------------------------
     def setup_idealized(self, hills=(), pert_amp=0.5, pert_levels=10, seed=1234, u0=1.0, v0=1.0, device=False):
@@ -302,6 +305,17 @@ class Moloch:
         rc = self.L.moloch_gpu_host_direct(self.h, 1 if enable else 0)
         _check(min(rc, 0))
 
+    def host_register(self, arr):
+        """Pin a host array that will be uploaded repeatedly: its uploads
+        become DMA copies overlapping the steps already issued.  The array
+        is kept alive until host_unregister or close."""
+        _check(self.L.moloch_gpu_host_register(self.h, arr.ctypes.data, arr.nbytes))
+        self._pinned[arr.ctypes.data] = arr
+
+    def host_unregister(self, arr):
+        _check(self.L.moloch_gpu_host_unregister(self.h, arr.ctypes.data))
+        self._pinned.pop(arr.ctypes.data, None)
+
     @property
     def kernel_count(self):
         return self.L.moloch_gpu_kernel_count(self.h)
@@ -350,8 +364,9 @@ class Moloch:
 
     def close(self):
         if getattr(self, "h", None):
-            self.L.moloch_gpu_destroy(self.h)
+            self.L.moloch_gpu_destroy(self.h)  # also unregisters the pinned arrays
             self.h = None
+            self._pinned = {}
 
     def __del__(self):
         try:

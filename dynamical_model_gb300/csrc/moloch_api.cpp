@@ -207,6 +207,20 @@ struct moloch_handle {
   // arrays through the host page tables (-1: not decided yet, 0: pinned
   // staging and host threads, 1: direct)
   int host_direct = -1;
+  // direct uploads run on their own stream into a device staging copy of
+  // the field, so they overlap the steps already issued; a device copy on
+  // the step stream then commits the field in stream order.  Per field id:
+  // staging buffer, "read done" event (upload stream), "committed" event
+  // (step stream, after which the staging buffer may be refilled)
+  cudaStream_t up_stream = nullptr;
+  void* up_stage[MOLOCH_F_COUNT] = {};
+  size_t up_stage_bytes[MOLOCH_F_COUNT] = {};
+  // host ranges the caller registered (pinned): uploads from them are DMA
+  // copies of the whole Fortran array into an FP64 staging buffer on the
+  // upload stream, then a gather/convert kernel on the step stream
+  std::vector<std::pair<const char*, size_t>> pinned;
+  cudaEvent_t up_read[MOLOCH_F_COUNT] = {};
+  cudaEvent_t up_commit[MOLOCH_F_COUNT] = {};
   // attached acoustic-cycle surrogate (FP32 storage only): each sound()
   // call first runs the surrogate; the plain substeps skip on acceptance
   moloch::mlp::Surrogate* sur = nullptr;
@@ -416,20 +430,64 @@ bool use_direct(moloch_handle* h) {
   return h->host_direct == 1;
 }
 
-// interior of a Fortran-layout field into the dense device copy, read by a
-// kernel straight from the caller's array; returns when the kernel is done
-// (the caller may change the array afterwards)
+// interior of a Fortran-layout field into the dense device copy: a kernel
+// on the upload stream reads the caller's array into the field's staging
+// buffer (concurrently with the steps already issued on the step stream),
+// then the step stream copies the staging buffer into the field after the
+// work issued before.  Returns when the kernel is done (the caller may
+// change the array afterwards).  fid: field id of the staging slot.
+bool is_pinned(const moloch_handle* h, const void* p, size_t bytes) {
+  const char* a = (const char*)p;
+  for (const auto& r : h->pinned)
+    if (a >= r.first && a + bytes <= r.first + r.second) return true;
+  return false;
+}
+
 template <class T>
-int upload_direct(moloch_handle* h, T* dst, const double* base, const FieldShape& s, int nj, int ni, int nk,
+int upload_direct(moloch_handle* h, int fid, T* dst, const double* base, const FieldShape& s, int nj, int ni, int nk,
                   int level4) {
   const long n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1;
   const long n3 = s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1;
-  const long A = (long)level4 * n1 * n2 * n3 + (s.ndim >= 3 ? (1 - s.lb[2]) * n1 * n2 : 0) +
-                 (s.ndim >= 2 ? (1 - s.lb[1]) * n1 : 0) + (1 - s.lb[0]);
+  const long off4 = (long)level4 * n1 * n2 * n3;
+  const long A = (s.ndim >= 3 ? (1 - s.lb[2]) * n1 * n2 : 0) + (s.ndim >= 2 ? (1 - s.lb[1]) * n1 : 0) + (1 - s.lb[0]);
   const long P = s.ndim >= 3 ? n1 * n2 : 0, Rw = s.ndim >= 2 ? n1 : 0;
-  moloch::init::launch_upload_direct<T>(dst, base, A, P, Rw, nj, ni, nk, h->stream);
+  const size_t slice = sizeof(double) * (size_t)n1 * n2 * n3;  // the host array of this field (one tracer)
+  const double* src = base + off4;
+  const bool dma = is_pinned(h, src, slice);
+  const size_t bytes = dma ? slice : sizeof(T) * (size_t)nj * ni * nk;
+  if (!h->up_stream) {  // highest priority: its few blocks slip in between the blocks of running steps
+    int lo = 0, hi = 0;
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CUDA_TRY(cudaStreamCreateWithPriority(&h->up_stream, cudaStreamNonBlocking, hi));
+  }
+  if (!h->up_read[fid]) {
+    CUDA_TRY(cudaEventCreateWithFlags(&h->up_read[fid], cudaEventDisableTiming));
+    CUDA_TRY(cudaEventCreateWithFlags(&h->up_commit[fid], cudaEventDisableTiming));
+    CUDA_TRY(cudaEventRecord(h->up_commit[fid], h->stream));
+  }
+  if (h->up_stage_bytes[fid] < bytes) {
+    CUDA_TRY(cudaStreamWaitEvent(h->up_stream, h->up_commit[fid], 0));
+    CUDA_TRY(cudaStreamSynchronize(h->up_stream));
+    if (h->up_stage[fid]) CUDA_TRY(cudaFree(h->up_stage[fid]));
+    CUDA_TRY(cudaMalloc(&h->up_stage[fid], bytes));
+    h->up_stage_bytes[fid] = bytes;
+  }
+  // the previous commit of this field has read the staging buffer
+  CUDA_TRY(cudaStreamWaitEvent(h->up_stream, h->up_commit[fid], 0));
+  if (dma) {  // copy engine: the Fortran array as it is; gather/convert on the step stream
+    CUDA_TRY(cudaMemcpyAsync(h->up_stage[fid], src, slice, cudaMemcpyHostToDevice, h->up_stream));
+    CUDA_TRY(cudaEventRecord(h->up_read[fid], h->up_stream));
+    CUDA_TRY(cudaStreamWaitEvent(h->stream, h->up_read[fid], 0));
+    moloch::init::launch_upload_direct<T>(dst, (const double*)h->up_stage[fid], A, P, Rw, nj, ni, nk, h->stream, true);
+  } else {  // a small kernel reads the host array through the host page tables
+    moloch::init::launch_upload_direct<T>((T*)h->up_stage[fid], src, A, P, Rw, nj, ni, nk, h->up_stream, false);
+    CUDA_TRY(cudaEventRecord(h->up_read[fid], h->up_stream));
+    CUDA_TRY(cudaStreamWaitEvent(h->stream, h->up_read[fid], 0));
+    CUDA_TRY(cudaMemcpyAsync(dst, h->up_stage[fid], bytes, cudaMemcpyDeviceToDevice, h->stream));
+  }
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  CUDA_TRY(cudaEventRecord(h->up_commit[fid], h->stream));
+  CUDA_TRY(cudaEventSynchronize(h->up_read[fid]));
   return MOLOCH_OK;
 }
 
@@ -795,17 +853,21 @@ int moloch_gpu_upload(moloch_handle_t* h, int field, const double* host_base, co
     if (h->initialized) h->initialized = false;  // statics changed: init again
     return MOLOCH_OK;
   }
-  const bool direct = use_direct(h);
+  const long nall = (long)(s.ub[0] - s.lb[0] + 1) * (s.ndim >= 2 ? s.ub[1] - s.lb[1] + 1 : 1) *
+                    (s.ndim >= 3 ? s.ub[2] - s.lb[2] + 1 : 1);
+  // registered (pinned) host arrays always go by DMA; others by the direct
+  // kernel where the device can read pageable memory, else staged
+  const bool direct = use_direct(h) || is_pinned(h, host_base, sizeof(double) * nall * (field == MOLOCH_F_QX ? 5 : 1));
   auto up = [&](int f, int level4) -> int {
     if (h->elem == 8) {
       double* p = field_ptr(h->vd, f);
       if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", f);
-      return direct ? upload_direct<double>(h, p, host_base, s, nj, ni, nk, level4)
+      return direct ? upload_direct<double>(h, f, p, host_base, s, nj, ni, nk, level4)
                     : upload_streamed<double>(h, p, host_base, s, nj, ni, nk, level4);
     }
     float* p = field_ptr(h->vf, f);
     if (!p) return fail(MOLOCH_ERR_ARG, "field %d cannot be uploaded", f);
-    return direct ? upload_direct<float>(h, p, host_base, s, nj, ni, nk, level4)
+    return direct ? upload_direct<float>(h, f, p, host_base, s, nj, ni, nk, level4)
                   : upload_streamed<float>(h, p, host_base, s, nj, ni, nk, level4);
   };
   if (field == MOLOCH_F_QX) {
@@ -819,6 +881,28 @@ int moloch_gpu_upload(moloch_handle_t* h, int field, const double* host_base, co
   const int rc = up(field, 0);
   if (!rc) h->uploaded |= 1u << field;
   return rc;
+}
+
+int moloch_gpu_host_register(moloch_handle_t* h, const void* ptr, size_t bytes) {
+  g_err.clear();
+  if (!h || !ptr || !bytes) return fail(MOLOCH_ERR_ARG, "null argument");
+  if (is_pinned(h, ptr, bytes)) return MOLOCH_OK;
+  CUDA_TRY(cudaHostRegister(const_cast<void*>(ptr), bytes, cudaHostRegisterDefault));
+  h->pinned.emplace_back((const char*)ptr, bytes);
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_host_unregister(moloch_handle_t* h, const void* ptr) {
+  g_err.clear();
+  if (!h || !ptr) return fail(MOLOCH_ERR_ARG, "null argument");
+  for (size_t q = 0; q < h->pinned.size(); ++q)
+    if (h->pinned[q].first == (const char*)ptr) {
+      if (h->up_stream) CUDA_TRY(cudaStreamSynchronize(h->up_stream));  // no copy from it in flight
+      CUDA_TRY(cudaHostUnregister(const_cast<void*>(ptr)));
+      h->pinned.erase(h->pinned.begin() + q);
+      return MOLOCH_OK;
+    }
+  return fail(MOLOCH_ERR_ARG, "range not registered with this handle");
 }
 
 int moloch_gpu_host_direct(moloch_handle_t* h, int enable) {
@@ -1661,6 +1745,16 @@ int moloch_gpu_destroy(moloch_handle_t* h) {
   if (h->out_done) cudaEventDestroy(h->out_done);
   for (int q = 0; q < 2; ++q)
     if (h->stage_ev[q]) cudaEventDestroy(h->stage_ev[q]);
+  if (h->up_stream) {
+    cudaStreamSynchronize(h->up_stream);
+    cudaStreamDestroy(h->up_stream);
+  }
+  for (const auto& r : h->pinned) cudaHostUnregister(const_cast<char*>(r.first));
+  for (int f = 0; f < MOLOCH_F_COUNT; ++f) {
+    if (h->up_stage[f]) cudaFree(h->up_stage[f]);
+    if (h->up_read[f]) cudaEventDestroy(h->up_read[f]);
+    if (h->up_commit[f]) cudaEventDestroy(h->up_commit[f]);
+  }
   if (h->own_stream) cudaStreamDestroy(h->stream);
   delete h;
   return MOLOCH_OK;

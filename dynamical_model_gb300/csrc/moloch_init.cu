@@ -184,30 +184,51 @@ int launch_fill(T* p, size_t n, double value, cudaStream_t st) {
 }
 
 // ---- direct host uploads ------------------------------------------------------
-// One thread per element, grid-stride; consecutive threads take consecutive
-// j, so the host array is read in whole rows.  Bound by the host link (about
-// 200 GB/s on GB300), not by the SMs.
+// One block of 128 threads per SM, each thread with eight independent host
+// reads in flight (about 1.2 MB across the GPU, enough for the host link,
+// about 200 GB/s on GB300): the kernel runs beside the steps it overlaps
+// while taking 4 of the 64 warp slots of an SM.  Consecutive threads take
+// consecutive j, so the host array is read in whole rows.
+constexpr int kUpUnroll = 8;
+
 template <class T>
-__global__ void k_upload_direct(T* __restrict__ dst, const double* __restrict__ src, long A, long P, long Rw, int nj,
-                                int ni, size_t n) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < n; e += (size_t)gridDim.x * blockDim.x) {
+__global__ void __launch_bounds__(128) k_upload_direct(T* __restrict__ dst, const double* __restrict__ src, long A,
+                                                       long P, long Rw, int nj, int ni, size_t n) {
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  auto at = [&](size_t e) {
     const size_t r = e / (size_t)nj;
     const int j = (int)(e - r * nj);
     const long kk = (long)(r / (size_t)ni), i = (long)(r - (size_t)kk * ni);
-    dst[e] = (T)src[A + kk * P + i * Rw + j];
+    return A + kk * P + i * Rw + j;
+  };
+  for (size_t e0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e0 < n; e0 += kUpUnroll * stride) {
+    double x[kUpUnroll];
+#pragma unroll
+    for (int u = 0; u < kUpUnroll; ++u) {
+      const size_t e = e0 + u * stride;
+      x[u] = e < n ? src[at(e)] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < kUpUnroll; ++u) {
+      const size_t e = e0 + u * stride;
+      if (e < n) dst[e] = (T)x[u];
+    }
   }
 }
 
+// wide: the source is device memory (a staging copy), read at HBM speed
+// with eight blocks per SM instead of one
 template <class T>
-int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st) {
+int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st,
+                         bool wide) {
   const size_t n = (size_t)nj * ni * nk;
-  const int blocks = (int)std::min<size_t>((n + 255) / 256, 152 * 8);
-  k_upload_direct<T><<<blocks > 0 ? blocks : 1, 256, 0, st>>>(dst, src, A, P, Rw, nj, ni, n);
+  const int blocks = (int)std::min<size_t>((n + 127) / 128, wide ? 152 * 8 : 152);
+  k_upload_direct<T><<<blocks > 0 ? blocks : 1, 128, 0, st>>>(dst, src, A, P, Rw, nj, ni, n);
   return 1;
 }
 
-template int launch_upload_direct<double>(double*, const double*, long, long, long, int, int, int, cudaStream_t);
-template int launch_upload_direct<float>(float*, const double*, long, long, long, int, int, int, cudaStream_t);
+template int launch_upload_direct<double>(double*, const double*, long, long, long, int, int, int, cudaStream_t, bool);
+template int launch_upload_direct<float>(float*, const double*, long, long, long, int, int, int, cudaStream_t, bool);
 
 template int launch_fill<double>(double*, size_t, double, cudaStream_t);
 template int launch_fill<float>(float*, size_t, double, cudaStream_t);

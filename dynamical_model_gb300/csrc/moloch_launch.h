@@ -47,7 +47,11 @@ template <class T> int launch_fill(T* p, size_t n, double value, cudaStream_t st
 // the host page tables (NVLink-C2C; the device reports pageable memory
 // access): dst[(kk*ni + i)*nj + j] = src[A + kk*P + i*Rw + j], the interior
 // of a Fortran-layout array (0-based kk < nk, i < ni, j < nj) in the bulk type.
+// wide: the source is device memory (a staging copy) and the grid fills the
+// GPU; otherwise one small block per SM, for a host source read while
+// steps run beside it
 template <class T>
-int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st);
+int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st,
+                         bool wide);
 }  // namespace init
 }  // namespace moloch

@@ -5,7 +5,7 @@
  * `mod_moloch` (nompi/mod_moloch.F90), whose public interface is
  *     public :: allocate_moloch , init_moloch , moloch        (:93)
  * A replacement `mod_moloch` written with ISO_C_BINDING keeps those three
- * names and forwards to the functions below (INTEGRATION.md shows the shim).
+ * names and forwards to the functions below.
  * All arrays cross the boundary as plain host pointers to the Fortran arrays
  * (column-major, j fastest) together with their lower and upper bounds, so
  * the library can check the layout contract of nompi/mod_atmosphere.F90:104-169
@@ -19,6 +19,8 @@
  */
 #ifndef MOLOCH_GB300_H
 #define MOLOCH_GB300_H
+
+#include <stddef.h>
 
 #ifdef __cplusplus
 extern "C" {
@@ -155,11 +157,24 @@ int moloch_gpu_download(moloch_handle_t* h, int field, double* host_base,
  * returns once the kernel is done.  Staged (0): host threads convert level
  * chunks into pinned staging that cudaMemcpyAsync moves.  Direct is the
  * default where the device reports pageable memory access with host page
- * tables.  Downloads and the output path are always staged (a kernel
+ * tables.  Uploads from ranges registered with moloch_gpu_host_register
+ * are DMA copies in either mode.  Downloads and the output path are always
+ * staged (a kernel
  * writing into host pages not yet touched takes a page fault per page).
  * enable: 1 use direct when supported, 0 staged, -1 only query.  Returns
  * the mode in effect (0 or 1) or a negative error. */
 int moloch_gpu_host_direct(moloch_handle_t* h, int enable);
+
+/* Register (pin, cudaHostRegister) a host range whose arrays will be
+ * uploaded again and again -- a Fortran driver's module arrays, allocated
+ * once.  An upload from inside a registered range is a copy-engine DMA of
+ * the whole Fortran array into a device staging buffer on the handle's
+ * upload stream, overlapping the steps already issued without taking SMs;
+ * a gather/convert kernel on the step stream then commits it in stream
+ * order.  The call returns once the DMA is done.  The range must stay
+ * allocated until moloch_gpu_host_unregister (or moloch_gpu_destroy). */
+int moloch_gpu_host_register(moloch_handle_t* h, const void* ptr, size_t bytes);
+int moloch_gpu_host_unregister(moloch_handle_t* h, const void* ptr);
 
 /* Output path (nompi/regcm_dynamical_core.F90:203-216 writes t and ps
  * every iout steps).  output_start snapshots t and ps on the device in

@@ -226,9 +226,10 @@ def test_output_path_overlaps_steps(gpu_lib, mode):
 
 @pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
 def test_direct_and_staged_transfers_agree(gpu_lib, mode):
-    """Uploads through the direct path (a kernel reading the host arrays)
-    and the staged path give identical device states: identical downloads
-    (halo rings included) and identical steps afterwards."""
+    """Uploads through the direct path (a kernel reading the host arrays),
+    the staged path and DMA from registered (pinned) arrays give identical
+    device states: identical downloads (halo rings included) and identical
+    steps afterwards."""
     if not gpu_lib.Moloch(8, 8, 4).host_direct:
         pytest.skip("device without pageable host memory access")
     a = gpu_lib.Moloch(37, 29, 9, mode=mode)
@@ -242,14 +243,23 @@ def test_direct_and_staged_transfers_agree(gpu_lib, mode):
     for n in names:
         da, db = a.download(n), b.download(n)
         assert np.array_equal(da, db), n
+    c = gpu_lib.Moloch(37, 29, 9, mode=mode)  # uploads from registered (pinned) arrays: DMA
+    c.setup_idealized(hills=((300.0, 18.0, 14.0, 4.0),), u0=3.0)
+    c.run(2, graph=True)
     for n in ("u", "v", "w", "pai", "t", "qx"):
         host = a.download(n) * (1.0 + 1e-3)  # a state the device does not hold yet
         a.upload(n, host)
         b.upload(n, host)
-    for g in (a, b):
+        pinned = np.asfortranarray(host.copy())
+        c.host_register(pinned)
+        c.upload(n, pinned)
+        pinned[...] = np.nan  # the upload has read the array when it returns
+        c.host_unregister(pinned)
+    for g in (a, b, c):
         g.run(1, graph=True)
     for n in names:
         assert np.array_equal(a.download(n), b.download(n)), n
+        assert np.array_equal(a.download(n), c.download(n)), n
 
 
 @pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
