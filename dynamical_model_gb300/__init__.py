@@ -336,12 +336,20 @@ class Moloch:
         the host; the next steps overlap the copy."""
         _check(self.L.moloch_gpu_output_start(self.h))
 
-    def output_finish(self):
-        """(t, ps) of the last output_start, reference layout with halos."""
+    def output_finish(self, t=None, ps=None):
+        """(t, ps) of the last output_start, reference layout with halos;
+        filled into the given arrays (for instance registered ones, which the
+        device then writes directly) or into new ones."""
         arrs, args = [], []
-        for name in ("t", "ps"):
+        for name, given in (("t", t), ("ps", ps)):
             bnds = field_bounds(name, self.jx, self.iy, self.kz)
-            a = np.zeros(tuple(u - l + 1 for l, u in bnds), dtype=np.float64, order="F")
+            shape = tuple(u - l + 1 for l, u in bnds)
+            if given is None:
+                a = np.zeros(shape, dtype=np.float64, order="F")
+            else:
+                if given.shape != shape or given.dtype != np.float64 or not given.flags.f_contiguous:
+                    raise ValueError(f"{name}: need a Fortran-ordered float64 array of shape {shape}")
+                a = given
             arrs.append(a)
             args += [a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
                      (ctypes.c_int * 4)(*[l for l, _ in bnds]), (ctypes.c_int * 4)(*[u for _, u in bnds])]

@@ -191,6 +191,7 @@ struct moloch_handle {
   // on a second stream while the step stream runs on
   void* out_dev = nullptr;
   void* out_host = nullptr;
+  void* out_f64 = nullptr;  // Fortran-layout FP64 t and ps, for registered output arrays
   cudaStream_t out_stream = nullptr;
   cudaEvent_t out_taken = nullptr, out_done = nullptr;
   bool out_pending = false;
@@ -1059,7 +1060,9 @@ int moloch_gpu_output_start(moloch_handle_t* h) {
   if (!h->out_dev) {
     CUDA_TRY(cudaMalloc(&h->out_dev, bytes));
     CUDA_TRY(cudaMallocHost(&h->out_host, bytes));
-    CUDA_TRY(cudaStreamCreateWithFlags(&h->out_stream, cudaStreamNonBlocking));
+    int lo = 0, hi = 0;  // highest priority: its copies and kernels slip in beside the running steps
+    CUDA_TRY(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CUDA_TRY(cudaStreamCreateWithPriority(&h->out_stream, cudaStreamNonBlocking, hi));
     CUDA_TRY(cudaEventCreateWithFlags(&h->out_taken, cudaEventDisableTiming));
     CUDA_TRY(cudaEventCreateWithFlags(&h->out_done, cudaEventDisableTiming));
   }
@@ -1086,6 +1089,38 @@ int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb
   for (int d = 0; d < sp.ndim; ++d)
     if (ps_host && (ps_lb[d] != sp.lb[d] || ps_ub[d] != sp.ub[d])) return fail(MOLOCH_ERR_BOUNDS, "output ps bounds");
   const size_t pl = (size_t)nj * ni, n3 = pl * kz;
+  auto host_len = [](const FieldShape& s, int nk) {
+    return (size_t)(s.ub[0] - s.lb[0] + 1) * (s.ub[1] - s.lb[1] + 1) * nk;
+  };
+  if ((!t_host || is_pinned(h, t_host, sizeof(double) * host_len(st, kz))) &&
+      (!ps_host || is_pinned(h, ps_host, sizeof(double) * host_len(sp, 1)))) {
+    // registered destinations: a kernel lays the snapshot out in Fortran
+    // order (halo rings included) in device memory, the copy engine moves
+    // it into the caller's arrays -- no host-side scatter, no SMs on the
+    // host link
+    const size_t lt = host_len(st, kz), lp = host_len(sp, 1);
+    if (!h->out_f64) CUDA_TRY(cudaMalloc(&h->out_f64, sizeof(double) * (lt + lp)));
+    double* dt = (double*)h->out_f64;
+    double* dp = dt + lt;
+    auto put = [&](const FieldShape& s, int nk, size_t off, double* dev, double* dst, size_t len) -> int {
+      const int n1 = s.ub[0] - s.lb[0] + 1, n2 = s.ub[1] - s.lb[1] + 1;
+      if (h->elem == 8)
+        moloch::init::launch_output_layout<double>(dev, (const double*)h->out_dev + off, s.lb[0], n1, s.lb[1], n2, nk,
+                                                   nj, ni, h->out_stream);
+      else
+        moloch::init::launch_output_layout<float>(dev, (const float*)h->out_dev + off, s.lb[0], n1, s.lb[1], n2, nk,
+                                                  nj, ni, h->out_stream);
+      CUDA_TRY(cudaMemcpyAsync(dst, dev, sizeof(double) * len, cudaMemcpyDeviceToHost, h->out_stream));
+      return MOLOCH_OK;
+    };
+    int rc = MOLOCH_OK;
+    if (t_host) rc = put(st, kz, 0, dt, t_host, lt);
+    if (!rc && ps_host) rc = put(sp, 1, n3, dp, ps_host, lp);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(h->out_stream));
+    h->out_pending = false;
+    return rc;
+  }
   CUDA_TRY(cudaEventSynchronize(h->out_done));
   h->out_pending = false;
   auto scatter = [&](const FieldShape& s, int nk, size_t off, double* base) {
@@ -1739,6 +1774,7 @@ int moloch_gpu_destroy(moloch_handle_t* h) {
   if (h->stage) cudaFreeHost(h->stage);
   if (h->out_stream) cudaStreamSynchronize(h->out_stream);
   if (h->out_dev) cudaFree(h->out_dev);
+  if (h->out_f64) cudaFree(h->out_f64);
   if (h->out_host) cudaFreeHost(h->out_host);
   if (h->out_stream) cudaStreamDestroy(h->out_stream);
   if (h->out_taken) cudaEventDestroy(h->out_taken);

@@ -183,50 +183,81 @@ int launch_fill(T* p, size_t n, double value, cudaStream_t st) {
   return 1;
 }
 
-// ---- direct host uploads ------------------------------------------------------
-// One block of 128 threads per SM, each thread with eight independent host
-// reads in flight (about 1.2 MB across the GPU, enough for the host link,
-// about 200 GB/s on GB300): the kernel runs beside the steps it overlaps
-// while taking 4 of the 64 warp slots of an SM.  Consecutive threads take
-// consecutive j, so the host array is read in whole rows.
-constexpr int kUpUnroll = 8;
-
+// ---- direct host uploads and output layout ------------------------------------
+// Row-wise: a block takes whole rows (one (level, i) row of nj values), its
+// threads consecutive j, so no per-element division and whole host rows.
+// The upload kernel serves two sources: the caller's host array read
+// through the host page tables (small grid, one block of 128 threads per
+// SM: it runs beside the steps it overlaps, each thread with up to eight
+// reads in flight) and a device staging copy of the array (one block per
+// row, HBM speed).
 template <class T>
 __global__ void __launch_bounds__(128) k_upload_direct(T* __restrict__ dst, const double* __restrict__ src, long A,
-                                                       long P, long Rw, int nj, int ni, size_t n) {
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  auto at = [&](size_t e) {
-    const size_t r = e / (size_t)nj;
-    const int j = (int)(e - r * nj);
-    const long kk = (long)(r / (size_t)ni), i = (long)(r - (size_t)kk * ni);
-    return A + kk * P + i * Rw + j;
-  };
-  for (size_t e0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e0 < n; e0 += kUpUnroll * stride) {
-    double x[kUpUnroll];
+                                                       long P, long Rw, int nj, int ni, int rows) {
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int kk = r / ni, i = r - kk * ni;
+    const double* __restrict__ in = src + A + kk * P + i * Rw;
+    T* __restrict__ out = dst + (size_t)r * nj;
+    for (int j0 = threadIdx.x; j0 < nj; j0 += 8 * blockDim.x) {
+      double x[8];
 #pragma unroll
-    for (int u = 0; u < kUpUnroll; ++u) {
-      const size_t e = e0 + u * stride;
-      x[u] = e < n ? src[at(e)] : 0.0;
-    }
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u * blockDim.x;
+        x[u] = j < nj ? in[j] : 0.0;
+      }
 #pragma unroll
-    for (int u = 0; u < kUpUnroll; ++u) {
-      const size_t e = e0 + u * stride;
-      if (e < n) dst[e] = (T)x[u];
+      for (int u = 0; u < 8; ++u) {
+        const int j = j0 + u * blockDim.x;
+        if (j < nj) out[j] = (T)x[u];
+      }
     }
   }
 }
 
-// wide: the source is device memory (a staging copy), read at HBM speed
-// with eight blocks per SM instead of one
+// wide: the source is device memory (a staging copy) and the grid has one
+// block per row; otherwise one block per SM
 template <class T>
 int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st,
                          bool wide) {
-  const size_t n = (size_t)nj * ni * nk;
-  const int blocks = (int)std::min<size_t>((n + 127) / 128, wide ? 152 * 8 : 152);
-  k_upload_direct<T><<<blocks > 0 ? blocks : 1, 128, 0, st>>>(dst, src, A, P, Rw, nj, ni, n);
+  const int rows = ni * nk;
+  const int blocks = wide ? rows : std::min(rows, 152);
+  k_upload_direct<T><<<blocks > 0 ? blocks : 1, 128, 0, st>>>(dst, src, A, P, Rw, nj, ni, rows);
   return 1;
 }
 
+// Fortran layout of an output field: every element of an array with bounds
+// (lb0:lb0+n1-1, lb1:lb1+n2-1, 1:nk) from the dense device field, halo
+// indices wrapped periodically (they lie within one period of the
+// interior), into device memory; a DMA then moves it to the caller's
+// registered host array.  One block per row.
+__device__ __forceinline__ int wrap1(int x, int n) {  // 1-based index -> 0-based periodic
+  int y = x - 1;
+  if (y < 0) y += n;
+  else if (y >= n) y -= n;
+  return y;
+}
+
+template <class T>
+__global__ void __launch_bounds__(128) k_output_layout(double* __restrict__ dst, const T* __restrict__ src, int lb0,
+                                                       int n1, int lb1, int n2, int nj, int ni, int rows) {
+  for (int r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int kk = r / n2, i = lb1 + (r - kk * n2);
+    const T* __restrict__ in = src + ((size_t)kk * ni + wrap1(i, ni)) * nj;
+    double* __restrict__ out = dst + (size_t)r * n1;
+    for (int q = threadIdx.x; q < n1; q += blockDim.x) out[q] = (double)in[wrap1(lb0 + q, nj)];
+  }
+}
+
+template <class T>
+int launch_output_layout(double* dst, const T* src, int lb0, int n1, int lb1, int n2, int nk, int nj, int ni,
+                         cudaStream_t st) {
+  const int rows = n2 * nk;
+  k_output_layout<T><<<rows > 0 ? rows : 1, 128, 0, st>>>(dst, src, lb0, n1, lb1, n2, nj, ni, rows);
+  return 1;
+}
+
+template int launch_output_layout<double>(double*, const double*, int, int, int, int, int, int, int, cudaStream_t);
+template int launch_output_layout<float>(double*, const float*, int, int, int, int, int, int, int, cudaStream_t);
 template int launch_upload_direct<double>(double*, const double*, long, long, long, int, int, int, cudaStream_t, bool);
 template int launch_upload_direct<float>(float*, const double*, long, long, long, int, int, int, cudaStream_t, bool);
 

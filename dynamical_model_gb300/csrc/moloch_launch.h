@@ -53,5 +53,11 @@ template <class T> int launch_fill(T* p, size_t n, double value, cudaStream_t st
 template <class T>
 int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st,
                          bool wide);
+// Fortran layout of an output field in device memory: every element of an
+// array with bounds (lb0:lb0+n1-1, lb1:lb1+n2-1, 1:nk) from the dense
+// device field, halo indices wrapped periodically
+template <class T>
+int launch_output_layout(double* dst, const T* src, int lb0, int n1, int lb1, int n2, int nk, int nj, int ni,
+                         cudaStream_t st);
 }  // namespace init
 }  // namespace moloch

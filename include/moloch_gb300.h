@@ -182,6 +182,10 @@ int moloch_gpu_host_unregister(moloch_handle_t* h, const void* ptr);
  * pinned host memory on a second stream, then returns: the next steps run
  * while the copy is in flight.  output_finish waits for that copy and fills
  * reference-layout host arrays (either may be NULL) with the snapshot.
+ * When both given arrays lie in ranges registered with
+ * moloch_gpu_host_register, a kernel on the second stream lays the
+ * snapshot out in their Fortran order on the device and the copy engine
+ * writes them, instead of host threads. 
  * One snapshot at a time: start, finish, start, ... */
 int moloch_gpu_output_start(moloch_handle_t* h);
 int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb, const int* t_ub,

@@ -202,10 +202,12 @@ def test_upload_download_roundtrip_and_bounds(gpu_lib, direct):
 
 
 @pytest.mark.parametrize("mode", ["fp64", "fp32_mixed"])
-def test_output_path_overlaps_steps(gpu_lib, mode):
+@pytest.mark.parametrize("registered", [False, True])
+def test_output_path_overlaps_steps(gpu_lib, mode, registered):
     """output_start after step 2, two more steps, output_finish: the arrays
     hold t and ps of step 2 (with periodic halos), and the run itself is
-    not disturbed."""
+    not disturbed; into new arrays (host threads) or into registered ones
+    (kernels writing them from the device snapshot)."""
     a = gpu_lib.Moloch(40, 28, 12, mode=mode)
     b = gpu_lib.Moloch(40, 28, 12, mode=mode)
     for g in (a, b):
@@ -214,7 +216,14 @@ def test_output_path_overlaps_steps(gpu_lib, mode):
     b.run(2, graph=True)
     a.output_start()
     a.run(2, graph=True)
-    t2, ps2 = a.output_finish()
+    if registered:
+        t_out, ps_out = np.full_like(a.download("t"), np.nan), np.full_like(a.download("ps"), np.nan)
+        a.host_register(t_out)
+        a.host_register(ps_out)
+        t2, ps2 = a.output_finish(t_out, ps_out)
+        assert t2 is t_out and ps2 is ps_out
+    else:
+        t2, ps2 = a.output_finish()
     assert np.array_equal(t2, b.download("t"))
     assert np.array_equal(ps2, b.download("ps"))
     b.run(2, graph=True)
