@@ -468,6 +468,9 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--size", default=None, help="JXxIYxKZ override (profiling a smaller case)")
     ap.add_argument("--only", default=None, choices=["mixed", "fp64"], help="time one path only (profiling)")
+    ap.add_argument("--tuning", default=None,
+                    help="comma-separated launch shapes for --only instead of autotuning (profiling runs under a "
+                         "profiler, whose timings would mislead the autotuner), e.g. 32,24,1")
     ap.add_argument("--workload", default="single",
                     choices=["single", "ensemble", "full1024", "surrogate", "accuracy"],
                     help="single: 512x512x60 (headline); ensemble: 64 uneven members; full1024: 1024x1024x60; "
@@ -505,7 +508,12 @@ def main():
         return run_accuracy(args, torch, dm, stream) if rank == 0 else 0
     # ---- headline path: FP32 storage + FP64 solve --------------------------
     if args.only:
-        d, _ = tuned(dm, "fp32_mixed" if args.only == "mixed" else "fp64", sptr)
+        mode = "fp32_mixed" if args.only == "mixed" else "fp64"
+        if args.tuning:
+            d = make_domain(dm, mode, sptr)
+            d.set_tuning([int(x) for x in args.tuning.split(",")])
+        else:
+            d, _ = tuned(dm, mode, sptr)
         d.run(args.warmup, graph=True)
         ms, launches = time_steps(torch, d, stream, args.steps)
         if rank == 0:
