@@ -308,8 +308,7 @@ __device__ __forceinline__ float narrow_trunc(double x) {
 // with the Exner/theta/pai update of the level above it.
 // defer_pai: leave zdiv2b final and pai to k_pai_update (divergence filter on).
 // PD: levels loaded ahead of the level computed, in both sweeps (a register
-// ring of PD level records).  The kernels use PD = 1: 64 registers (FP32),
-// 8 blocks per SM, no spills.  A ring of 3 levels at 4 blocks per SM (so
+// ring of PD level records).  The kernels use PD = 1.  A ring of 3 levels at 4 blocks per SM (so
 // that the back-substitution finds more of the down-sweep's levels in L2)
 // measured 13 % slower at 512 x 512 x 60: fewer columns in flight cost more
 // bandwidth than the extra L2 hits saved.
@@ -501,8 +500,11 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
   if (last) S[(size_t)kz * pl] = T(0);
 }
 
+// FP32: 9 blocks of 128 threads per SM (56 registers, 24 bytes spilled):
+// 1.5 waves at 512 x 512 instead of 1.68 with 8 blocks (4.51 against
+// 4.61 ms per step; 10 blocks, 48 registers, 4.84 ms)
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4) k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 9 : 4) k_sound_column(View<T> d, int nsound, int last, int defer_pai) {
   b_sound_column<T, 1>(d, blockIdx.x, blockIdx.y, blockIdx.z, nsound, last, defer_pai);
 }
 
