@@ -1257,8 +1257,10 @@ __device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, 
   }
 }
 
+// FP32: 8 blocks per SM (64 registers, 48 bytes spilled), 3.5 % faster
+// than the 6 blocks that 80 registers allow
 template <class T>
-__global__ void __launch_bounds__(128) k_divdamp_strip(View<T> d, int R) {
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_divdamp_strip(View<T> d, int R) {
   b_divdamp_strip<T>(d, blockIdx.x, blockIdx.y, R);
 }
 
