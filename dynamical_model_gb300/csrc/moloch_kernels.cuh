@@ -509,7 +509,7 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 9 : 4) k_soun
 }
 
 template <class T>
-__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 6 : 4)
+__global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4)
     kb_sound_column(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int nsound, int last, int defer_pai) {
   __shared__ View<T> sv;
   const int4 t = tiles[blockIdx.x];
@@ -1257,15 +1257,15 @@ __device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, 
   }
 }
 
-// FP32: 8 blocks per SM (64 registers, 48 bytes spilled), 3.5 % faster
-// than the 6 blocks that 80 registers allow
+// (8 blocks per SM with 64 registers measured slower in the full step:
+// 2.74 against 2.56 ms per step)
 template <class T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3) k_divdamp_strip(View<T> d, int R) {
+__global__ void __launch_bounds__(128) k_divdamp_strip(View<T> d, int R) {
   b_divdamp_strip<T>(d, blockIdx.x, blockIdx.y, R);
 }
 
 template <class T>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3)
     kb_divdamp_strip(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int R) {
   __shared__ View<T> sv;
   const int4 t = tiles[blockIdx.x];
@@ -1448,7 +1448,7 @@ __global__ void __launch_bounds__(kColBX* kColBY, vert_min_blocks<T, F>()) k_waf
 }
 
 template <class T, int F>
-__global__ void __launch_bounds__(kColBX* kColBY)
+__global__ void __launch_bounds__(kColBX* kColBY, vert_min_blocks<T, F>())
     kb_waf_vertical(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
   __shared__ View<T> sv;
   const int4 t = tiles[blockIdx.x];
