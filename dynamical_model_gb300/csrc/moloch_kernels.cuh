@@ -13,8 +13,8 @@
 //   k_lap_filter       :423-440 divergence_filter (mo_divfilter)
 //   k_pai_update       :716-728 (split form used when the filter is on)
 //   k_sound_momentum   :730-837  Equations 17, 18
-//   k_stag_to_x        :1327-1341, :1389-1417  (u,v,w) -> (ux,vx,wx)
-//   k_waf_vertical     :966-1073  both vertical WAF passes in registers, all 10 fields
+//   k_waf_vertical     :966-1073  both vertical WAF passes in registers, all 10 fields,
+//                      with (u,v,w) -> (ux,vx,wx) of :1327-1341, :1389-1417 formed on the fly
 //   k_waf_horizontal   :1075-1187 meridional + zonal WAF of one level, p0 in shared memory
 //   k_stag_from_x      :1343-1387  (ux,vx,wx) -> (u,v,w)
 //   k_filter_increment :442-481 + :333-353 filtpai / filttheta
@@ -1274,51 +1274,6 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3)
   b_divdamp_strip<T>(sv, t.y, t.z, R);
 }
 
-// ---- advection: staggered -> cross points (:1327-1341, :1389-1417) -----
-template <class T>
-__device__ __forceinline__ void b_stag_to_x(const View<T>& d, const int bx, const int by, const int bz) {
-  int jj = bx * kPtBX + threadIdx.x;
-  int ii = by * kPtBY + threadIdx.y;
-  const int nj = d.nj, ni = d.ni, kz = d.kz, kk = bz;
-  if (jj >= nj || ii >= ni) return;
-  const T* __restrict__ u = d.ubuf[d.cur];
-  const T* __restrict__ v = d.vbuf[d.cur];
-  const size_t o = (size_t)kk * d.pl;
-  const size_t c = jj + (size_t)nj * ii;
-  const size_t rowj = (size_t)nj * ii;
-  d.ux[o + c] = T(0.5625) * (u[o + rowj + wp1(jj, nj)] + u[o + c]) -
-                T(0.0625) * (u[o + rowj + wp2(jj, nj)] + u[o + rowj + wm1(jj, nj)]);
-  d.vx[o + c] = T(0.5625) * (v[o + jj + (size_t)nj * wp1(ii, ni)] + v[o + c]) -
-                T(0.0625) * (v[o + jj + (size_t)nj * wp2(ii, ni)] + v[o + jj + (size_t)nj * wm1(ii, ni)]);
-  const T* __restrict__ w = d.w;
-  const size_t pl = d.pl;
-  T wxv;
-  if (kk == 0)
-    wxv = T(0.5) * (w[c + pl] + w[c]);
-  else if (kk == kz - 1)
-    wxv = T(0.5) * (w[c + (size_t)kz * pl] + w[c + (size_t)(kz - 1) * pl]);
-  else
-    wxv = T(0.5625) * (w[c + (kk + 1) * pl] + w[c + kk * pl]) -
-          T(0.0625) * (w[c + (kk + 2) * pl] + w[c + (kk - 1) * pl]);
-  d.wx[o + c] = wxv;
-}
-
-template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_to_x(View<T> d) {
-  b_stag_to_x<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
-}
-
-template <class T>
-__global__ void __launch_bounds__(kPtBX* kPtBY)
-    kb_stag_to_x(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
-  __shared__ View<T> sv;
-  const int4 t = tiles[blockIdx.x];
-  copy_view(&sv, views + t.x);
-  __syncthreads();
-  b_stag_to_x<T>(sv, t.y, t.z, t.w);
-}
-
-
 // ---- advection: vertical WAF, two passes at dt/2 (:966-1073) ------------
 // wfw(k+1) of one pass from x(max(k-1,1)), x(k), x(k+1), x(min(k+2,kz))
 template <class T>
@@ -1360,15 +1315,15 @@ __device__ __forceinline__ float waf_vflux<float>(float s_k1, float dtrdz, float
 // s/2, the metric term of the update), which the compiler computes once.
 // The grid puts the field group fastest, so the groups of one column tile
 // run together and share the s / metric loads through L2.
-template <class T, int F>
-__device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, const int by, const int bz) {
-  constexpr int NG = kNumAdvected / F;
-  const int g = bx % NG;
-  const int tj = bx / NG;
-  const int jj = tj * kColBX + threadIdx.x;
-  const int ii = by * kColBY + threadIdx.y;
+// G >= 0: the thread's field group holds some of fields 2, 3, 4 (ux, vx,
+// wx), which are formed here from the staggered winds -- the fourth-order
+// averages of :1327-1341 and :1389-1417, two-point at the bottom and top
+// levels of wx -- and stored for the horizontal pass, which reads them.
+// Each level is formed once, in order, with its store; the clamped repeats
+// at the bottom reuse the last level.  G = -1: a group of read fields only.
+template <class T, int F, int G>
+__device__ __forceinline__ void b_waf_vertical_g(const View<T>& d, const int g, const int jj, const int ii) {
   const int nj = d.nj, ni = d.ni, kz = d.kz;
-  if (jj >= nj || ii >= ni) return;
   const size_t pl = d.pl;
   const size_t c = jj + (size_t)nj * ii;
   const T* src[F];
@@ -1382,12 +1337,41 @@ __device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, c
   const T* __restrict__ wafu = d.wafu;
   const T* __restrict__ wafd = d.wafd;
   const T dtrdz = d.dtrdz_a;
+  auto xval = [&](const int u, const int kk) -> T {
+    const size_t o = (size_t)kk * pl;
+    if constexpr (G < 0) {
+      return src[u][c + o];
+    } else {
+      const int f = G * F + u;
+      T x;
+      if (f == 2) {
+        const T* __restrict__ us = d.ubuf[d.cur] + o + (size_t)nj * ii;
+        x = T(0.5625) * (us[wp1(jj, nj)] + us[jj]) - T(0.0625) * (us[wp2(jj, nj)] + us[wm1(jj, nj)]);
+      } else if (f == 3) {
+        const T* __restrict__ vs = d.vbuf[d.cur] + o + jj;
+        x = T(0.5625) * (vs[(size_t)nj * wp1(ii, ni)] + vs[(size_t)nj * ii]) -
+            T(0.0625) * (vs[(size_t)nj * wp2(ii, ni)] + vs[(size_t)nj * wm1(ii, ni)]);
+      } else if (f == 4) {
+        const T* __restrict__ w = d.w + c;
+        if (kk == 0)
+          x = T(0.5) * (w[pl] + w[0]);
+        else if (kk == kz - 1)
+          x = T(0.5) * (w[(size_t)kz * pl] + w[(size_t)(kz - 1) * pl]);
+        else
+          x = T(0.5625) * (w[(kk + 1) * pl] + w[kk * pl]) - T(0.0625) * (w[(kk + 2) * pl] + w[(kk - 1) * pl]);
+      } else {
+        return src[u][c + o];
+      }
+      const_cast<T*>(src[u])[c + o] = x;
+      return x;
+    }
+  };
   T xa[F], xb[F], xc[F];               // pass-1 window x(t-1), x(t), x(t+1)
   T wfw1[F], wfw2[F];                  // wfw1(t), wfw2(m)
   T y0[F], y1[F], y2[F], y3[F];        // wz1(t-3 .. t)
 #pragma unroll
   for (int u = 0; u < F; ++u) {
-    xa[u] = src[u][c]; xb[u] = xa[u]; xc[u] = src[u][c + pl];
+    xa[u] = xval(u, 0); xb[u] = xa[u]; xc[u] = kz > 1 ? xval(u, 1) : xa[u];
     wfw1[u] = T(0); wfw2[u] = T(0);
     y0[u] = T(0); y1[u] = T(0); y2[u] = T(0); y3[u] = T(0);
   }
@@ -1410,7 +1394,7 @@ __device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, c
     for (int u = 0; u < F; ++u) {
       T w1 = y3[u];
       if (FAST || t <= kz) {
-        const T xd = src[u][c + (size_t)(t2 - 1) * pl];
+        const T xd = (FAST || t + 2 <= kz) ? xval(u, t2 - 1) : xc[u];  // x(min(t+2, kz))
         const T wfw1n = (FAST || t <= kz - 1) ? waf_vflux(sD, dtrdz, xa[u], xb[u], xc[u], xd) : T(0);
         w1 = ((xb[u] - wfw1[u] * uC) + wfw1n * dC) + (sC * uC - sD * dC) * xb[u];
         xa[u] = xb[u]; xb[u] = xc[u]; xc[u] = xd; wfw1[u] = wfw1n;
@@ -1430,6 +1414,32 @@ __device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, c
   for (int t = 1; t <= 3; ++t) step(t, std::false_type());
   for (int t = 4; t <= tf; ++t) step(t, std::true_type());
   for (int t = tf + 1; t <= kz + 2; ++t) step(t, std::false_type());
+}
+
+template <class T, int F>
+__device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, const int by, const int bz) {
+  constexpr int NG = kNumAdvected / F;
+  const int g = bx % NG;
+  const int tj = bx / NG;
+  const int jj = tj * kColBX + threadIdx.x;
+  const int ii = by * kColBY + threadIdx.y;
+  if (jj >= d.nj || ii >= d.ni) return;
+  // the groups holding fields 2..4 (block-uniform branch)
+  if constexpr (F == 1) {
+    if (g == 2) b_waf_vertical_g<T, 1, 2>(d, g, jj, ii);
+    else if (g == 3) b_waf_vertical_g<T, 1, 3>(d, g, jj, ii);
+    else if (g == 4) b_waf_vertical_g<T, 1, 4>(d, g, jj, ii);
+    else b_waf_vertical_g<T, 1, -1>(d, g, jj, ii);
+  } else if constexpr (F == 2) {
+    if (g == 1) b_waf_vertical_g<T, 2, 1>(d, g, jj, ii);
+    else if (g == 2) b_waf_vertical_g<T, 2, 2>(d, g, jj, ii);
+    else b_waf_vertical_g<T, 2, -1>(d, g, jj, ii);
+  } else if constexpr (F == 5) {
+    if (g == 0) b_waf_vertical_g<T, 5, 0>(d, g, jj, ii);
+    else b_waf_vertical_g<T, 5, -1>(d, g, jj, ii);
+  } else {
+    b_waf_vertical_g<T, F, 0>(d, g, jj, ii);
+  }
 }
 
 // Blocks per SM by bulk type and fields per thread.  FP32, one field per
@@ -2095,8 +2105,7 @@ template <class T>
 int launch_advection(View<T>& d, cudaStream_t st) {
   const dim3 pb(kPtBX, kPtBY), pg = pt_grid(d.nj, d.ni, d.kz);
   const dim3 hg((d.nj + 31) / 32, (d.ni + 7) / 8, (d.kz + d.hz_levels - 1) / d.hz_levels);
-  MOLOCH_LAUNCH(KK_STAG_TO_X, st, k_stag_to_x<T><<<pg, pb, 0, st>>>(d));
-  launch_waf_vertical<T>(d, st);
+  launch_waf_vertical<T>(d, st);  // forms ux, vx, wx from u, v, w as well
   if (d.hz_levels >= 16) {  // warp strips of hz_levels rows
     const int nstrips = ((d.nj + kStripJ - 1) / kStripJ) * ((d.ni + d.hz_levels - 1) / d.hz_levels);
     MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, k_waf_hstrip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d));
@@ -2107,7 +2116,7 @@ int launch_advection(View<T>& d, cudaStream_t st) {
   d.bind_fields();
   MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pg, pb, 0, st>>>(d));
   d.cur = 0;
-  return 4;
+  return 3;
 }
 
 template <class T>
@@ -2188,7 +2197,6 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
       n += 4;
       cur ^= 1;
     }
-    MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<npt, pb, 0, st>>>(V(), PT));
     blaunch_waf_vertical<T>(b, V(), st);
     if (b.hstrip)
       MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_hstrip<T><<<nhz, 128, 0, st>>>(V(), HZ));
@@ -2197,7 +2205,7 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
     fcur ^= 1;
     MOLOCH_LAUNCH(KK_STAG_FROM_X, st, kb_stag_from_x<T><<<npt, pb, 0, st>>>(V(), PT));
     cur = 0;
-    n += 4;
+    n += 3;
   }
   MOLOCH_LAUNCH(KK_POSTDIAG, st, kb_postdiag<T><<<nco, cb, 0, st>>>(V(), CO));
   return n + 1;
@@ -2207,7 +2215,6 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
 template <class T>
 int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur) {
   const dim3 pb(kPtBX, kPtBY), cb(kColBX, kColBY), hb(32, 8);
-  MOLOCH_LAUNCH(KK_STAG_TO_X, st, kb_stag_to_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
   blaunch_waf_vertical<T>(b, b.views[cur][fcur], st);
   if (b.hstrip)
     MOLOCH_LAUNCH(KK_WAF_HORIZONTAL, st, kb_waf_hstrip<T><<<b.ntiles[TK_HORIZONTAL], 128, 0, st>>>(b.views[cur][fcur], b.tiles[TK_HORIZONTAL]));
@@ -2216,7 +2223,7 @@ int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur) {
   fcur ^= 1;
   MOLOCH_LAUNCH(KK_STAG_FROM_X, st, kb_stag_from_x<T><<<b.ntiles[TK_POINT], pb, 0, st>>>(b.views[cur][fcur], b.tiles[TK_POINT]));
   cur = 0;
-  return 4;
+  return 3;
 }
 
 int diag_parts(int nj, int ni) {
