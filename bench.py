@@ -601,7 +601,7 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
     # ---- end to end through the C ABI with host arrays ----------------------
     e2e = None
     if not args.no_e2e:
-        n_e2e = max(2, min(args.steps, 5))
+        n_e2e = max(2, args.steps)
         ms_e2e, h2d, d2h = e2e_steps(torch, dm, dsur, stream, n_e2e, args.warmup)
         ms_e2e = reduce_max(dist, ms_e2e, device)
         e2e = {"value": n_dom * gp * n_e2e / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,

@@ -189,8 +189,8 @@ int launch_fill(T* p, size_t n, double value, cudaStream_t st) {
 // The upload kernel serves two sources: the caller's host array read
 // through the host page tables (small grid, one block of 128 threads per
 // SM: it runs beside the steps it overlaps, each thread with up to eight
-// reads in flight) and a device staging copy of the array (one block per
-// row, HBM speed).
+// reads in flight) and a device staging copy of the array (that one by
+// k_upload_gather below, at HBM speed).
 template <class T>
 __global__ void __launch_bounds__(128) k_upload_direct(T* __restrict__ dst, const double* __restrict__ src, long A,
                                                        long P, long Rw, int nj, int ni, int rows) {
@@ -214,13 +214,56 @@ __global__ void __launch_bounds__(128) k_upload_direct(T* __restrict__ dst, cons
   }
 }
 
-// wide: the source is device memory (a staging copy) and the grid has one
-// block per row; otherwise one block per SM
+// The same gather from a device staging copy: kUpR rows per block, all
+// kUpR x kUpV loads of a thread issued before its stores (16 in flight for
+// rows of up to 512 points), so the blocks do not end after one round trip.
+constexpr int kUpR = 4, kUpV = 4;
+template <class T>
+__global__ void __launch_bounds__(128) k_upload_gather(T* __restrict__ dst, const double* __restrict__ src, long A,
+                                                       long P, long Rw, int nj, int ni, int rows) {
+  const int r0 = blockIdx.x * kUpR;
+  for (int j0 = threadIdx.x; j0 < nj; j0 += kUpV * 128) {
+    double x[kUpR][kUpV];
+#pragma unroll
+    for (int a = 0; a < kUpR; ++a) {
+      const int r = r0 + a;
+      const bool rv = r < rows;
+      const int kk = rv ? r / ni : 0, i = rv ? r - kk * ni : 0;
+      const double* __restrict__ in = src + A + kk * P + i * Rw;
+#pragma unroll
+      for (int u = 0; u < kUpV; ++u) {
+        const int j = j0 + u * 128;
+        x[a][u] = (rv && j < nj) ? in[j] : 0.0;
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < kUpR; ++a) {
+      const int r = r0 + a;
+      if (r < rows) {
+        T* __restrict__ out = dst + (size_t)r * nj;
+#pragma unroll
+        for (int u = 0; u < kUpV; ++u) {
+          const int j = j0 + u * 128;
+          if (j < nj) out[j] = (T)x[a][u];
+        }
+      }
+    }
+  }
+}
+
+// wide: the source is device memory (a staging copy), gathered by
+// k_upload_gather; otherwise the source is host memory read through the
+// host page tables by one block per SM
 template <class T>
 int launch_upload_direct(T* dst, const double* src, long A, long P, long Rw, int nj, int ni, int nk, cudaStream_t st,
                          bool wide) {
   const int rows = ni * nk;
-  const int blocks = wide ? rows : std::min(rows, 152);
+  if (wide) {
+    const int blocks = (rows + kUpR - 1) / kUpR;
+    k_upload_gather<T><<<blocks > 0 ? blocks : 1, 128, 0, st>>>(dst, src, A, P, Rw, nj, ni, rows);
+    return 1;
+  }
+  const int blocks = std::min(rows, 152);
   k_upload_direct<T><<<blocks > 0 ? blocks : 1, 128, 0, st>>>(dst, src, A, P, Rw, nj, ni, rows);
   return 1;
 }
