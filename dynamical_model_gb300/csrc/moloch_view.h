@@ -135,7 +135,7 @@ struct View {
 // Kernel kinds, for per-kernel CUDA-event timing (moloch_gpu_profile_step).
 enum KernelKind {
   KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_DAMP, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE,
-  KK_SOUND_MOMENTUM, KK_STAG_TO_X, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
+  KK_SOUND_MOMENTUM, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
   KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_COUNT
 };
 
