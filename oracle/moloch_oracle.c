@@ -1199,6 +1199,20 @@ int oracle_step(void *h, int istep, int lprint, double *diag) {
   return bad;
 }
 
+/* the staggering of advection() alone, for the cross-check of
+   tests/test_oracle_diagnostics.py: to_x = 1 runs uvstagtox + wstagtox
+   (u, v, w -> ux, vx, wx), 0 runs xtouvstag + xtowstag (back) */
+void oracle_stagger(void *h, int to_x) {
+  Moloch *m = (Moloch *)h;
+  if (to_x) {
+    uvstagtox(m);
+    wstagtox(m);
+  } else {
+    xtouvstag(m);
+    xtowstag(m);
+  }
+}
+
 /* phases, for per-phase parity tests: 0 reset+prediag, 1 sound, 2 advection, 3 postdiag */
 void oracle_phase(void *h, int phase) {
   Moloch *m = (Moloch *)h;

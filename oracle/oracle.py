@@ -49,6 +49,7 @@ def lib(checked=False):
     L.oracle_step.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                               ctypes.POINTER(ctypes.c_double)]
     L.oracle_phase.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.oracle_stagger.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_get.restype = ctypes.c_int
     L.oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     L.oracle_set.restype = ctypes.c_int
@@ -116,6 +117,9 @@ class Oracle:
 
     def phase(self, p):
         self.L.oracle_phase(self.h, p)
+
+    def stagger(self, to_x):
+        self.L.oracle_stagger(self.h, int(to_x))
 
     def get(self, name):
         nk = self.kz + 1 if name in FIELDS_KZP1 else self.kz

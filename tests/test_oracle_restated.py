@@ -1,6 +1,8 @@
-"""A second restatement of the pointwise diagnostics of moloch(), in NumPy
-and written from the reference's source alone, against the C oracle's
-phases 0 (reset + pre-diagnostics) and 3 (post-diagnostics).
+"""A second restatement of parts of the step, in NumPy and written from the
+reference's source alone, against the C oracle: the pointwise diagnostics
+of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
+post-diagnostics) and the staggering of advection() (the oracle's
+stagger hook).
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
@@ -104,4 +106,65 @@ def test_postdiagnostics_restated(oracle_mod):
     expect = {"tvirt": tvirt, "t": t, "p": p, "rho": rho, "ps": ps, "qsat": pfwsat(t, p, c["ep2"])}
     for n, v in expect.items():
         assert rel(o.get(n), v) <= 1e-13, (n, rel(o.get(n), v))
+    o.close()
+
+
+# ---- staggering (nompi/mod_moloch.F90:1327-1417) ---------------------------
+# Arrays are (levels, i, j): the last axis is j.  The domain is periodic, so
+# the reference's width-2 halo copies before each stencil are index wraps.
+def uv_to_x(u, v):
+    ux = 0.5625 * (np.roll(u, -1, 2) + u) - 0.0625 * (np.roll(u, -2, 2) + np.roll(u, 1, 2))
+    vx = 0.5625 * (np.roll(v, -1, 1) + v) - 0.0625 * (np.roll(v, -2, 1) + np.roll(v, 1, 1))
+    return ux, vx
+
+
+def w_to_x(w):
+    """w has kz+1 levels (Fortran 1..kz+1), wx kz; index = Fortran level - 1."""
+    kz = w.shape[0] - 1
+    wx = np.empty((kz,) + w.shape[1:])
+    k = np.arange(1, kz - 1)
+    wx[k] = 0.5625 * (w[k + 1] + w[k]) - 0.0625 * (w[k + 2] + w[k - 1])
+    wx[0] = 0.5 * (w[1] + w[0])
+    wx[kz - 1] = 0.5 * (w[kz] + w[kz - 1])
+    return wx
+
+
+def x_to_uv(ux, vx):
+    u = 0.5625 * (ux + np.roll(ux, 1, 2)) - 0.0625 * (np.roll(ux, -1, 2) + np.roll(ux, 2, 2))
+    v = 0.5625 * (vx + np.roll(vx, 1, 1)) - 0.0625 * (np.roll(vx, -1, 1) + np.roll(vx, 2, 1))
+    return u, v
+
+
+def x_to_w(wx, w_old):
+    """Fortran levels 3..kz-1 fourth order, 2 and kz two-point; levels 1 and
+    kz+1 keep their values."""
+    kz = wx.shape[0]
+    w = w_old.copy()
+    k = np.arange(2, kz - 1)  # Fortran 3 .. kz-1
+    w[k] = 0.5625 * (wx[k] + wx[k - 1]) - 0.0625 * (wx[k + 1] + wx[k - 2])
+    w[1] = 0.5 * (wx[1] + wx[0])
+    w[kz - 1] = 0.5 * (wx[kz - 1] + wx[kz - 2])
+    return w
+
+
+def test_staggering_restated(oracle_mod):
+    o = make(oracle_mod, ("u", "v", "w"))
+    u, v, w = o.get("u"), o.get("v"), o.get("w")
+    o.stagger(True)
+    ux, vx = uv_to_x(u, v)
+    for n, want in (("ux", ux), ("vx", vx), ("wx", w_to_x(w))):
+        got = o.get(n)
+        assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), n
+    # back, from perturbed cross-point values (not a round trip of the above)
+    rng = np.random.default_rng(9)
+    for n in ("ux", "vx", "wx"):
+        a = o.get(n)
+        o.set(n, a + 0.1 * rng.standard_normal(a.shape))
+    ux, vx, wx = o.get("ux"), o.get("vx"), o.get("wx")
+    w_before = o.get("w")
+    o.stagger(False)
+    u2, v2 = x_to_uv(ux, vx)
+    for n, want in (("u", u2), ("v", v2), ("w", x_to_w(wx, w_before))):
+        got = o.get(n)
+        assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), n
     o.close()
