@@ -1282,6 +1282,16 @@ int oracle_set(void *h, const char *name, const double *in) {
   return nk;
 }
 
+/* wafone on one named field with the step's dta = dt / mo_nadv, for the
+   cross-check of tests/test_oracle_restated.py; -1 for an unknown name */
+int oracle_wafone(void *h, const char *name) {
+  Moloch *m = (Moloch *)h;
+  A3 *a = (A3 *)field3(m, name);
+  if (!a) return -1;
+  wafone(m, a, m->dt / (double)m->mo_nadv);
+  return 0;
+}
+
 /* the full bounded array (halo included), for layout-contract tests */
 int oracle_get_bounded(void *h, const char *name, double *out, int *lb, int *ub) {
   Moloch *m = (Moloch *)h;

@@ -50,6 +50,8 @@ def lib(checked=False):
                               ctypes.POINTER(ctypes.c_double)]
     L.oracle_phase.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_stagger.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.oracle_wafone.restype = ctypes.c_int
+    L.oracle_wafone.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     L.oracle_get.restype = ctypes.c_int
     L.oracle_get.argtypes = [ctypes.c_void_p, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     L.oracle_set.restype = ctypes.c_int
@@ -120,6 +122,10 @@ class Oracle:
 
     def stagger(self, to_x):
         self.L.oracle_stagger(self.h, int(to_x))
+
+    def wafone(self, name):
+        if self.L.oracle_wafone(self.h, name.encode()) < 0:
+            raise KeyError(name)
 
     def get(self, name):
         nk = self.kz + 1 if name in FIELDS_KZP1 else self.kz

@@ -1,8 +1,8 @@
 """A second restatement of parts of the step, in NumPy and written from the
 reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
-post-diagnostics) and the staggering of advection() (the oracle's
-stagger hook).
+post-diagnostics), the staggering of advection() and wafone (the
+oracle's stagger and wafone hooks).
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
@@ -167,4 +167,160 @@ def test_staggering_restated(oracle_mod):
     for n, want in (("u", u2), ("v", v2), ("w", x_to_w(wx, w_before))):
         got = o.get(n)
         assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), n
+    o.close()
+
+
+# ---- wafone, ROTLLR branch (nompi/mod_moloch.F90:929-1187) -----------------
+MINDEN = 1.0e-30  # :95
+
+
+def superbee(r):
+    # b = max(wlow, min(whigh, max(r, min(2 r, 1)))), wlow = 0, whigh = 2
+    return np.maximum(0.0, np.minimum(2.0, np.maximum(r, np.minimum(2.0 * r, 1.0))))
+
+
+def safe_den(z):
+    # sign(max(abs(z), minden), z)
+    return np.copysign(np.maximum(np.abs(z), MINDEN), z)
+
+
+class Bounded:
+    """A reference array with its Fortran bounds: a[j, i, k] -> data[k-lk, i-li, j-lj]."""
+
+    def __init__(self, o, name):
+        self.data, self.lb, _ = o.get_bounded(name)
+
+    def ji(self, j0, j1, i0, i1, k=None):
+        """Fortran ranges j0..j1, i0..i1 (inclusive) of level k (or a 2-D field)."""
+        d = self.data[0] if k is None else self.data[k - self.lb[2]]  # a 2-D field has one level
+        return d[..., i0 - self.lb[1]:i1 - self.lb[1] + 1, j0 - self.lb[0]:j1 - self.lb[0] + 1]
+
+
+def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita):
+    """pp: interior (kz, ni, nj) of the advected field; s, fmzf: interior
+    (kz+1, ni, nj); fmz, u, v, msfu, msfv, msfx: Bounded.  Returns the new
+    interior of pp."""
+    kz, ni, nj = pp.shape
+    dtrdx = dta / dx
+    dtrdy = dta / dx
+    dtrdz = 0.5 * (dta / dzita)  # do_vadvtwice
+    P = {k: pp[k - 1] for k in range(1, kz + 1)}  # Fortran level -> (ni, nj)
+    S = {k: s[k - 1] for k in range(1, kz + 2)}
+    FZ = {k: fmz.ji(1, nj, 1, ni, k) for k in range(1, kz + 1)}
+    FF = {k: fmzf[k - 1] for k in range(1, kz + 2)}
+
+    def vertical(src):
+        wfw = {1: np.zeros((ni, nj)), kz + 1: np.zeros((ni, nj))}
+        for k in range(1, kz):
+            zamu = S[k + 1] * dtrdz
+            pos = zamu >= 0.0
+            is_ = np.where(pos, 1.0, -1.0)
+            num = np.where(pos, src[k + 1] - src[min(k + 2, kz)], src[max(k - 1, 1)] - src[k])
+            r = num / safe_den(src[k] - src[k + 1])
+            b = superbee(r)
+            zphi = (is_ + zamu * b) - is_ * b
+            wfw[k + 1] = (0.5 * S[k + 1]) * ((1.0 + zphi) * src[k + 1] + (1.0 - zphi) * src[k])
+        out = {}
+        for k in range(1, kz + 1):
+            zrfmu = (dtrdz * FZ[k]) / FF[k]
+            zrfmd = (dtrdz * FZ[k]) / FF[k + 1]
+            zdv = (S[k] * zrfmu - S[k + 1] * zrfmd) * src[k]
+            out[k] = ((src[k] - wfw[k] * zrfmu) + wfw[k + 1] * zrfmd) + zdv
+        return out
+
+    wz = vertical(vertical(P))  # two passes at dt/2 (do_vadvtwice, :1022-1073)
+    new = np.empty_like(pp)
+    for k in range(1, kz + 1):
+        # meridional: wz with its periodic ring of two rows, Fortran i = -1 .. ni+2
+        w2 = wz[k]
+        ext = np.concatenate([w2[ni - 2:ni], w2, w2[0:2]], axis=0)  # row q <-> i = q - 1
+
+        def WZ(i):
+            return ext[i + 1]
+
+        imin, imax = -1, ni + 2
+        vk = v.ji(1, nj, 0, ni + 2, k)  # rows i = 0 .. ni+2
+
+        def V(i):
+            return vk[i]
+
+        zpby = {}
+        for i in range(1, ni + 2):
+            zamu = V(i) * dtrdy
+            pos = zamu > 0.0
+            is_ = np.where(pos, 1.0, -1.0)
+            ihp = min(i + 1, imax)
+            num = np.where(pos, WZ(i - 1) - WZ(max(i - 2, imin)), WZ(ihp) - WZ(max(ihp - 1, imin)))
+            r = num / safe_den(WZ(i) - WZ(i - 1))
+            b = superbee(r)
+            zphi = (is_ + zamu * b) - is_ * b
+            zpby[i] = (0.5 * V(i)) * ((1.0 + zphi) * WZ(i - 1) + (1.0 - zphi) * WZ(i))
+        fzk = fmz.ji(0, nj + 1, 0, ni + 1, k)  # rows i = 0 .. ni+1, columns j = 0 .. nj+1
+        rmv = 1.0 / msfv.ji(1, nj, 0, ni + 1)   # rows i = 0 .. ni+1
+        mx = msfx.ji(1, nj, 1, ni)
+        p0 = np.empty((ni, nj))
+        for i in range(1, ni + 1):
+            fc = fzk[i, 1:nj + 1]
+            zhxvtn = (dtrdy * rmv[i + 1]) * mx[i - 1]
+            zhxvts = (dtrdy * rmv[i]) * mx[i - 1]
+            zrfmn = ((zhxvtn * 2.0) * fc) / (fc + fzk[i + 1, 1:nj + 1])
+            zrfms = ((zhxvts * 2.0) * fc) / (fc + fzk[i - 1, 1:nj + 1])
+            zdv = (V(i + 1) * zrfmn - V(i) * zrfms) * P[k][i - 1]
+            p0[i - 1] = ((WZ(i) + zpby[i] * zrfms) - zpby[i + 1] * zrfmn) + zdv
+        # zonal: p0 with its periodic ring of two columns, Fortran j = -1 .. nj+2
+        pext = np.concatenate([p0[:, nj - 2:nj], p0, p0[:, 0:2]], axis=1)  # column q <-> j = q - 1
+
+        def P0(j):
+            return pext[:, j + 1]
+
+        jmin, jmax = -1, nj + 2
+        uk = u.ji(0, nj + 2, 1, ni, k)  # columns j = 0 .. nj+2
+        mu = msfu.ji(0, nj + 1, 1, ni)  # columns j = 0 .. nj+1
+        zpbw = {}
+        for j in range(1, nj + 2):
+            zamu = (uk[:, j] * mu[:, j]) * dtrdx
+            pos = zamu > 0.0
+            is_ = np.where(pos, 1.0, -1.0)
+            jhp = min(j + 1, jmax)
+            num = np.where(pos, P0(j - 1) - P0(max(j - 2, jmin)), P0(jhp) - P0(max(jhp - 1, jmin)))
+            r = num / safe_den(P0(j) - P0(j - 1))
+            b = superbee(r)
+            zphi = (is_ + zamu * b) - is_ * b
+            zpbw[j] = (0.5 * uk[:, j]) * ((1.0 + zphi) * P0(j - 1) + (1.0 - zphi) * P0(j))
+        for j in range(1, nj + 1):
+            fc = fzk[1:ni + 1, j]
+            zcostx = dtrdx * mu[:, j]
+            zrfme = ((zcostx * 2.0) * fc) / (fc + fzk[1:ni + 1, j + 1])
+            zrfmw = ((zcostx * 2.0) * fc) / (fc + fzk[1:ni + 1, j - 1])
+            zdv = (uk[:, j + 1] * zrfme - uk[:, j] * zrfmw) * P[k][:, j - 1]
+            new[k - 1][:, j - 1] = ((P0(j) + zpbw[j] * zrfmw) - zpbw[j + 1] * zrfme) + zdv
+    return new
+
+
+def test_wafone_restated(oracle_mod):
+    """After the staggering has filled the u, v rings (as advection() does
+    before its wafone calls), wafone of theta and of the cross-point u."""
+    o = make(oracle_mod, ("u", "v", "tetav"))
+    rng = np.random.default_rng(3)
+    for n in ("u", "v"):  # winds of both signs, so both upwind branches run
+        a = o.get(n)
+        o.set(n, a * np.where(rng.uniform(size=a.shape) < 0.5, -1.0, 1.0))
+    o.stagger(True)
+    for n in ("u", "v", "s"):
+        a = o.get(n)
+        assert (a > 0).any() and (a < 0).any(), n
+    sc = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, sc)
+    dt, dx, dzita, nadv = sc[0], sc[1], sc[2], sc[6]
+    args = dict(s=o.get("s"), fmz=Bounded(o, "fmz"), fmzf=o.get("fmzf"), u=Bounded(o, "u"),
+                v=Bounded(o, "v"), msfu=Bounded(o, "msfu"), msfv=Bounded(o, "msfv"),
+                msfx=Bounded(o, "msfx"), dta=dt / nadv, dx=dx, dzita=dzita)
+    for name in ("tetav", "ux"):
+        want = wafone_np(o.get(name), **args)
+        before = o.get(name)
+        o.wafone(name)
+        got = o.get(name)
+        assert np.max(np.abs(got - before)) > 1e-6 * np.max(np.abs(before)), name  # it moved
+        err = np.max(np.abs(got - want)) / np.max(np.abs(want))
+        assert err <= 1e-14, (name, err)
     o.close()
