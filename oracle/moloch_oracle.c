@@ -1282,6 +1282,13 @@ int oracle_set(void *h, const char *name, const double *in) {
   return nk;
 }
 
+/* divdamp with the step's dts = dt / mo_nadv / mo_nsound, for the
+   cross-check of tests/test_oracle_restated.py */
+void oracle_divdamp(void *h) {
+  Moloch *m = (Moloch *)h;
+  divdamp(m, m->dt / (double)m->mo_nadv / (double)m->mo_nsound);
+}
+
 /* wafone on one named field with the step's dta = dt / mo_nadv, for the
    cross-check of tests/test_oracle_restated.py; -1 for an unknown name */
 int oracle_wafone(void *h, const char *name) {

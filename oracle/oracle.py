@@ -50,6 +50,7 @@ def lib(checked=False):
                               ctypes.POINTER(ctypes.c_double)]
     L.oracle_phase.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_stagger.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.oracle_divdamp.argtypes = [ctypes.c_void_p]
     L.oracle_wafone.restype = ctypes.c_int
     L.oracle_wafone.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     L.oracle_get.restype = ctypes.c_int
@@ -122,6 +123,9 @@ class Oracle:
 
     def stagger(self, to_x):
         self.L.oracle_stagger(self.h, int(to_x))
+
+    def divdamp(self):
+        self.L.oracle_divdamp(self.h)
 
     def wafone(self, name):
         if self.L.oracle_wafone(self.h, name.encode()) < 0:

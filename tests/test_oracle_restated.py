@@ -1,8 +1,8 @@
 """A second restatement of parts of the step, in NumPy and written from the
 reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
-post-diagnostics), the staggering of advection() and wafone (the
-oracle's stagger and wafone hooks).
+post-diagnostics), the staggering of advection(), wafone and divdamp (the
+oracle's stagger, wafone and divdamp hooks).
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
@@ -323,4 +323,43 @@ def test_wafone_restated(oracle_mod):
         assert np.max(np.abs(got - before)) > 1e-6 * np.max(np.abs(before)), name  # it moved
         err = np.max(np.abs(got - want)) / np.max(np.abs(want))
         assert err <= 1e-14, (name, err)
+    o.close()
+
+
+# ---- divdamp, ROTLLR branch (nompi/mod_moloch.F90:853-895) -----------------
+XDAMP = 0.0625  # :96
+
+
+def divdamp_np(u, v, zdiv2, xknu, mu, dx, dts):
+    """u, v, zdiv2: interiors (kz, ni, nj); xknu (kz,); mu: msfu interior
+    (ni, nj).  The width-1 ring of zdiv2 is its periodic image
+    (:858-861).  Returns the new u, v, zdiv2."""
+    ddamp = 0.125 * (dx / dts)
+    zw = np.roll(zdiv2, 1, 2)  # zdiv2(j-1)
+    zs = np.roll(zdiv2, 1, 1)  # zdiv2(i-1)
+    c = (xknu * ddamp)[:, None, None]
+    u2 = u + ((c * mu[None]) * (zdiv2 - zw))
+    v2 = v + (c * (zdiv2 - zs))
+    ddamp = (XDAMP * 0.015625) / dts
+    p2d = 0.125 * (((zw + np.roll(zdiv2, -1, 2)) + zs) + np.roll(zdiv2, -1, 1)) - 0.5 * zdiv2
+    return u2, v2, zdiv2 + ddamp * p2d
+
+
+def test_divdamp_restated(oracle_mod):
+    o = make(oracle_mod, ("u", "v"))
+    rng = np.random.default_rng(11)
+    z = o.get("zdiv2")
+    o.set("zdiv2", z + 1e-4 * rng.standard_normal(z.shape))  # a divergence field of both signs
+    sc = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, sc)
+    dt, dx, nadv, nsound = sc[0], sc[1], sc[6], sc[7]
+    xk = (ctypes.c_double * o.kz)()
+    oracle_mod.lib().oracle_xknu(o.h, xk)
+    xknu = np.array(list(xk))
+    mu = Bounded(o, "msfu").ji(1, o.nj, 1, o.ni)
+    u2, v2, z2 = divdamp_np(o.get("u"), o.get("v"), o.get("zdiv2"), xknu, mu, dx, dt / nadv / nsound)
+    o.divdamp()
+    for n, want in (("u", u2), ("v", v2), ("zdiv2", z2)):
+        got = o.get(n)
+        assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), n
     o.close()
