@@ -1,8 +1,9 @@
 """A second restatement of parts of the step, in NumPy and written from the
 reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
-post-diagnostics), the staggering of advection(), wafone and divdamp (the
-oracle's stagger, wafone and divdamp hooks).
+post-diagnostics), sound() (phase 1), the staggering of advection(),
+wafone and divdamp (the oracle's stagger, wafone and divdamp hooks).
+Together they cover every routine of the step.
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
@@ -362,4 +363,192 @@ def test_divdamp_restated(oracle_mod):
     for n, want in (("u", u2), ("v", v2), ("zdiv2", z2)):
         got = o.get(n)
         assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), n
+    o.close()
+
+
+# ---- sound(), ROTLLR branch (nompi/mod_moloch.F90:483-851) -----------------
+WLHV = 2500610.0  # mod_constants.F90:167
+
+
+def pad1(a):
+    """The width-1 periodic ring (corners included) around (levels, i, j)."""
+    return np.pad(a, ((0, 0), (1, 1), (1, 1)), mode="wrap")
+
+
+def gzita_np(zita, ztop, a0):
+    # nompi/mod_zita.F90:109-120; ratio**2 = r r, ratio**3 = (r r) r
+    r = zita / ztop
+    r2 = r * r
+    return (((0.0 - 1.0 * a0) * r - (3.0 - 2.0 * a0) * r2) + (2.0 - 1.0 * a0) * (r2 * r)) + 1.0
+
+
+def zita_levels(kz, ztop):
+    # model_zitaf / model_zitah (nompi/mod_zita.F90:57-85), accumulated from the ground
+    dz = ztop / float(kz)
+    zf = np.zeros(kz + 1)
+    for k in range(kz - 1, -1, -1):
+        zf[k] = zf[k + 1] + dz
+    zh = np.zeros(kz)
+    zh[kz - 1] = dz * 0.5
+    for k in range(kz - 2, -1, -1):
+        zh[k] = zh[k + 1] + dz
+    return zf, zh
+
+
+def sound_np(st, sc, c, dts, nsub):
+    """One sound() call: nsub substeps of dts.  st: interiors (levels, i, j)
+    of the state and the diagnostics; sc: Bounded statics and the 1-D level
+    tables; c: constants.  Returns the new u, v, w, pai, tetav, s, deltaw,
+    zdiv2."""
+    u, v, w = st["u"].copy(), st["v"].copy(), st["w"].copy()
+    pai, tet, s, dw = st["pai"].copy(), st["tetav"].copy(), st["s"].copy(), st["deltaw"].copy()
+    kz, ni, nj = u.shape
+    cpd, rdrcv, rwat, egrav = c["cpd"], c["rdrcv"], c["rwat"], EGRAV
+    dtrdx = dts / sc["dx"]
+    dtrdy = dts / sc["dx"]
+    dtrdz = dts / sc["dzita"]
+    zcs2 = (dtrdz * dtrdz) * rdrcv
+    F = sc["fmz"].data  # (kz, ni+2, nj+2): rings i, j = 0 .. n+1
+    FI = F[:, 1:ni + 1, 1:nj + 1]
+    fmzf, qv, qc, qs_, t = st["fmzf"], st["qv"], st["qc"], st["qsat"], st["t"]
+    qwl, qwi = st["qwltot"], st["qwitot"]
+    hx = sc["hx"].ji(1, nj + 1, 1, ni)   # columns j = 1 .. nj+1
+    hy = sc["hy"].ji(1, nj, 1, ni + 1)   # rows i = 1 .. ni+1
+    mx = sc["msfx"].ji(1, nj, 1, ni)
+    mu = sc["msfu"].ji(1, nj, 1, ni)
+    rmv = 1.0 / sc["msfv"].ji(1, nj, 1, ni + 1)  # rows i = 1 .. ni+1
+    coru = sc["coru"].ji(1, nj, 1, ni)
+    corv = sc["corv"].ji(1, nj, 1, ni)
+    gk, gkh = sc["gzitak"], sc["gzitakh"]  # Fortran level k -> index k-1
+    I, J = slice(1, ni + 1), slice(1, nj + 1)
+    wwkw = np.zeros((kz + 1, ni, nj))
+    for n in range(1, nsub + 1):
+        U, V = pad1(u), pad1(v)  # rings and corners at the start of the substep (:512-527)
+        # surface w and s (:529-565)
+        zuh = U[kz - 1][I, J] * hx[:, 0:nj] + U[kz - 1][I, 2:nj + 2] * hx[:, 1:nj + 1]
+        zvh = V[kz - 1][I, J] * hy[0:ni] + V[kz - 1][2:ni + 2, J] * hy[1:ni + 1]
+        w[kz] = 0.5 * (zuh + zvh)
+        s[kz] = -w[kz]
+        for k in range(2, kz + 1):
+            uu, vv = U[k - 1] + U[k - 2], V[k - 1] + V[k - 2]
+            zuh = uu[I, J] * hx[:, 0:nj] + uu[I, 2:nj + 2] * hx[:, 1:nj + 1]
+            zvh = vv[I, J] * hy[0:ni] + vv[2:ni + 2, J] * hy[1:ni + 1]
+            s[k - 1] = -((0.25 * (zuh + zvh)) * gk[k - 1])
+        # Equation 16 (:575-597)
+        zdiv2 = np.empty((kz, ni, nj))
+        for k in range(1, kz + 1):
+            f = F[k - 1]
+            fc = f[I, J]
+            zrfmzum = 2.0 / (fc + f[I, 0:nj])
+            zrfmzvm = 2.0 / (fc + f[0:ni, J])
+            zrfmzup = 2.0 / (fc + f[I, 2:nj + 2])
+            zrfmzvp = 2.0 / (fc + f[2:ni + 2, J])
+            zum = (dtrdx * U[k - 1][I, J]) * zrfmzum
+            zup = (dtrdx * U[k - 1][I, 2:nj + 2]) * zrfmzup
+            zvm = ((dtrdy * V[k - 1][I, J]) * zrfmzvm) * rmv[0:ni]
+            zvp = ((dtrdy * V[k - 1][2:ni + 2, J]) * zrfmzvp) * rmv[1:ni + 1]
+            zdiv2[k - 1] = (fc * mx) * ((zup - zum) + (zvp - zvm))
+        u, v, zdiv2 = divdamp_np(u, v, zdiv2, sc["xknu"], mu, sc["dx"], dts)
+        for k in range(1, kz + 1):
+            zdiv2[k - 1] = zdiv2[k - 1] + (FI[k - 1] * dtrdz) * (s[k - 1] - s[k])
+        # implicit w (:634-679)
+        wwkw[kz] = 0.0
+        for k in range(kz, 1, -1):
+            a, b = k - 1, k - 2  # indices of levels k and k-1
+            dw[a] = -w[a]
+            zrom1w = ((0.5 * cpd) * fmzf[a]) * (tet[b] + tet[a])
+            zrom1w = zrom1w - (((((cpd * w[a]) * fmzf[a]) * fmzf[a]) * float(n)) * dtrdz) * (tet[b] - tet[a])
+            moist = (qv[a] > 0.96 * qs_[a]) & (w[a] > 0.1)
+            zqs = 0.5 * (qs_[a] + qs_[b])
+            zdth = ((((((egrav * w[a]) * float(n - 1)) * dts) * WLHV) * WLHV) * zqs) / \
+                ((((cpd * pai[b]) * rwat) * t[b]) * t[b])
+            zrom1w = np.where(moist, zrom1w + zdth * fmzf[a], zrom1w)
+            zwexpl = (w[a] - (zrom1w * dtrdz) * (pai[b] - pai[a])) - egrav * dts
+            zwexpl = zwexpl + ((rdrcv * zrom1w) * dtrdz) * (pai[b] * zdiv2[b] - pai[a] * zdiv2[a])
+            zu = ((zcs2 * FI[b]) * zrom1w) * pai[b] + 0.0  # + ffilt(k), zero
+            zd = ((zcs2 * FI[a]) * zrom1w) * pai[a] + 0.0
+            zrapp = 1.0 / (((1.0 + zd) + zu) - zd * wwkw[a + 1])
+            w[a] = zrapp * (zwexpl + zd * w[a + 1])
+            wwkw[a] = zrapp * zu
+        for k in range(2, kz + 1):
+            a = k - 1
+            w[a] = w[a] + wwkw[a] * w[a - 1]
+            dw[a] = dw[a] + w[a]
+        # new Exner function and theta (:683-712)
+        for k in range(1, kz + 1):
+            a = k - 1
+            zdiv2[a] = zdiv2[a] + (dtrdz * FI[a]) * (w[a] - w[a + 1])
+        zdiv2 = (zdiv2 * ((1.0 + 0.86 * qv) + 3.2 * qc)) / ((1.0 + 0.96 * qv) + 4.8 * qc)
+        tet = tet * (1.0 + (rdrcv * zdiv2) * ((0.25 * qv + 4.2 * qwl) + 2.1 * qwi))
+        TET = pad1(tet)
+        # the pai ring is filled before the update (:716-728), the deltaw ring after the solve
+        PAI = pad1(pai)
+        pai = pai * (1.0 - rdrcv * zdiv2)
+        PAI[:, I, J] = pai
+        DW = pad1(dw)
+        # ud, vd: the rings keep the values from the start of the substep (:730-735)
+        UD, VD = U.copy(), V.copy()
+        UD[:, I, J] = u
+        VD[:, I, J] = v
+        # Equations 17 and 18 (:737-787)
+        un = np.empty_like(u)
+        vn = np.empty_like(v)
+        for k in range(1, kz + 1):
+            a = k - 1
+            zcx = dtrdx * mu
+            zfz = egrav * dts + 0.25 * (((DW[a][I, 0:nj] + DW[a + 1][I, 0:nj]) + DW[a][I, J]) + DW[a + 1][I, J])
+            zrom1u = (0.5 * cpd) * (TET[a][I, 0:nj] + TET[a][I, J])
+            zcor1u = ((coru * dts) * 0.25) * (((VD[a][I, J] + VD[a][I, 0:nj]) + VD[a][2:ni + 2, 0:nj]) +
+                                               VD[a][2:ni + 2, J])
+            un[a] = ((u[a] + zcor1u) - ((zfz * hx[:, 0:nj]) * gkh[a])) - \
+                ((zcx * zrom1u) * (PAI[a][I, J] - PAI[a][I, 0:nj]))
+            zcy = dtrdy
+            zfz = egrav * dts + 0.25 * (((DW[a][0:ni, J] + DW[a + 1][0:ni, J]) + DW[a][I, J]) + DW[a + 1][I, J])
+            zrom1v = (0.5 * cpd) * (TET[a][0:ni, J] + TET[a][I, J])
+            zcor1v = ((corv * dts) * 0.25) * (((UD[a][I, J] + UD[a][0:ni, J]) + UD[a][I, 2:nj + 2]) +
+                                               UD[a][0:ni, 2:nj + 2])
+            vn[a] = ((v[a] - zcor1v) - ((zfz * hy[0:ni]) * gkh[a])) - \
+                ((zcy * zrom1v) * (PAI[a][I, J] - PAI[a][0:ni, J]))
+        u, v = un, vn
+    # complete Equation 10 (:841-849)
+    for k in range(2, kz + 1):
+        s[k - 1] = (w[k - 1] + s[k - 1]) * fmzf[k - 1]
+    s[0] = 0.0
+    s[kz] = 0.0
+    return {"u": u, "v": v, "w": w, "pai": pai, "tetav": tet, "s": s, "deltaw": dw, "zdiv2": zdiv2}
+
+
+def test_sound_restated(oracle_mod):
+    """One sound() call (five substeps) from a developed state with a moist,
+    rising region, so the latent-heat branch of the explicit w runs."""
+    o = make(oracle_mod, ("u", "v", "pai", "tetav"))
+    w = o.get("w")
+    rng = np.random.default_rng(13)
+    w[1:-1] = 0.3 * rng.standard_normal(w[1:-1].shape)  # w(1) = 0 and the surface w stay
+    o.set("w", w)
+    qv, qsat = o.get("qv"), o.get("qsat")
+    qv[:, 2:6, 3:8] = 0.98 * qsat[:, 2:6, 3:8]
+    o.set("qv", qv)
+    cst = (ctypes.c_double * 11)()
+    oracle_mod.lib().oracle_constants(cst)
+    c = {"rwat": cst[1], "cpd": cst[2], "rdrcv": cst[4]}
+    scal = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, scal)
+    dt, dx, dzita, ztop, a0, nadv, nsound = scal[0], scal[1], scal[2], scal[3], scal[5], scal[6], scal[7]
+    xk = (ctypes.c_double * o.kz)()
+    oracle_mod.lib().oracle_xknu(o.h, xk)
+    zf, zh = zita_levels(o.kz, ztop)
+    sc = {n: Bounded(o, n) for n in ("fmz", "hx", "hy", "coru", "corv", "msfu", "msfv", "msfx")}
+    sc.update(dx=dx, dzita=dzita, xknu=np.array(list(xk)), gzitak=gzita_np(zf, ztop, a0),
+              gzitakh=gzita_np(zh, ztop, a0))
+    st = {n: o.get(n) for n in ("u", "v", "w", "pai", "tetav", "s", "deltaw", "fmzf", "qv", "qc", "qsat",
+                                "t", "qwltot", "qwitot")}
+    moist = (st["qv"][1:] > 0.96 * st["qsat"][1:]) & (st["w"][1:-1] > 0.1)
+    assert moist.any()  # the latent-heat branch is taken somewhere
+    want = sound_np(st, sc, c, dt / nadv / nsound, int(nsound))
+    o.phase(1)
+    for n, v in want.items():
+        got = o.get(n)
+        err = np.max(np.abs(got - v)) / max(np.max(np.abs(v)), 1e-300)
+        assert err <= 1e-13, (n, err)
     o.close()
