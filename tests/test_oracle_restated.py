@@ -3,7 +3,8 @@ reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
 wafone and divdamp (the oracle's stagger, wafone and divdamp hooks).
-Together they cover every routine of the step.
+Together they cover the routines of the step in its default configuration
+(ROTLLR map factors, filters off), except the lprint printout.
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
