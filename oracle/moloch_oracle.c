@@ -7,11 +7,15 @@
  *
  * PARITY UNPINNED: the reference is Fortran and no Fortran compiler exists
  * on any machine this project runs on, so the reference itself cannot be
- * run and it ships no golden vectors or tests.  This restatement is pinned
- * only by known-answer checks written from the equations
- * (tests/test_oracle_known_answers.py) and by golden fixtures it generated
- * itself (tests/golden/), which guard it against regressions, not against
- * misreading the reference.
+ * run and it ships no golden vectors or tests.  This restatement is checked
+ * by known-answer checks written from the equations
+ * (tests/test_oracle_known_answers.py), by a second restatement of its
+ * routines in NumPy written from the reference's source alone
+ * (tests/test_oracle_restated.py, through the oracle_stagger,
+ * oracle_wafone and oracle_divdamp hooks and the phases), and by golden
+ * fixtures it generated itself (tests/golden/).  These catch slips and
+ * regressions, not a misreading of the reference that both restatements
+ * share.
  *
  * What it restates (paths relative to the reference project):
  *   nompi/mod_moloch.F90            moloch(), sound(), divdamp(), advection(),
