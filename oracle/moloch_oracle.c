@@ -12,7 +12,8 @@
  * (tests/test_oracle_known_answers.py), by a second restatement of its
  * routines in NumPy written from the reference's source alone
  * (tests/test_oracle_restated.py, through the oracle_stagger,
- * oracle_wafone and oracle_divdamp hooks and the phases), and by golden
+ * oracle_wafone, oracle_divdamp and oracle_filter hooks and the phases),
+ * and by golden
  * fixtures it generated itself (tests/golden/).  These catch slips and
  * regressions, not a misreading of the reference that both restatements
  * share.
@@ -1284,6 +1285,15 @@ int oracle_set(void *h, const char *name, const double *in) {
     for (int i = 1; i <= m->ni; i++)
       for (int j = 1; j <= m->nj; j++) E3(*a, j, i, k) = in[q++];
   return nk;
+}
+
+/* one 3-D filter for the cross-check of tests/test_oracle_restated.py:
+   0 divergence_filter, 1 filtpai, 2 filttheta */
+void oracle_filter(void *h, int which) {
+  Moloch *m = (Moloch *)h;
+  if (which == 0) divergence_filter(m);
+  else if (which == 1) filtpai(m);
+  else if (which == 2) filttheta(m);
 }
 
 /* divdamp with the step's dts = dt / mo_nadv / mo_nsound, for the

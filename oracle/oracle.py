@@ -51,6 +51,7 @@ def lib(checked=False):
     L.oracle_phase.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_stagger.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_divdamp.argtypes = [ctypes.c_void_p]
+    L.oracle_filter.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_wafone.restype = ctypes.c_int
     L.oracle_wafone.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     L.oracle_get.restype = ctypes.c_int
@@ -123,6 +124,9 @@ class Oracle:
 
     def stagger(self, to_x):
         self.L.oracle_stagger(self.h, int(to_x))
+
+    def filter(self, which):
+        self.L.oracle_filter(self.h, int(which))
 
     def divdamp(self):
         self.L.oracle_divdamp(self.h)

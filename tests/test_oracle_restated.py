@@ -2,9 +2,9 @@
 reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
-wafone and divdamp (the oracle's stagger, wafone and divdamp hooks).
-Together they cover the routines of the step in its default configuration
-(ROTLLR map factors, filters off), except the lprint printout.
+wafone, divdamp and the 3-D filters (the oracle's stagger, wafone, divdamp
+and filter hooks).  Together they cover the routines of the step with
+ROTLLR map factors, except the lprint printout.
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
@@ -552,4 +552,35 @@ def test_sound_restated(oracle_mod):
         got = o.get(n)
         err = np.max(np.abs(got - v)) / max(np.max(np.abs(v)), 1e-300)
         assert err <= 1e-13, (n, err)
+    o.close()
+
+
+# ---- the 3-D filters (nompi/mod_moloch.F90:423-481) ------------------------
+NUPAITQ = 0.05  # :106
+
+
+def lap_filter_np(a, coef):
+    """a + coef(k) (0.125 (aW + aE + aS + aN) - 0.5 a), ring periodic; coef
+    per level (kz,)."""
+    p2d = 0.125 * (((np.roll(a, 1, 2) + np.roll(a, -1, 2)) + np.roll(a, 1, 1)) + np.roll(a, -1, 1)) - 0.5 * a
+    return a + coef[:, None, None] * p2d
+
+
+def test_filters_restated(oracle_mod):
+    o = make(oracle_mod, ("pai", "tetav"))
+    rng = np.random.default_rng(17)
+    z = o.get("zdiv2")
+    o.set("zdiv2", z + 1e-4 * rng.standard_normal(z.shape))
+    scal = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, scal)
+    anu2 = scal[8]
+    xk = (ctypes.c_double * o.kz)()
+    oracle_mod.lib().oracle_xknu(o.h, xk)
+    xknu = np.array(list(xk))
+    for which, name, coef in ((0, "zdiv2", anu2 * xknu), (1, "pai", np.full(o.kz, NUPAITQ)),
+                              (2, "tetav", np.full(o.kz, NUPAITQ))):
+        want = lap_filter_np(o.get(name), coef)
+        o.filter(which)
+        got = o.get(name)
+        assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), name
     o.close()
