@@ -12,8 +12,8 @@
  * (tests/test_oracle_known_answers.py), by a second restatement of its
  * routines in NumPy written from the reference's source alone
  * (tests/test_oracle_restated.py, through the oracle_stagger,
- * oracle_wafone, oracle_divdamp and oracle_filter hooks and the phases),
- * and by golden
+ * oracle_wafone, oracle_divdamp, oracle_filter and oracle_set_map_factors
+ * hooks and the phases), and by golden
  * fixtures it generated itself (tests/golden/).  These catch slips and
  * regressions, not a misreading of the reference that both restatements
  * share.
@@ -1285,6 +1285,25 @@ int oracle_set(void *h, const char *name, const double *in) {
     for (int i = 1; i <= m->ni; i++)
       for (int j = 1; j <= m->nj; j++) E3(*a, j, i, k) = in[q++];
   return nk;
+}
+
+/* replace the map factors msfu, msfv, msfx (whole bounded arrays, as
+   oracle_get_bounded returns them) and redo the terms init_moloch derives
+   from them (mx2, rmu, rmv; :254-256), so the cross-check of
+   tests/test_oracle_restated.py can run the non-ROTLLR branches with map
+   factors other than 1 */
+void oracle_set_map_factors(void *h, const double *msfu, const double *msfv, const double *msfx) {
+  Moloch *m = (Moloch *)h;
+  int nj = m->nj, ni = m->ni;
+  memcpy(m->msfu.p, msfu, sizeof(double) * m->msfu.n1 * (m->msfu.u2 - m->msfu.l2 + 1));
+  memcpy(m->msfv.p, msfv, sizeof(double) * m->msfv.n1 * (m->msfv.u2 - m->msfv.l2 + 1));
+  memcpy(m->msfx.p, msfx, sizeof(double) * m->msfx.n1 * (m->msfx.u2 - m->msfx.l2 + 1));
+  for (int i = 1; i <= ni; i++)
+    for (int j = 1; j <= nj; j++) E2(m->mx2, j, i) = E2(m->msfx, j, i) * E2(m->msfx, j, i);
+  for (int i = 1; i <= ni; i++)
+    for (int j = 0; j <= nj + 1; j++) E2(m->rmu, j, i) = 1.0 / E2(m->msfu, j, i);
+  for (int i = 0; i <= ni + 1; i++)
+    for (int j = 1; j <= nj; j++) E2(m->rmv, j, i) = 1.0 / E2(m->msfv, j, i);
 }
 
 /* one 3-D filter for the cross-check of tests/test_oracle_restated.py:

@@ -52,6 +52,7 @@ def lib(checked=False):
     L.oracle_stagger.argtypes = [ctypes.c_void_p, ctypes.c_int]
     L.oracle_divdamp.argtypes = [ctypes.c_void_p]
     L.oracle_filter.argtypes = [ctypes.c_void_p, ctypes.c_int]
+    L.oracle_set_map_factors.argtypes = [ctypes.c_void_p] + [ctypes.POINTER(ctypes.c_double)] * 3
     L.oracle_wafone.restype = ctypes.c_int
     L.oracle_wafone.argtypes = [ctypes.c_void_p, ctypes.c_char_p]
     L.oracle_get.restype = ctypes.c_int
@@ -124,6 +125,11 @@ class Oracle:
 
     def stagger(self, to_x):
         self.L.oracle_stagger(self.h, int(to_x))
+
+    def set_map_factors(self, msfu, msfv, msfx):
+        """Whole bounded arrays in the layout get_bounded returns."""
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (msfu, msfv, msfx)]
+        self.L.oracle_set_map_factors(self.h, *[a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)) for a in arrs])
 
     def filter(self, which):
         self.L.oracle_filter(self.h, int(which))

@@ -3,8 +3,9 @@ reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
 wafone, divdamp and the 3-D filters (the oracle's stagger, wafone, divdamp
-and filter hooks).  Together they cover the routines of the step with
-ROTLLR map factors, except the lprint printout.
+and filter hooks).  Together they cover the routines of the step, except
+the lprint printout; wafone and sound() in both map-factor branches, the
+non-ROTLLR one with map factors other than 1 (oracle_set_map_factors).
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
 tetav before the advection loop), :355-391 (tvirt, t, p, rho, the
@@ -16,6 +17,7 @@ last bit)."""
 import ctypes
 
 import numpy as np
+import pytest
 
 P00 = 1.0e5
 LRATE = 0.00649
@@ -56,13 +58,13 @@ def rel(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
 
 
-def make(oracle_mod, names):
+def make(oracle_mod, names, rotllr=True):
     """A developed state (one step: moisture, winds and theta no longer the
     initial profiles), then the inputs of the phase under test perturbed by
     a seeded relative 1e-3, so that the phase's outputs cannot be left over
     from the step's own diagnostics."""
     cfg = oracle_mod.make_cfg(13, 11, 9, hills=((300.0, 6.5, 5.5, 3.0),), pert_amp=0.5, pert_levels=9,
-                              seed=42, u0=3.0, v0=-2.0)
+                              seed=42, u0=3.0, v0=-2.0, rotllr=rotllr)
     o = oracle_mod.Oracle(cfg)
     o.step(1)
     rng = np.random.default_rng(5)
@@ -198,10 +200,10 @@ class Bounded:
         return d[..., i0 - self.lb[1]:i1 - self.lb[1] + 1, j0 - self.lb[0]:j1 - self.lb[0] + 1]
 
 
-def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita):
+def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita, rotllr=True):
     """pp: interior (kz, ni, nj) of the advected field; s, fmzf: interior
     (kz+1, ni, nj); fmz, u, v, msfu, msfv, msfx: Bounded.  Returns the new
-    interior of pp."""
+    interior of pp.  rotllr False: the map-factor branch (:1189-1298)."""
     kz, ni, nj = pp.shape
     dtrdx = dta / dx
     dtrdy = dta / dx
@@ -246,9 +248,12 @@ def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita):
         def V(i):
             return vk[i]
 
+        rmv = 1.0 / msfv.ji(1, nj, 0, ni + 1)   # rows i = 0 .. ni+1
+        mx = msfx.ji(1, nj, 1, ni)
+        mx2 = mx * mx
         zpby = {}
         for i in range(1, ni + 2):
-            zamu = V(i) * dtrdy
+            zamu = V(i) * dtrdy if rotllr else (V(i) * rmv[i]) * dtrdy
             pos = zamu > 0.0
             is_ = np.where(pos, 1.0, -1.0)
             ihp = min(i + 1, imax)
@@ -256,19 +261,24 @@ def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita):
             r = num / safe_den(WZ(i) - WZ(i - 1))
             b = superbee(r)
             zphi = (is_ + zamu * b) - is_ * b
-            zpby[i] = (0.5 * V(i)) * ((1.0 + zphi) * WZ(i - 1) + (1.0 - zphi) * WZ(i))
+            vh = 0.5 * V(i) if rotllr else (0.5 * V(i)) * rmv[i]
+            zpby[i] = vh * ((1.0 + zphi) * WZ(i - 1) + (1.0 - zphi) * WZ(i))
         fzk = fmz.ji(0, nj + 1, 0, ni + 1, k)  # rows i = 0 .. ni+1, columns j = 0 .. nj+1
-        rmv = 1.0 / msfv.ji(1, nj, 0, ni + 1)   # rows i = 0 .. ni+1
-        mx = msfx.ji(1, nj, 1, ni)
         p0 = np.empty((ni, nj))
         for i in range(1, ni + 1):
             fc = fzk[i, 1:nj + 1]
-            zhxvtn = (dtrdy * rmv[i + 1]) * mx[i - 1]
-            zhxvts = (dtrdy * rmv[i]) * mx[i - 1]
-            zrfmn = ((zhxvtn * 2.0) * fc) / (fc + fzk[i + 1, 1:nj + 1])
-            zrfms = ((zhxvts * 2.0) * fc) / (fc + fzk[i - 1, 1:nj + 1])
-            zdv = (V(i + 1) * zrfmn - V(i) * zrfms) * P[k][i - 1]
-            p0[i - 1] = ((WZ(i) + zpby[i] * zrfms) - zpby[i + 1] * zrfmn) + zdv
+            if rotllr:
+                zhxvtn = (dtrdy * rmv[i + 1]) * mx[i - 1]
+                zhxvts = (dtrdy * rmv[i]) * mx[i - 1]
+                zrfmn = ((zhxvtn * 2.0) * fc) / (fc + fzk[i + 1, 1:nj + 1])
+                zrfms = ((zhxvts * 2.0) * fc) / (fc + fzk[i - 1, 1:nj + 1])
+                zdv = (V(i + 1) * zrfmn - V(i) * zrfms) * P[k][i - 1]
+                p0[i - 1] = ((WZ(i) + zpby[i] * zrfms) - zpby[i + 1] * zrfmn) + zdv
+            else:
+                zrfmn = ((dtrdy * 2.0) * fc) / (fc + fzk[i + 1, 1:nj + 1])
+                zrfms = ((dtrdy * 2.0) * fc) / (fc + fzk[i - 1, 1:nj + 1])
+                zdv = ((V(i + 1) * rmv[i + 1]) * zrfmn - (V(i) * rmv[i]) * zrfms) * P[k][i - 1]
+                p0[i - 1] = WZ(i) + mx2[i - 1] * ((zpby[i] * zrfms - zpby[i + 1] * zrfmn) + zdv)
         # zonal: p0 with its periodic ring of two columns, Fortran j = -1 .. nj+2
         pext = np.concatenate([p0[:, nj - 2:nj], p0, p0[:, 0:2]], axis=1)  # column q <-> j = q - 1
 
@@ -278,9 +288,10 @@ def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita):
         jmin, jmax = -1, nj + 2
         uk = u.ji(0, nj + 2, 1, ni, k)  # columns j = 0 .. nj+2
         mu = msfu.ji(0, nj + 1, 1, ni)  # columns j = 0 .. nj+1
+        rmu = 1.0 / mu
         zpbw = {}
         for j in range(1, nj + 2):
-            zamu = (uk[:, j] * mu[:, j]) * dtrdx
+            zamu = (uk[:, j] * mu[:, j]) * dtrdx if rotllr else (uk[:, j] * rmu[:, j]) * dtrdx
             pos = zamu > 0.0
             is_ = np.where(pos, 1.0, -1.0)
             jhp = min(j + 1, jmax)
@@ -288,21 +299,31 @@ def wafone_np(pp, s, fmz, fmzf, u, v, msfu, msfv, msfx, dta, dx, dzita):
             r = num / safe_den(P0(j) - P0(j - 1))
             b = superbee(r)
             zphi = (is_ + zamu * b) - is_ * b
-            zpbw[j] = (0.5 * uk[:, j]) * ((1.0 + zphi) * P0(j - 1) + (1.0 - zphi) * P0(j))
+            uh = 0.5 * uk[:, j] if rotllr else (0.5 * uk[:, j]) * rmu[:, j]
+            zpbw[j] = uh * ((1.0 + zphi) * P0(j - 1) + (1.0 - zphi) * P0(j))
         for j in range(1, nj + 1):
             fc = fzk[1:ni + 1, j]
-            zcostx = dtrdx * mu[:, j]
-            zrfme = ((zcostx * 2.0) * fc) / (fc + fzk[1:ni + 1, j + 1])
-            zrfmw = ((zcostx * 2.0) * fc) / (fc + fzk[1:ni + 1, j - 1])
-            zdv = (uk[:, j + 1] * zrfme - uk[:, j] * zrfmw) * P[k][:, j - 1]
-            new[k - 1][:, j - 1] = ((P0(j) + zpbw[j] * zrfmw) - zpbw[j + 1] * zrfme) + zdv
+            if rotllr:
+                zcostx = dtrdx * mu[:, j]
+                zrfme = ((zcostx * 2.0) * fc) / (fc + fzk[1:ni + 1, j + 1])
+                zrfmw = ((zcostx * 2.0) * fc) / (fc + fzk[1:ni + 1, j - 1])
+                zdv = (uk[:, j + 1] * zrfme - uk[:, j] * zrfmw) * P[k][:, j - 1]
+                new[k - 1][:, j - 1] = ((P0(j) + zpbw[j] * zrfmw) - zpbw[j + 1] * zrfme) + zdv
+            else:
+                zrfme = ((dtrdx * 2.0) * fc) / (fc + fzk[1:ni + 1, j + 1])
+                zrfmw = ((dtrdx * 2.0) * fc) / (fc + fzk[1:ni + 1, j - 1])
+                zdv = ((uk[:, j + 1] * rmu[:, j + 1]) * zrfme - (uk[:, j] * rmu[:, j]) * zrfmw) * P[k][:, j - 1]
+                new[k - 1][:, j - 1] = P0(j) + mx2[:, j - 1] * ((zpbw[j] * zrfmw - zpbw[j + 1] * zrfme) + zdv)
     return new
 
 
-def test_wafone_restated(oracle_mod):
+@pytest.mark.parametrize("rotllr", [True, False])
+def test_wafone_restated(oracle_mod, rotllr):
     """After the staggering has filled the u, v rings (as advection() does
     before its wafone calls), wafone of theta and of the cross-point u."""
-    o = make(oracle_mod, ("u", "v", "tetav"))
+    o = make(oracle_mod, ("u", "v", "tetav"), rotllr=rotllr)
+    if not rotllr:
+        skew_map_factors(o, 23)
     rng = np.random.default_rng(3)
     for n in ("u", "v"):  # winds of both signs, so both upwind branches run
         a = o.get(n)
@@ -316,7 +337,7 @@ def test_wafone_restated(oracle_mod):
     dt, dx, dzita, nadv = sc[0], sc[1], sc[2], sc[6]
     args = dict(s=o.get("s"), fmz=Bounded(o, "fmz"), fmzf=o.get("fmzf"), u=Bounded(o, "u"),
                 v=Bounded(o, "v"), msfu=Bounded(o, "msfu"), msfv=Bounded(o, "msfv"),
-                msfx=Bounded(o, "msfx"), dta=dt / nadv, dx=dx, dzita=dzita)
+                msfx=Bounded(o, "msfx"), dta=dt / nadv, dx=dx, dzita=dzita, rotllr=rotllr)
     for name in ("tetav", "ux"):
         want = wafone_np(o.get(name), **args)
         before = o.get(name)
@@ -332,16 +353,17 @@ def test_wafone_restated(oracle_mod):
 XDAMP = 0.0625  # :96
 
 
-def divdamp_np(u, v, zdiv2, xknu, mu, dx, dts):
+def divdamp_np(u, v, zdiv2, xknu, mu, dx, dts, mv=None):
     """u, v, zdiv2: interiors (kz, ni, nj); xknu (kz,); mu: msfu interior
-    (ni, nj).  The width-1 ring of zdiv2 is its periodic image
+    (ni, nj); mv: msfv interior for the non-ROTLLR form (:874-881), None
+    for ROTLLR.  The width-1 ring of zdiv2 is its periodic image
     (:858-861).  Returns the new u, v, zdiv2."""
     ddamp = 0.125 * (dx / dts)
     zw = np.roll(zdiv2, 1, 2)  # zdiv2(j-1)
     zs = np.roll(zdiv2, 1, 1)  # zdiv2(i-1)
     c = (xknu * ddamp)[:, None, None]
     u2 = u + ((c * mu[None]) * (zdiv2 - zw))
-    v2 = v + (c * (zdiv2 - zs))
+    v2 = v + (c * (zdiv2 - zs)) if mv is None else v + ((c * mv[None]) * (zdiv2 - zs))
     ddamp = (XDAMP * 0.015625) / dts
     p2d = 0.125 * (((zw + np.roll(zdiv2, -1, 2)) + zs) + np.roll(zdiv2, -1, 1)) - 0.5 * zdiv2
     return u2, v2, zdiv2 + ddamp * p2d
@@ -396,7 +418,7 @@ def zita_levels(kz, ztop):
     return zf, zh
 
 
-def sound_np(st, sc, c, dts, nsub):
+def sound_np(st, sc, c, dts, nsub, rotllr=True):
     """One sound() call: nsub substeps of dts.  st: interiors (levels, i, j)
     of the state and the diagnostics; sc: Bounded statics and the 1-D level
     tables; c: constants.  Returns the new u, v, w, pai, tetav, s, deltaw,
@@ -418,6 +440,8 @@ def sound_np(st, sc, c, dts, nsub):
     mx = sc["msfx"].ji(1, nj, 1, ni)
     mu = sc["msfu"].ji(1, nj, 1, ni)
     rmv = 1.0 / sc["msfv"].ji(1, nj, 1, ni + 1)  # rows i = 1 .. ni+1
+    rmu = 1.0 / sc["msfu"].ji(1, nj + 1, 1, ni)  # columns j = 1 .. nj+1
+    mv = sc["msfv"].ji(1, nj, 1, ni)
     coru = sc["coru"].ji(1, nj, 1, ni)
     corv = sc["corv"].ji(1, nj, 1, ni)
     gk, gkh = sc["gzitak"], sc["gzitakh"]  # Fortran level k -> index k-1
@@ -444,12 +468,19 @@ def sound_np(st, sc, c, dts, nsub):
             zrfmzvm = 2.0 / (fc + f[0:ni, J])
             zrfmzup = 2.0 / (fc + f[I, 2:nj + 2])
             zrfmzvp = 2.0 / (fc + f[2:ni + 2, J])
-            zum = (dtrdx * U[k - 1][I, J]) * zrfmzum
-            zup = (dtrdx * U[k - 1][I, 2:nj + 2]) * zrfmzup
-            zvm = ((dtrdy * V[k - 1][I, J]) * zrfmzvm) * rmv[0:ni]
-            zvp = ((dtrdy * V[k - 1][2:ni + 2, J]) * zrfmzvp) * rmv[1:ni + 1]
-            zdiv2[k - 1] = (fc * mx) * ((zup - zum) + (zvp - zvm))
-        u, v, zdiv2 = divdamp_np(u, v, zdiv2, sc["xknu"], mu, sc["dx"], dts)
+            if rotllr:
+                zum = (dtrdx * U[k - 1][I, J]) * zrfmzum
+                zup = (dtrdx * U[k - 1][I, 2:nj + 2]) * zrfmzup
+                zvm = ((dtrdy * V[k - 1][I, J]) * zrfmzvm) * rmv[0:ni]
+                zvp = ((dtrdy * V[k - 1][2:ni + 2, J]) * zrfmzvp) * rmv[1:ni + 1]
+                zdiv2[k - 1] = (fc * mx) * ((zup - zum) + (zvp - zvm))
+            else:  # :598-621
+                zum = ((dtrdx * U[k - 1][I, J]) * rmu[:, 0:nj]) * zrfmzum
+                zup = ((dtrdx * U[k - 1][I, 2:nj + 2]) * rmu[:, 1:nj + 1]) * zrfmzup
+                zvm = ((dtrdy * V[k - 1][I, J]) * rmv[0:ni]) * zrfmzvm
+                zvp = ((dtrdy * V[k - 1][2:ni + 2, J]) * rmv[1:ni + 1]) * zrfmzvp
+                zdiv2[k - 1] = ((mx * mx) * fc) * ((zup - zum) + (zvp - zvm))
+        u, v, zdiv2 = divdamp_np(u, v, zdiv2, sc["xknu"], mu, sc["dx"], dts, None if rotllr else mv)
         for k in range(1, kz + 1):
             zdiv2[k - 1] = zdiv2[k - 1] + (FI[k - 1] * dtrdz) * (s[k - 1] - s[k])
         # implicit w (:634-679)
@@ -503,7 +534,7 @@ def sound_np(st, sc, c, dts, nsub):
                                                VD[a][2:ni + 2, J])
             un[a] = ((u[a] + zcor1u) - ((zfz * hx[:, 0:nj]) * gkh[a])) - \
                 ((zcx * zrom1u) * (PAI[a][I, J] - PAI[a][I, 0:nj]))
-            zcy = dtrdy
+            zcy = dtrdy if rotllr else dtrdy * mv  # :797 non-ROTLLR
             zfz = egrav * dts + 0.25 * (((DW[a][0:ni, J] + DW[a + 1][0:ni, J]) + DW[a][I, J]) + DW[a + 1][I, J])
             zrom1v = (0.5 * cpd) * (TET[a][0:ni, J] + TET[a][I, J])
             zcor1v = ((corv * dts) * 0.25) * (((UD[a][I, J] + UD[a][0:ni, J]) + UD[a][I, 2:nj + 2]) +
@@ -519,10 +550,22 @@ def sound_np(st, sc, c, dts, nsub):
     return {"u": u, "v": v, "w": w, "pai": pai, "tetav": tet, "s": s, "deltaw": dw, "zdiv2": zdiv2}
 
 
-def test_sound_restated(oracle_mod):
+def skew_map_factors(o, seed):
+    """Map factors within 5 % of 1 instead of the idealized grid's 1, so the
+    non-ROTLLR branches' factors change the result."""
+    rng = np.random.default_rng(seed)
+    arrs = [o.get_bounded(n)[0] for n in ("msfu", "msfv", "msfx")]
+    o.set_map_factors(*[a * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, a.shape)) for a in arrs])
+
+
+@pytest.mark.parametrize("rotllr", [True, False])
+def test_sound_restated(oracle_mod, rotllr):
     """One sound() call (five substeps) from a developed state with a moist,
-    rising region, so the latent-heat branch of the explicit w runs."""
-    o = make(oracle_mod, ("u", "v", "pai", "tetav"))
+    rising region, so the latent-heat branch of the explicit w runs.  The
+    non-ROTLLR case runs with map factors other than 1."""
+    o = make(oracle_mod, ("u", "v", "pai", "tetav"), rotllr=rotllr)
+    if not rotllr:
+        skew_map_factors(o, 21)
     w = o.get("w")
     rng = np.random.default_rng(13)
     w[1:-1] = 0.3 * rng.standard_normal(w[1:-1].shape)  # w(1) = 0 and the surface w stay
@@ -546,7 +589,7 @@ def test_sound_restated(oracle_mod):
                                 "t", "qwltot", "qwitot")}
     moist = (st["qv"][1:] > 0.96 * st["qsat"][1:]) & (st["w"][1:-1] > 0.1)
     assert moist.any()  # the latent-heat branch is taken somewhere
-    want = sound_np(st, sc, c, dt / nadv / nsound, int(nsound))
+    want = sound_np(st, sc, c, dt / nadv / nsound, int(nsound), rotllr)
     o.phase(1)
     for n, v in want.items():
         got = o.get(n)
