@@ -1205,7 +1205,7 @@ int oracle_step(void *h, int istep, int lprint, double *diag) {
 }
 
 /* the staggering of advection() alone, for the cross-check of
-   tests/test_oracle_diagnostics.py: to_x = 1 runs uvstagtox + wstagtox
+   tests/test_oracle_restated.py: to_x = 1 runs uvstagtox + wstagtox
    (u, v, w -> ux, vx, wx), 0 runs xtouvstag + xtowstag (back) */
 void oracle_stagger(void *h, int to_x) {
   Moloch *m = (Moloch *)h;

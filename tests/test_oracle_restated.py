@@ -3,8 +3,8 @@ reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
 wafone, divdamp and the 3-D filters (the oracle's stagger, wafone, divdamp
-and filter hooks).  Together they cover the routines of the step, except
-the lprint printout; wafone and sound() in both map-factor branches, the
+and filter hooks) and the lprint printout.  Together they cover the
+routines of the step; wafone and sound() in both map-factor branches, the
 non-ROTLLR one with map factors other than 1 (oracle_set_map_factors).
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
@@ -626,4 +626,16 @@ def test_filters_restated(oracle_mod):
         o.filter(which)
         got = o.get(name)
         assert np.max(np.abs(got - want)) <= 1e-15 * np.max(np.abs(want)), name
+    o.close()
+
+
+# ---- the lprint printout (nompi/mod_moloch.F90:395-411) --------------------
+def test_lprint_restated(oracle_mod):
+    """maxval/minval of ps over the interior and of u, v over the interior
+    columns and all levels, as moloch(istep, .true.) prints them."""
+    o = make(oracle_mod, ())
+    bad, d = o.step(2, lprint=True)
+    ps, u, v = o.get("ps"), o.get("u"), o.get("v")
+    assert bad == 0
+    assert d == [ps.max(), ps.min(), u.max(), u.min(), v.max(), v.min()]
     o.close()
