@@ -3,8 +3,9 @@ reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
 wafone, divdamp and the 3-D filters (the oracle's stagger, wafone, divdamp
-and filter hooks) and the lprint printout.  Together they cover the
-routines of the step; wafone and sound() in both map-factor branches, the
+and filter hooks), the lprint printout and the initial state of
+fill_atmosphere.  Together they cover the routines of the step; wafone and
+sound() in both map-factor branches, the
 non-ROTLLR one with map factors other than 1 (oracle_set_map_factors).
 
 Reference: nompi/mod_moloch.F90:289-323 (p, qsat, tvirt, qwltot, qwitot,
@@ -638,4 +639,62 @@ def test_lprint_restated(oracle_mod):
     ps, u, v = o.get("ps"), o.get("u"), o.get("v")
     assert bad == 0
     assert d == [ps.max(), ps.min(), u.max(), u.min(), v.max(), v.min()]
+    o.close()
+
+
+# ---- the initial state: fill_atmosphere (nompi/mod_atmosphere.F90:171-235) -
+def test_fill_atmosphere_restated(oracle_mod):
+    """qv, t (with the warm bubble on the lowest level) and the hydrostatic
+    pai of the idealized state over a hill, from the oracle's zeta and
+    fmzf.  The bubble radius mixes default-REAL and FP64 arithmetic (:199:
+    real(iy)/5_rkx is a default-REAL division, and md is a default-REAL
+    sqrt), restated here with float32."""
+    jx, iy, kz = 23, 19, 12
+    cfg = oracle_mod.make_cfg(jx, iy, kz, hills=((600.0, 9.0, 11.0, 4.0),), pert_amp=0.0)
+    o = oracle_mod.Oracle(cfg)
+    cst = (ctypes.c_double * 11)()
+    oracle_mod.lib().oracle_constants(cst)
+    rgas, cpd, rovcp, ep1 = cst[0], cst[2], cst[6], cst[7]
+    scal = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, scal)
+    dzita = scal[2]
+    zeta, fmzf = o.get("zeta"), o.get("fmzf")
+    ts, qs, ps, tropoh = 300.0, 0.01865, 101480.0, 15000.0
+    tvs = ts * (1.0 + ep1 * qs)
+    tvt = tvs - LRATE * tropoh
+    low = zeta < tropoh
+    qi = (qs * np.exp(-zeta / 4000.0)) * np.exp((-zeta / 7500.0) ** 2)
+    qv = np.where(low, qi, 1.0e-8)
+    t = np.where(low, (tvs - LRATE * zeta) / (1.0 + qi), tvt)
+    mx, my = jx // 2, iy // 2
+    bi = np.float32(np.float32(iy) / np.float32(5))
+    mr = np.sqrt((float(np.float32(jx)) / 5.0) ** 2 + float(bi * bi)) / 2.0
+    j = np.arange(1, jx + 1)[None, :]
+    i = np.arange(1, iy + 1)[:, None]
+    fj, fi = (j - mx).astype(np.float32), (i - my).astype(np.float32)
+    md = np.sqrt(fj * fj + fi * fi).astype(np.float64)  # float32 sqrt, widened
+    t[kz - 1] = np.where(md < mr, t[kz - 1] + (mr - md) / mr, t[kz - 1])
+    pai = np.empty_like(t)
+    zdelta = zeta[kz - 1] * EGRAV
+    tv1 = t[kz - 1] * (1.0 + ep1 * qv[kz - 1])
+    tv2 = t[kz - 2] * (1.0 + ep1 * qv[kz - 2])
+    lrt = (tv2 - tv1) / (zeta[kz - 2] - zeta[kz - 1])
+    lrt = 0.65 * lrt - 0.35 * LRATE
+    tv = tv1 - (0.5 * zeta[kz - 1]) * lrt
+    zz = 1.0 / (rgas * tv)
+    p = ps * np.exp(-zdelta * zz)
+    pai[kz - 1] = (p / P00) ** rovcp
+    for k in range(kz - 1, 0, -1):  # Fortran k = kz-1 .. 1; index k-1
+        a = k - 1
+        tv1 = t[a] * (1.0 + ep1 * qv[a])
+        tv2 = t[a + 1] * (1.0 + ep1 * qv[a + 1])
+        zb = (((2.0 * EGRAV) * dzita) / (fmzf[a + 1] * cpd) + tv1) - tv2
+        zd = np.sqrt(zb * zb + (4.0 * tv2) * tv1)
+        pai[a] = -((pai[a + 1] / (2.0 * tv2)) * (zb - zd))
+    assert (md < mr).any() and (md >= mr).any()  # the bubble covers part of the level
+    for n, want in (("qv", qv), ("t", t), ("pai", pai)):
+        got = o.get(n)
+        err = np.max(np.abs(got - want) / np.abs(want))
+        assert err <= 1e-14, (n, err)
+    assert np.all(o.get("u") == 1.0) and np.all(o.get("v") == 1.0)
     o.close()
