@@ -3,8 +3,8 @@ reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
 wafone, divdamp and the 3-D filters (the oracle's stagger, wafone, divdamp
-and filter hooks), the lprint printout and the initial state of
-fill_atmosphere.  Together they cover the routines of the step; wafone and
+and filter hooks), the lprint printout and the initial state of param()
+and fill_atmosphere.  Together they cover the routines of the step; wafone and
 sound() in both map-factor branches, the
 non-ROTLLR one with map factors other than 1 (oracle_set_map_factors).
 
@@ -697,4 +697,71 @@ def test_fill_atmosphere_restated(oracle_mod):
         err = np.max(np.abs(got - want) / np.abs(want))
         assert err <= 1e-14, (n, err)
     assert np.all(o.get("u") == 1.0) and np.all(o.get("v") == 1.0)
+    o.close()
+
+
+# ---- param(): orography terms and the zita metric (regcm_dynamical_core.F90:93-194,
+# ---- nompi/mod_zita.F90:88-179) --------------------------------------------
+def zfz_np(ztop, zh):
+    return ztop / (np.exp(ztop / zh) - 1.0)
+
+
+def md_zeta_np(zita, geopot, ztop, zh, a0):
+    orog = geopot * (1.0 / EGRAV)  # geopot * regrav
+    return orog * (gzita_np(zita, ztop, a0) - 1.0) + zfz_np(ztop, zh) * (np.exp(zita / zh) - 1.0)
+
+
+def md_fmz_np(zita, geopot, ztop, zh, a0):
+    orog = geopot * (1.0 / EGRAV)
+    r = zita / ztop
+    gzp = (((0.0 - 1.0 * a0) * 1.0 - (6.0 - 4.0 * a0) * r) + (6.0 - 3.0 * a0) * (r * r)) / ztop
+    bzp = (zfz_np(ztop, zh) * np.exp(zita / zh)) / zh
+    return 1.0 / (gzp * orog + bzp)
+
+
+def test_param_restated(oracle_mod):
+    """hx, hy from the orography (with the ghosts of ht at 0, never set by
+    the reference), zeta, fmz and fmzf on the zita levels, and their
+    periodic rings, for hills that reach the domain's edges."""
+    jx, iy, kz = 17, 14, 10
+    cfg = oracle_mod.make_cfg(jx, iy, kz, hills=((700.0, 2.0, 3.0, 3.0), (400.0, 15.0, 12.0, 2.5)))
+    o = oracle_mod.Oracle(cfg)
+    scal = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, scal)
+    dx, ztop, zh, a0 = scal[1], scal[3], scal[4], scal[5]
+    ht_b = Bounded(o, "ht")
+    assert ht_b.lb[:2] == (-1, -1)
+    full = ht_b.data[0]
+    ring = full.copy()
+    ring[2:iy + 2, 2:jx + 2] = 0.0
+    assert np.all(ring == 0.0)  # the ghosts stay 0
+    ht = np.zeros((iy + 2, jx + 2))  # i, j = 0 .. n+1, ghosts 0
+    ht[1:iy + 1, 1:jx + 1] = full[2:iy + 2, 2:jx + 2]
+    rdx, regrav = 1.0 / dx, 1.0 / EGRAV
+    hx = np.empty((iy, jx + 2))
+    hx[:, 1:jx + 1] = (((ht[1:iy + 1, 1:jx + 1] - ht[1:iy + 1, 0:jx]) * 1.0) * rdx) * regrav  # msfu = 1
+    hx[:, 0], hx[:, jx + 1] = hx[:, jx], hx[:, 1]
+    hy = np.empty((iy + 2, jx))
+    hy[1:iy + 1] = ((ht[1:iy + 1, 1:jx + 1] - ht[0:iy, 1:jx + 1]) * rdx) * regrav
+    hy[0], hy[iy + 1] = hy[iy], hy[1]
+    assert np.array_equal(Bounded(o, "hx").data[0], hx)
+    assert np.array_equal(Bounded(o, "hy").data[0], hy)
+    assert hx[:, 1].any() and hy[1].any()  # the hills reach the first row and column
+    zf, zhf = zita_levels(kz, ztop)
+    g = ht[1:iy + 1, 1:jx + 1]
+    zeta = np.stack([md_zeta_np(zhf[k], g, ztop, zh, a0) for k in range(kz)])
+    fmz = np.stack([md_fmz_np(zhf[k], g, ztop, zh, a0) for k in range(kz)])
+    fmzf = np.stack([md_fmz_np(zf[k], g, ztop, zh, a0) for k in range(kz + 1)])
+    zeta_b = np.pad(zeta, ((0, 0), (2, 2), (2, 2)), mode="wrap")
+    fmz_b = np.pad(fmz, ((0, 0), (1, 1), (1, 1)), mode="wrap")
+    for n, want, tol in (("zeta", zeta_b, 1e-14), ("fmz", fmz_b, 1e-14)):
+        got = Bounded(o, n).data
+        # the rings' corners are not filled by the reference (never read)
+        mask = np.ones(want.shape[1:], bool)
+        w = 2 if n == "zeta" else 1
+        mask[:w, :w] = mask[:w, -w:] = mask[-w:, :w] = mask[-w:, -w:] = False
+        err = np.max(np.abs(got[:, mask] - want[:, mask]) / np.abs(want[:, mask]))
+        assert err <= tol, (n, err)
+    err = np.max(np.abs(o.get("fmzf") - fmzf) / np.abs(fmzf))
+    assert err <= 1e-14, ("fmzf", err)
     o.close()
