@@ -3,8 +3,8 @@ reference's source alone, against the C oracle: the pointwise diagnostics
 of moloch() (the oracle's phases 0, reset + pre-diagnostics, and 3,
 post-diagnostics), sound() (phase 1), the staggering of advection(),
 wafone, divdamp and the 3-D filters (the oracle's stagger, wafone, divdamp
-and filter hooks), the lprint printout and the initial state of param()
-and fill_atmosphere.  Together they cover the routines of the step; wafone and
+and filter hooks), the lprint printout, one whole step composed from those
+pieces, and the initial state of param() and fill_atmosphere.  Together they cover the routines of the step; wafone and
 sound() in both map-factor branches, the
 non-ROTLLR one with map factors other than 1 (oracle_set_map_factors).
 
@@ -764,4 +764,75 @@ def test_param_restated(oracle_mod):
         assert err <= tol, (n, err)
     err = np.max(np.abs(o.get("fmzf") - fmzf) / np.abs(fmzf))
     assert err <= 1e-14, ("fmzf", err)
+    o.close()
+
+
+# ---- one whole moloch() step from the pieces above (nompi/mod_moloch.F90:272-421)
+class Padded(Bounded):
+    """A periodic field with a ring of width w on the j and i sides."""
+
+    def __init__(self, a, w):
+        self.data = np.pad(a, ((0, 0), (w, w), (w, w)), mode="wrap")
+        self.lb = (1 - w, 1 - w, 1)
+
+
+def test_whole_step_restated(oracle_mod):
+    """reset_tendencies, the pre-diagnostics, three times sound() and
+    advection() (ten fields), the post-diagnostics, composed in the order of
+    moloch() from the restatements above, against one oracle step."""
+    o = make(oracle_mod, ("u", "v", "t", "pai"))
+    cst = (ctypes.c_double * 11)()
+    oracle_mod.lib().oracle_constants(cst)
+    c = {"rgas": cst[0], "rwat": cst[1], "cpd": cst[2], "rdrcv": cst[4], "cpovr": cst[5], "ep1": cst[7],
+         "ep2": cst[8]}
+    scal = (ctypes.c_double * 9)()
+    oracle_mod.lib().oracle_scalars(o.h, scal)
+    dt, dx, dzita, ztop, a0, nadv, nsound = scal[0], scal[1], scal[2], scal[3], scal[5], int(scal[6]), int(scal[7])
+    xk = (ctypes.c_double * o.kz)()
+    oracle_mod.lib().oracle_xknu(o.h, xk)
+    zf, zh = zita_levels(o.kz, ztop)
+    sc = {n: Bounded(o, n) for n in ("fmz", "hx", "hy", "coru", "corv", "msfu", "msfv", "msfx")}
+    sc.update(dx=dx, dzita=dzita, xknu=np.array(list(xk)), gzitak=gzita_np(zf, ztop, a0),
+              gzitakh=gzita_np(zh, ztop, a0))
+    f = {n: o.get(n) for n in ("u", "v", "w", "pai", "t", "qv", "qc", "qi", "qr", "qs", "fmzf", "zeta")}
+    kz = o.kz
+    # reset_tendencies (:1313-1325) and the pre-diagnostics (:289-323)
+    s = np.zeros((kz + 1,) + f["u"].shape[1:])
+    dw = np.zeros_like(s)
+    p = (f["pai"] ** c["cpovr"]) * P00
+    qsat = pfwsat(f["t"], p, c["ep2"])
+    tvirt = f["t"] * (1.0 + c["ep1"] * f["qv"] - f["qc"] - f["qi"] - f["qr"] - f["qs"])
+    qwl, qwi = f["qc"] + f["qr"], f["qi"] + f["qs"]
+    tet = tvirt / f["pai"]
+    u, v, w, pai = f["u"], f["v"], f["w"], f["pai"]
+    q = {n: f[n] for n in ("qv", "qc", "qi", "qr", "qs")}
+    dta = dt / nadv
+    for _ in range(nadv):
+        st = {"u": u, "v": v, "w": w, "pai": pai, "tetav": tet, "s": s, "deltaw": dw, "fmzf": f["fmzf"],
+              "qv": q["qv"], "qc": q["qc"], "qsat": qsat, "t": f["t"], "qwltot": qwl, "qwitot": qwi}
+        r = sound_np(st, sc, c, dta / nsound, nsound)
+        u, v, w, pai, tet, s, dw = r["u"], r["v"], r["w"], r["pai"], r["tetav"], r["s"], r["deltaw"]
+        # advection (:897-927)
+        ux, vx = uv_to_x(u, v)
+        wx = w_to_x(w)
+        args = dict(s=s, fmz=sc["fmz"], fmzf=f["fmzf"], u=Padded(u, 2), v=Padded(v, 2), msfu=sc["msfu"],
+                    msfv=sc["msfv"], msfx=sc["msfx"], dta=dta, dx=dx, dzita=dzita)
+        tet, pai, ux, vx, wx = (wafone_np(a, **args) for a in (tet, pai, ux, vx, wx))
+        q = {n: wafone_np(a, **args) for n, a in q.items()}
+        u, v = x_to_uv(ux, vx)
+        w = x_to_w(wx, w)
+    # the post-diagnostics (:355-391)
+    tvirt = tet * pai
+    t = tvirt / (1.0 + c["ep1"] * q["qv"] - q["qc"] - q["qi"] - q["qr"] - q["qs"])
+    p = (pai ** c["cpovr"]) * P00
+    rho = p / (c["rgas"] * t)
+    zeta = f["zeta"]
+    lrt = 0.65 * ((tvirt[-2] - tvirt[-1]) / (zeta[-2] - zeta[-1])) - 0.35 * LRATE
+    ps = p[-1] * np.exp((zeta[-1] * EGRAV) / (c["rgas"] * (tvirt[-1] - 0.5 * zeta[-1] * lrt)))
+    want = {"u": u, "v": v, "w": w, "pai": pai, "tetav": tet, "t": t, "p": p, "rho": rho, "ps": ps,
+            "qsat": pfwsat(t, p, c["ep2"]), "s": s, **q}
+    o.step(2)
+    for n, x in want.items():
+        err = np.max(np.abs(o.get(n) - x)) / max(np.max(np.abs(x)), 1e-300)
+        assert err <= 1e-13, (n, err)
     o.close()
