@@ -27,8 +27,10 @@ namespace moloch {
 namespace knoalloc {
 
 // Largest jx*iy*kz a call may pass: 2^21 points.  Scratch = wz + p0 =
-// 2 * 2^21 doubles = 32 MiB, held by every GPU that loads this library
-// until the process exits.
+// 2 * 2^21 doubles = 32 MiB.  The CUDA runtime reserves it on a device when
+// it loads this file's device code there -- with lazy module loading (the
+// default), during the first call on that device, which looks the array up
+// -- and holds it until the process exits.
 constexpr long long kMaxPoints = 1LL << 21;
 static __device__ __align__(256) double g_scratch[2 * kMaxPoints];
 
@@ -191,6 +193,10 @@ extern "C" int moloch_gpu_wafone_noalloc(double* pp, const double* s, const doub
     moloch_internal_set_error("wafone_noalloc: jx, iy and kz must be >= 4");
     return MOLOCH_ERR_ARG;
   }
+  if (kz > 65535) {  // the meridional and zonal kernels take k as gridDim.z
+    moloch_internal_set_error("wafone_noalloc: kz must be <= 65535");
+    return MOLOCH_ERR_ARG;
+  }
   if ((long long)jx * iy * kz > kMaxPoints) {
     char buf[200];
     snprintf(buf, sizeof buf, "wafone_noalloc: jx*iy*kz = %lld exceeds the fixed scratch of %lld points",
@@ -234,10 +240,14 @@ extern "C" int moloch_gpu_wafone_noalloc(double* pp, const double* s, const doub
   a.dtrdz = 0.5 * (dta / dzita);
   a.rotllr = rotllr;
   cudaStream_t st = (cudaStream_t)stream;
-  k_na_vertical<<<dim3((jx + 31) / 32, (iy + 3) / 4), dim3(32, 4), 0, st>>>(a);
-  k_na_meridional<<<dim3((jx + 31) / 32, (iy + 7) / 8, kz), dim3(32, 8), 0, st>>>(a);
-  k_na_zonal<<<dim3((jx + 31) / 32, (iy + 7) / 8, kz), dim3(32, 8), 0, st>>>(a);
-  e = cudaGetLastError();
+  // each launch's own status: cudaGetLastError here would also return (and
+  // clear) an error the caller left pending before this call
+  void* args[] = {&a};
+  const dim3 gv((jx + 31) / 32, (iy + 3) / 4), bv(32, 4);
+  const dim3 gh((jx + 31) / 32, (iy + 7) / 8, kz), bh(32, 8);
+  e = cudaLaunchKernel((const void*)k_na_vertical, gv, bv, args, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void*)k_na_meridional, gh, bh, args, 0, st);
+  if (e == cudaSuccess) e = cudaLaunchKernel((const void*)k_na_zonal, gh, bh, args, 0, st);
   if (e != cudaSuccess) {
     moloch_internal_set_error(cudaGetErrorString(e));
     return MOLOCH_ERR_CUDA;

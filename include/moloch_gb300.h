@@ -353,10 +353,14 @@ int moloch_sur_destroy(moloch_surrogate_t* s);
  * msfv, msfx are jx*iy periodic arrays) and pp is advected in place.
  * The two work arrays live in one fixed __device__ array of 32 MiB that
  * every GPU loading the library keeps until exit, so jx*iy*kz may not
- * exceed 2097152 (2^21) points; larger sizes return MOLOCH_ERR_ARG.
- * The first call on a device looks that array's address up once
- * (cudaGetSymbolAddress with the device current): make the first call on
- * each device before any stream capture.  All calls share the array, so
+ * exceed 2097152 (2^21) points and kz may not exceed 65535; larger sizes
+ * return MOLOCH_ERR_ARG.  The first call on a device looks that array's
+ * address up once (cudaGetSymbolAddress with the device current); under
+ * CUDA's default lazy module loading that is also when the CUDA runtime
+ * loads this code on the device and reserves the 32 MiB.  So make the
+ * first call on each device before any stream capture and before the
+ * program reserves the rest of the GPU's memory (its pool or data
+ * regions); later calls reserve nothing.  All calls share the array, so
  * calls that overlap on the GPU (other streams, other threads) race; each
  * call overwrites the work arrays completely before reading them.  No
  * cudaMalloc, cudaFree or allocating library routine is called. */

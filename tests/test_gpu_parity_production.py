@@ -1,0 +1,159 @@
+"""Parity of the CUDA step against the CPU oracle at the benchmarked sizes,
+with the launch shapes the autotuner picks there, and of the non-ROTLLR
+branches with map factors other than 1.
+
+Cases and tolerances:
+  * 512 x 512 x 60, the benchmarked workload (500 m Gaussian hill of
+    20-gridpoint radius at the centre, seeded +-0.5 K theta noise on the
+    lowest 10 levels), 2 steps with the launch shapes the autotuner picks
+    for the FP64 step on this GPU: FP64 (multiply-add contraction) relative
+    L2 <= 1e-12 per field; FP64_EXACT bit-identical in the prognostic
+    fields u, v, w, pai, t, qv, qc and in tetav, tvirt, and <= 1e-15 in
+    ps, p, rho, qsat (CUDA's pow may differ from the host libm in the last
+    bit);
+  * the same workload in FP32 storage with the FP32 autotuned shapes,
+    2 steps: theta RMSE <= 1e-3 K, u, v, w RMSE <= 1e-3 m/s, relative L2 of
+    pai, t, qv <= 1e-5 (the stated error of the FP32 path);
+  * 256 x 256 x 40 (the surrogate case's grid) with a 300 m hill and a
+    5 m/s wind, 3 steps, FP64 <= 1e-12 and FP64_EXACT as above;
+  * the non-ROTLLR branches (sound :598-621, :788-837; wafone :1189-1298)
+    with map factors within 5 % of 1 (the idealized grid has exactly 1,
+    where a missing or misplaced factor would not show), periodic rings,
+    every sound-kernel variant: 3 steps, FP64_EXACT <= 1e-13 and
+    FP64 <= 1e-12.
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+from tests.test_gpu_parity import DIAG, PROG, compare, pair
+
+pytestmark = pytest.mark.gpu
+
+EXACT_SAME = ("u", "v", "w", "pai", "t", "qv", "qc", "tetav", "tvirt")
+EXACT_POW = ("ps", "p", "rho", "qsat")
+
+
+def bench_hill(jx, iy):
+    return ((500.0, (jx + 1) / 2.0, (iy + 1) / 2.0, 20.0),)
+
+
+def tuned(dm, jx, iy, kz, mode, hills, **kw):
+    """The autotuner's choice on a scratch handle of the same workload."""
+    t = dm.Moloch(jx, iy, kz, mode=mode)
+    t.setup_idealized(hills=hills, **kw)
+    ch = t.autotune()
+    t.close()
+    return ch
+
+
+def rmse(a, b):
+    return float(np.sqrt(np.mean((np.asarray(a) - np.asarray(b)) ** 2)))
+
+
+def check_exact(o, g):
+    for n in EXACT_SAME:
+        a, b = g.get(n), o.get(n)
+        assert np.array_equal(a, b), (n, float(np.max(np.abs(a - b))))
+    compare(o, g, EXACT_POW, 1e-15)
+
+
+@pytest.fixture(scope="module")
+def fp64_choice_512(gpu_lib):
+    return tuned(gpu_lib, 512, 512, 60, "fp64", bench_hill(512, 512))
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp64_exact"])
+def test_benchmark_workload_512x512x60(oracle_mod, gpu_lib, fp64_choice_512, mode):
+    o, g = pair(oracle_mod, gpu_lib, 512, 512, 60, mode=mode, hills=bench_hill(512, 512))
+    g.set_tuning(fp64_choice_512)
+    for s in (1, 2):
+        o.step(s)
+        g.moloch(s)
+    if mode == "fp64_exact":
+        check_exact(o, g)
+    else:
+        worst = compare(o, g, PROG + DIAG, 1e-12)
+        print("512x512x60 fp64", fp64_choice_512, {k: f"{v:.1e}" for k, v in worst.items()})
+    o.close()
+    g.close()
+
+
+def test_benchmark_workload_512x512x60_fp32(oracle_mod, gpu_lib):
+    hills = bench_hill(512, 512)
+    choice = tuned(gpu_lib, 512, 512, 60, "fp32_mixed", hills)
+    o, g = pair(oracle_mod, gpu_lib, 512, 512, 60, mode="fp32_mixed", hills=hills)
+    g.set_tuning(choice)
+    for s in (1, 2):
+        o.step(s)
+        g.moloch(s)
+    th_g, th_o = g.get("t") / g.get("pai"), o.get("t") / o.get("pai")
+    err = {"theta_K": rmse(th_g, th_o), "u": rmse(g.get("u"), o.get("u")), "v": rmse(g.get("v"), o.get("v")),
+           "w": rmse(g.get("w"), o.get("w"))}
+    rel = {n: rel_l2(g.get(n), o.get(n)) for n in ("pai", "t", "qv")}
+    print("512x512x60 fp32_mixed", choice, {k: f"{v:.1e}" for k, v in {**err, **rel}.items()})
+    assert all(v <= 1e-3 for v in err.values()), err
+    assert all(v <= 1e-5 for v in rel.values()), rel
+    o.close()
+    g.close()
+
+
+@pytest.mark.parametrize("mode", ["fp64", "fp64_exact"])
+def test_surrogate_grid_256x256x40(oracle_mod, gpu_lib, mode):
+    hills = ((300.0, 128.5, 128.5, 12.0),)
+    choice = tuned(gpu_lib, 256, 256, 40, "fp64", hills, u0=5.0)
+    o, g = pair(oracle_mod, gpu_lib, 256, 256, 40, mode=mode, hills=hills, u0=5.0)
+    g.set_tuning(choice)
+    for s in (1, 2, 3):
+        o.step(s)
+        g.moloch(s)
+    if mode == "fp64_exact":
+        check_exact(o, g)
+    else:
+        compare(o, g, PROG + DIAG, 1e-12)
+    o.close()
+    g.close()
+
+
+def periodic_map_factors(jx, iy, seed):
+    """Map factors within 5 % of 1 in the reference's bounded layouts
+    (msfu (0:nj+1, 1:ni), msfv (1:nj, 0:ni+1), msfx (1:nj, 1:ni)) as
+    (i, j) arrays, their rings periodic images of the interior -- what the
+    upload contract assumes of every halo."""
+    rng = np.random.default_rng(seed)
+    mu, mv, mx = (1.0 + 0.05 * rng.uniform(-1.0, 1.0, (iy, jx)) for _ in range(3))
+    msfu = np.concatenate([mu[:, -1:], mu, mu[:, :1]], axis=1)
+    msfv = np.concatenate([mv[-1:, :], mv, mv[:1, :]], axis=0)
+    return msfu, msfv, mx
+
+
+def skewed_pair(oracle_mod, dm, jx, iy, kz, mode, seed=5, **kw):
+    o, g = pair(oracle_mod, dm, jx, iy, kz, mode=mode, rotllr=False, **kw)
+    msfu, msfv, msfx = periodic_map_factors(jx, iy, seed)
+    o.set_map_factors(msfu[None], msfv[None], msfx[None])
+    for name, a in (("msfu", msfu), ("msfv", msfv), ("msfx", msfx)):
+        g.upload(name, a.T)
+    g.init()  # init_moloch again: mx2, rmu, rmv and the WAF metric terms
+    for name, a in (("msfu", msfu), ("msfv", msfv), ("msfx", msfx)):
+        assert np.array_equal(g.download(name), a.T), name
+    return o, g
+
+
+@pytest.mark.parametrize("variant", [0, 7, 11, 24])
+@pytest.mark.parametrize("mode,tol", [("fp64_exact", 1e-13), ("fp64", 1e-12)])
+def test_non_rotllr_map_factors(oracle_mod, gpu_lib, mode, tol, variant):
+    o, g = skewed_pair(oracle_mod, gpu_lib, 40, 33, 16, mode, hills=((300.0, 20.0, 16.0, 4.0),),
+                       u0=6.0, v0=-4.0)
+    g.set_tuning([16 if variant else 1, variant])
+    for s in (1, 2, 3):
+        o.step(s)
+        g.moloch(s)
+    compare(o, g, PROG + DIAG, tol)
+    # the factors change the result: the same run with factors of 1 differs
+    o1 = oracle_mod.Oracle(oracle_mod.make_cfg(40, 33, 16, hills=((300.0, 20.0, 16.0, 4.0),), u0=6.0, v0=-4.0,
+                                               rotllr=False))
+    for s in (1, 2, 3):
+        o1.step(s)
+    assert rel_l2(o1.get("u"), o.get("u")) > 1e-4
+    for x in (o, g, o1):
+        x.close()
