@@ -78,6 +78,7 @@ _PROTOS = {
     "moloch_gpu_download": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]),
     "moloch_gpu_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int]),
     "moloch_gpu_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "moloch_gpu_kernel_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "moloch_gpu_phase": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
@@ -266,6 +267,12 @@ class Moloch:
 
     def sync(self):
         _check(self.L.moloch_gpu_sync(self.h))
+
+    def set_wait_limit(self, cycles=0, skip_job=-1):
+        """Limit (SM clock cycles, 0: default) of the staged column kernel's
+        bounded waits; skip_job >= 0 is a test hook that leaves that staged
+        chunk unissued so a wait runs out (moloch_gpu_set_wait_limit)."""
+        _check(self.L.moloch_gpu_set_wait_limit(self.h, int(cycles), int(skip_job)))
 
     def profile_step(self):
         """One step with CUDA events around every kernel: {kernel: (ms, launches)}."""

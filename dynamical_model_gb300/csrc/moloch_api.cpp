@@ -225,6 +225,9 @@ struct moloch_handle {
   // attached acoustic-cycle surrogate (FP32 storage only): each sound()
   // call first runs the surrogate; the plain substeps skip on acceptance
   moloch::mlp::Surrogate* sur = nullptr;
+  // TMA tensor maps of the staged column kernel (FP32 storage), one set per
+  // advected-field buffer set
+  alignas(64) unsigned char cmaps[4096];
   int nj() const { return grid.jx; }
   int ni() const { return grid.iy; }
   int kz() const { return grid.kz; }
@@ -284,6 +287,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   const int parts = kfast::diag_parts(h->nj(), h->ni());
   v.dpart = (double*)take(sizeof(double) * 9 * parts);
   v.dres = (double*)take(sizeof(double) * 16);
+  v.kerr = (int*)take(sizeof(int));
   v.dparts = parts;
   v.nj = h->nj(); v.ni = h->ni(); v.kz = h->kz(); v.pl = (int)pl; v.rotllr = h->prm.rotllr;
   v.cur = 0;
@@ -291,6 +295,9 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.kmarch = 0;
   v.vfields = 1;
   v.sur_skip = nullptr;
+  v.cmaps = nullptr;
+  v.spin_cycles = kDefaultSpinCycles;
+  v.fault_skip_job = -1;
   return off + 256;
 }
 
@@ -653,6 +660,11 @@ int init_impl(moloch_handle* h, View<T>& v) {
   CUDA_TRY(cudaMemsetAsync(v.s, 0, sizeof(T) * pl * (kz + 1), h->stream));
   CUDA_TRY(cudaMemsetAsync(v.deltaw, 0, sizeof(T) * pl * (kz + 1), h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if constexpr (sizeof(T) == sizeof(float)) {
+    v.cmaps = nullptr;
+    if (kfast::column_maps_bytes() <= (int)sizeof(h->cmaps) && kfast::build_column_maps(v, h->cmaps))
+      v.cmaps = h->cmaps;
+  }
   return MOLOCH_OK;
 }
 
@@ -725,6 +737,18 @@ int check_launch(const char* what) {
   return MOLOCH_OK;
 }
 
+// reads and clears the flag a bounded device wait sets when it gives up
+int check_kerr(moloch_handle* h) {
+  int* kerr = h->elem == 8 ? h->vd.kerr : h->vf.kerr;
+  int v = 0;
+  CUDA_TRY(cudaMemcpyAsync(&v, kerr, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if (!v) return MOLOCH_OK;
+  CUDA_TRY(cudaMemsetAsync(kerr, 0, sizeof(int), h->stream));
+  CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return fail(MOLOCH_ERR_TIMEOUT, "a bounded device wait of the column solve gave up; the state is invalid");
+}
+
 int read_diag(moloch_handle* h, moloch_diag_t* diag) {
   int n = h->elem == 8 ? launch_phase(h, h->vd, 4) : launch_phase(h, h->vf, 4);
   h->kernels += n;
@@ -733,6 +757,7 @@ int read_diag(moloch_handle* h, moloch_diag_t* diag) {
   const double* dres = h->elem == 8 ? h->vd.dres : h->vf.dres;
   CUDA_TRY(cudaMemcpyAsync(h->hres, dres, sizeof(double) * 9, cudaMemcpyDeviceToHost, h->stream));
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  if ((rc = check_kerr(h))) return rc;
   moloch_diag_t d{};
   d.maxps = h->hres[0]; d.minps = h->hres[1];
   d.maxu = h->hres[2]; d.minu = h->hres[3]; d.maxv = h->hres[4]; d.minv = h->hres[5];
@@ -1229,6 +1254,16 @@ int moloch_gpu_sync(moloch_handle_t* h) {
   g_err.clear();
   if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
   CUDA_TRY(cudaStreamSynchronize(h->stream));
+  return check_kerr(h);
+}
+
+int moloch_gpu_set_wait_limit(moloch_handle_t* h, long long cycles, int skip_job) {
+  g_err.clear();
+  if (!h) return fail(MOLOCH_ERR_ARG, "null handle");
+  if (cycles <= 0) cycles = kDefaultSpinCycles;
+  h->vd.spin_cycles = h->vf.spin_cycles = cycles;
+  h->vd.fault_skip_job = h->vf.fault_skip_job = skip_job < 0 ? -1 : skip_job;
+  drop_graphs(h);  // both are kernel parameters baked into captured graphs
   return MOLOCH_OK;
 }
 
@@ -1305,7 +1340,7 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     h->vf.hz_levels = choice[0];
   }
   if (n > 1) {
-    if (choice[1] < 0 || choice[1] > 31) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 63) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     h->vd.kmarch = choice[1];
     h->vf.kmarch = choice[1];
   }
@@ -1358,9 +1393,11 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   // three), timed on sound()
   double best1 = 1e30;
   int pick1 = h->elem == 8 ? h->vd.kmarch : h->vf.kmarch;
-  for (int cand = 0; cand < 32; ++cand) {
+  const bool staged_ok = h->elem == 4 && h->vf.cmaps != nullptr;
+  for (int cand = 0; cand < 64; ++cand) {
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both
+    if ((cand & 32) && !staged_ok) continue;  // staged column solve: FP32 domains with tensor maps
     h->vd.kmarch = cand;
     h->vf.kmarch = cand;
     float ms = 0.f, tot = 0.f;

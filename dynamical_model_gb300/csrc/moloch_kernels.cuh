@@ -21,6 +21,7 @@
 //   k_postdiag         :355-391  tvirt, t, p, rho, ps, qsat
 //   k_diag_*           :395-411  max/min of ps, u, v; NaN/Inf check; FP64 column sums
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cstdint>
 #include <type_traits>
@@ -519,6 +520,12 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4)
 }
 
 
+
+}  // namespace MOLOCH_KNS
+}  // namespace moloch
+#include "moloch_column_tm.cuh"
+namespace moloch {
+namespace MOLOCH_KNS {
 
 // ---- 5-point Laplacian filter of one field, out of place ----------------
 // out = a + coef(k) * (0.125*(aW+aE+aS+aN) - 0.5*a)   (:423-481)
@@ -2025,6 +2032,26 @@ int launch_prediag(const View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   return 1;
 }
 
+// the staged column kernel runs when asked for (kmarch bit 32) on an FP32
+// domain whose tensor maps were built
+template <class T>
+inline bool column_tm_ok(const View<T>& d) {
+  return sizeof(T) == 4 && (d.kmarch & 32) && d.cmaps != nullptr;
+}
+inline int column_tm_grid(int nj, int ni) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 1;
+  }
+  const int ntiles = ((nj + 31) / 32) * ((ni + 3) / 4);
+  return ntiles < nsm ? ntiles : nsm;
+}
+template <class T>
+inline int column_tm_grid(const View<T>& d) { return column_tm_grid(d.nj, d.ni); }
+
 // one sound() call: nsound substeps; flips d.cur once per substep, twice
 // with the fused divergence/damping kernel (kmarch bit 16)
 template <class T>
@@ -2057,7 +2084,16 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       MOLOCH_LAUNCH(KK_PAI_UPDATE, st, k_pai_update<T><<<pg, pb, 0, st>>>(d));
       n += 3;
     } else {
-      MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
+      bool staged = false;
+      if constexpr (sizeof(T) == 4) {
+        if (column_tm_ok(d)) {
+          MOLOCH_LAUNCH(KK_SOUND_COLUMN, st,
+                        k_sound_column_tm<T><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(
+                            d, static_cast<const ColumnMaps*>(d.cmaps)[d.fcur], ns, last));
+          staged = true;
+        }
+      }
+      if (!staged) MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
     if (d.kmarch & 8) {

@@ -20,3 +20,66 @@ template int blaunch_advection<double>(const Batch<double>&, cudaStream_t, int&,
 template int blaunch_advection<float>(const Batch<float>&, cudaStream_t, int&, int&);
 }  // namespace kfast
 }  // namespace moloch
+
+// ---- tensor maps of the staged column kernel --------------------------------
+#include <mutex>
+
+namespace moloch {
+namespace kfast {
+namespace {
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  });
+  return fn;
+}
+// dense FP32 field (nj, ni, nk), j fastest, as boxes of 32 x 4 x kKCT
+bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, int nk) {
+  const cuuint64_t dims[3] = {(cuuint64_t)nj, (cuuint64_t)ni, (cuuint64_t)nk};
+  const cuuint64_t strides[2] = {(cuuint64_t)nj * 4, (cuuint64_t)nj * ni * 4};
+  const cuuint32_t box[3] = {32, 4, (cuuint32_t)kKCT};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+}  // namespace
+
+int column_maps_bytes() { return (int)(2 * sizeof(ColumnMaps)); }
+
+bool build_column_maps(const View<float>& v, void* out) {
+  if (v.kz > kTmMaxKz || v.kz < 2 || v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn) return false;
+  static std::once_flag attr;
+  std::call_once(attr, [] {
+    cudaFuncSetAttribute(k_sound_column_tm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem);
+  });
+  ColumnMaps* cm = static_cast<ColumnMaps*>(out);
+  const int nj = v.nj, ni = v.ni, kz = v.kz;
+  for (int set = 0; set < 2; ++set) {
+    CUtensorMap* m = cm[set].m;
+    const bool ok =
+        map3(fn, &m[CM_W], v.w, nj, ni, kz + 1) && map3(fn, &m[CM_FMZF], v.fmzf, nj, ni, kz + 1) &&
+        map3(fn, &m[CM_QV], v.fset[set][5], nj, ni, kz) && map3(fn, &m[CM_TET], v.fset[set][0], nj, ni, kz) &&
+        map3(fn, &m[CM_PAI], v.fset[set][1], nj, ni, kz) && map3(fn, &m[CM_QSAT], v.qsat, nj, ni, kz) &&
+        map3(fn, &m[CM_ZD], v.zdiv2b, nj, ni, kz) && map3(fn, &m[CM_FMZ], v.fmz, nj, ni, kz) &&
+        map3(fn, &m[CM_T], v.t, nj, ni, kz) && map3(fn, &m[CM_QC], v.fset[set][6], nj, ni, kz) &&
+        map3(fn, &m[CM_QWL], v.qwltot, nj, ni, kz) && map3(fn, &m[CM_QWI], v.qwitot, nj, ni, kz) &&
+        map3(fn, &m[CM_S], v.s, nj, ni, kz + 1);
+    if (!ok) return false;
+  }
+  return cudaGetLastError() == cudaSuccess;
+}
+}  // namespace kfast
+}  // namespace moloch

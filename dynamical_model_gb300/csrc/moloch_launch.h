@@ -21,6 +21,12 @@ namespace moloch {
 MOLOCH_DECLARE_LAUNCHERS(kexact)
 MOLOCH_DECLARE_LAUNCHERS(kfast)
 namespace kfast {
+// TMA tensor maps of the staged column kernel for both advected-field
+// buffer sets of an FP32 domain, written to `out` (column_maps_bytes()
+// bytes, 64-byte aligned); false when the domain does not qualify (kz > 64,
+// jx not a multiple of 4) or the driver cannot encode them
+int column_maps_bytes();
+bool build_column_maps(const View<float>& v, void* out);
 template <class T> int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& cur, int& fcur);
 template <class T> int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur);
 }

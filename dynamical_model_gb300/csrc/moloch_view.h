@@ -17,6 +17,9 @@
 
 namespace moloch {
 
+// default limit of a bounded device wait: about one second of SM clock
+constexpr long long kDefaultSpinCycles = 2000000000LL;
+
 constexpr int kNumAdvected = 10;  // tetav pai ux vx wx qv qc qi qr qs (mod_moloch.F90:911-920)
 
 template <class T>
@@ -108,13 +111,23 @@ struct View {
   // launch shape chosen by the autotuner: levels per k_waf_horizontal block
   int hz_levels;
   int kmarch;      // sound kernel variants, bit mask: 1 divergence, 2 damping, 4 momentum
-                   // k-marching; 8 momentum as warp strips; 16 divergence + damping fused
+                   // k-marching; 8 momentum as warp strips; 16 divergence + damping fused;
+                   // 32 column solve staged by TMA with its column state in TMEM
   int vfields;     // advected fields per thread of k_waf_vertical: 1, 2, 5 or 10
 
   // set when a learned surrogate stands in for sound(): the plain sound
   // kernels return at once while *sur_skip == 1 (the surrogate's cycle was
   // accepted); nullptr when no surrogate is attached
   const int* sur_skip;
+
+  // staged column kernel (k_sound_column_tm, FP32 storage): host pointer to
+  // the two sets of TMA tensor maps (one per advected-field buffer set),
+  // nullptr when the kernel cannot run on this domain
+  const void* cmaps;
+  // device word set by a bounded wait that gave up (MOLOCH_ERR_TIMEOUT)
+  int* kerr;
+  long long spin_cycles;  // limit of every such wait, in SM clock cycles
+  int fault_skip_job;     // test hook: a job the producer leaves unissued (-1: none)
 
   // diagnostics
   double* dpart;  // per-block partial reductions

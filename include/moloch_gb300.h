@@ -191,8 +191,19 @@ int moloch_gpu_output_start(moloch_handle_t* h);
 int moloch_gpu_output_finish(moloch_handle_t* h, double* t_host, const int* t_lb, const int* t_ub,
                              double* ps_host, const int* ps_lb, const int* ps_ub);
 
-/* Block until the handle's stream is idle. */
+/* Block until the handle's stream is idle.  MOLOCH_ERR_TIMEOUT when a
+ * bounded wait of the staged column kernel gave up since the last check
+ * (the state is then invalid); lprint steps check the same flag. */
 int moloch_gpu_sync(moloch_handle_t* h);
+
+/* Bounded device waits of the staged column kernel (tuning bit 32): every
+ * wait gives up after `cycles` SM clock cycles (<= 0: the default, 2e9,
+ * about one second), sets the flag moloch_gpu_sync reports and lets the
+ * kernel return.  skip_job >= 0 is a test hook: the kernel's loader leaves
+ * that staged chunk (counted per CTA from 0) unissued, so a wait on it
+ * runs out; -1 turns it off.  No reference counterpart (the reference has
+ * no device waits). */
+int moloch_gpu_set_wait_limit(moloch_handle_t* h, long long cycles, int skip_job);
 
 /* The stream the handle launches on (a cudaStream_t). */
 void* moloch_gpu_stream(moloch_handle_t* h);
@@ -226,7 +237,10 @@ const char* moloch_gpu_kernel_name(int kind);
  *               thread, next level prefetched), 8 momentum as warp strips
  *               (30 columns x 32 rows), 16 divergence and damping fused in
  *               one warp-strip kernel (29 columns x 32 rows; overrides 1
- *               and 2); 0 = one level per thread;
+ *               and 2), 32 the implicit-w column solve staged by TMA with
+ *               its column state in TMEM (FP32 storage, jx a multiple of 4,
+ *               kz <= 64; elsewhere the bit is ignored); 0 = one level per
+ *               thread;
  *   choice[2] = advected fields per thread of the vertical WAF kernel:
  *               1, 2, 5 or 10 (the fields of a thread share the velocity
  *               loads and terms).

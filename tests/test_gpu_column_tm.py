@@ -1,0 +1,95 @@
+"""The implicit-w column solve staged by TMA with its column state in TMEM
+(k_sound_column_tm, tuning bit 32, FP32 storage) against the
+one-thread-per-column kernel and the oracle, and its bounded waits.
+
+  * Against k_sound_column<float> on the same state: the same FP32/FP64
+    arithmetic per level in the same order, so the steps agree to the last
+    bit when the compiler contracts both alike; bound 1e-6 relative L2
+    (printed: the measured difference).  Sizes cover partial tiles (jx not a
+    multiple of 32, iy not a multiple of 4), kz from 13 to the largest the
+    TMEM columns hold (64) and the last-substep path.
+  * Against the oracle: tests/test_gpu_mixed.py runs 100 steps with this
+    kernel (tuning [32, 56]).
+  * A bounded wait that runs out: a test hook leaves one staged chunk
+    unissued, the wait on it gives up after about a millisecond,
+    moloch_gpu_sync returns MOLOCH_ERR_TIMEOUT (6), and the next steps on a
+    fresh state are correct again (the context stays usable).
+"""
+import numpy as np
+import pytest
+
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+FIELDS = ("u", "v", "w", "pai", "t", "qv", "qc", "tetav", "s", "deltaw")
+
+
+def _pair(dm, jx, iy, kz, base, hills, **kw):
+    a = dm.Moloch(jx, iy, kz, mode="fp32_mixed")
+    b = dm.Moloch(jx, iy, kz, mode="fp32_mixed")
+    for g in (a, b):
+        g.setup_idealized(hills=hills, **kw)
+    a.set_tuning([16, base])
+    b.set_tuning([16, base | 32])
+    return a, b
+
+
+@pytest.mark.parametrize("jx,iy,kz", [(64, 44, 30), (36, 29, 13), (96, 37, 60), (128, 64, 64), (40, 33, 40)])
+def test_staged_column_matches_column_kernel(gpu_lib, jx, iy, kz):
+    a, b = _pair(gpu_lib, jx, iy, kz, 24, ((500.0, jx / 2, iy / 2, 5.0),), u0=6.0, v0=-4.0)
+    for s in (1, 2, 3):
+        a.moloch(s)
+        b.moloch(s)
+    b.run(2, graph=True)
+    a.run(2, graph=True)
+    worst = {n: rel_l2(b.get(n), a.get(n)) for n in FIELDS}
+    print(f"{jx}x{iy}x{kz} staged vs one-thread column solve:", {k: f"{v:.1e}" for k, v in worst.items()})
+    assert all(v <= 1e-6 for v in worst.values()), worst
+    a.close()
+    b.close()
+
+
+def test_staged_column_is_used_only_where_it_fits(gpu_lib):
+    """jx not a multiple of 4 (no TMA row stride) and kz > 64 (TMEM full)
+    fall back to the one-thread kernel: results identical to it."""
+    for jx, iy, kz in ((37, 20, 12), (32, 16, 70)):
+        a, b = _pair(gpu_lib, jx, iy, kz, 24, ((300.0, jx / 2, iy / 2, 4.0),), u0=3.0)
+        for s in (1, 2):
+            a.moloch(s)
+            b.moloch(s)
+        for n in FIELDS:
+            assert np.array_equal(a.get(n), b.get(n)), (jx, kz, n)
+        a.close()
+        b.close()
+
+
+def test_staged_column_wait_runs_out(gpu_lib):
+    jx, iy, kz = 64, 48, 20
+    hills = ((400.0, 32.0, 24.0, 4.0),)
+    g = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    ref = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
+    for x in (g, ref):
+        x.setup_idealized(hills=hills, u0=4.0)
+        x.set_tuning([16, 56])
+    # each CTA's staged chunk 3 is never issued: the compute warps' wait on
+    # it and the loader's wait for that stage to drain both give up after
+    # 2e6 cycles (about 1 ms); the kernel reports, drains and returns
+    g.set_wait_limit(2_000_000, 3)
+    g.moloch(1)
+    with pytest.raises(gpu_lib.MolochError) as ei:
+        g.sync()
+    assert ei.value.code == 6
+    g.sync()  # the flag is cleared once reported
+    # back to the default limit, a fresh state: the context is usable and the
+    # steps are correct again
+    g.set_wait_limit(0, -1)
+    g.setup_idealized(hills=hills, u0=4.0)
+    for s in (1, 2, 3):
+        g.moloch(s)
+        ref.moloch(s)
+    g.sync()
+    for n in FIELDS:
+        assert np.array_equal(g.get(n), ref.get(n)), n
+    g.close()
+    ref.close()

@@ -64,11 +64,12 @@ def _state(g):
 
 
 @pytest.mark.parametrize("jx,iy,kz,tuning", [(24, 20, 8, [1, 0]), (37, 29, 12, [1, 0]), (37, 29, 12, [32, 11]),
-                                             (24, 20, 8, [16, 7]), (37, 29, 12, [32, 24])])
+                                             (24, 20, 8, [16, 7]), (37, 29, 12, [32, 24]), (24, 20, 8, [16, 39])])
 def test_sur_cycle_matches_oracle(gpu_lib, jx, iy, kz, tuning):
     """tuning: the plain kernel variants that must all stand aside on a
     committed cycle (one level per thread, strips, k-marching, the fused
-    divergence/damping strips, which flip the u/v buffers twice a substep)."""
+    divergence/damping strips, which flip the u/v buffers twice a substep,
+    and the column solve staged by TMA with its state in TMEM)."""
     from oracle import mlp_oracle as mo
     g = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     g.setup_idealized(hills=((400.0, jx / 2, iy / 2, 3.0),), u0=5.0, v0=-3.0)
@@ -152,7 +153,7 @@ def test_sur_collected_pairs_match_oracle(gpu_lib, tuning):
     b.close()
 
 
-@pytest.mark.parametrize("tuning", [[1, 0], [32, 24]])
+@pytest.mark.parametrize("tuning", [[1, 0], [32, 24], [32, 56]])
 def test_sur_fallback_is_bit_identical(gpu_lib, tuning):
     jx, iy, kz = 32, 24, 10
     a = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")

@@ -100,6 +100,10 @@ def test_wafone_noalloc_matches_oracle_with_map_factors(oracle_mod, gpu_lib, rot
     o.set_map_factors(msfu[None], msfv[None], msfx[None])
     o.phase(0)
     o.phase(1)
+    # advection() refreshes the u, v rings in uvstagtox (:1389-1417) before
+    # its wafone calls; wafone reads u along j and v along i, which that
+    # refresh makes periodic images of the interior
+    o.stagger(1)
     scal = (ctypes.c_double * 9)()
     oracle_mod.lib().oracle_scalars(o.h, scal)
     dt, dx, dzita, nadv = scal[0], scal[1], scal[2], scal[6]
