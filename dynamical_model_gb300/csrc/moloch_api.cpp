@@ -1274,7 +1274,7 @@ long long moloch_gpu_kernel_count(moloch_handle_t* h) { return h ? h->kernels : 
 static const char* const kKindNames[KK_COUNT] = {
     "k_prediag", "k_sound_div", "k_sound_damp", "k_sound_column", "k_lap_filter", "k_pai_update",
     "k_sound_momentum", "k_waf_vertical", "k_waf_horizontal", "k_stag_from_x",
-    "k_filter_increment", "k_postdiag", "k_diag", "k_sound_divdamp"};
+    "k_filter_increment", "k_postdiag", "k_diag", "k_sound_divdamp", "k_sound_column_tm"};
 
 int moloch_gpu_kernel_kinds(void) { return KK_COUNT; }
 

@@ -303,6 +303,16 @@ __device__ __forceinline__ float narrow_trunc(double x) {
   return __uint_as_float(m | (hi & 0x80000000u));
 }
 
+// a*b - c*d and a*b + c*d with the multiply-add contraction fixed in FP32
+// storage: left to the compiler either product may be fused, and two
+// kernels doing the same arithmetic (k_sound_column, k_sound_column_tm)
+// could round differently.  FP64 keeps the expression as written (the
+// exact build contracts nothing).
+__device__ __forceinline__ float prod_sub(float a, float b, float c, float d) { return __fmaf_rn(a, b, -__fmul_rn(c, d)); }
+__device__ __forceinline__ double prod_sub(double a, double b, double c, double d) { return a * b - c * d; }
+__device__ __forceinline__ float prod_add(float a, float b, float c, float d) { return __fmaf_rn(c, d, __fmul_rn(a, b)); }
+__device__ __forceinline__ double prod_add(double a, double b, double c, double d) { return a * b + c * d; }
+
 // ---- sound: implicit w (Thomas, :634-686) + Exner/theta (:690-728) -----
 // One thread per column.  Down-sweep k = kz..2 with FP64 pivots in every
 // mode, stash of the FP64 down-sweep values, then back-substitution fused
@@ -391,7 +401,7 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
       zrom1w = zrom1w + zdth * fz;
     }
     T zwexpl = (wk - (zrom1w * dtrdz) * (pkm - pk)) - egdts;
-    zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * (pkm * zd_km - pk * zd_k);
+    zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * prod_sub(pkm, zd_km, pk, zd_k);
     const T zu_t = ((zcs2 * fkm) * zrom1w) * pkm + ff;
     const T zd_t = ((zcs2 * fk) * zrom1w) * pk + ff;
     ST wpk;
@@ -454,7 +464,7 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     T zd = f.zd;
     zd = zd + (dtrdz * f.fmz) * (wl - wh);
     zd = (zd * ((T(1) + T(0.86) * f.qv) + T(3.2) * f.qc)) / ((T(1) + T(0.96) * f.qv) + T(4.8) * f.qc);
-    TET[q] = f.tet * (T(1) + (rdrcv * zd) * ((T(0.25) * f.qv + T(4.2) * f.qwl) + T(2.1) * f.qwi));
+    TET[q] = f.tet * (T(1) + (rdrcv * zd) * (prod_add(T(0.25), f.qv, T(4.2), f.qwl) + T(2.1) * f.qwi));
     if (defer_pai) {
       ZD[q] = zd;
     } else {
@@ -2087,7 +2097,7 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       bool staged = false;
       if constexpr (sizeof(T) == 4) {
         if (column_tm_ok(d)) {
-          MOLOCH_LAUNCH(KK_SOUND_COLUMN, st,
+          MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
                         k_sound_column_tm<T><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(
                             d, static_cast<const ColumnMaps*>(d.cmaps)[d.fcur], ns, last));
           staged = true;

@@ -43,11 +43,11 @@ EncodeTiledFn encode_tiled() {
   });
   return fn;
 }
-// dense FP32 field (nj, ni, nk), j fastest, as boxes of 32 x 4 x kKCT
+// dense FP32 field (nj, ni, nk), j fastest, as boxes of 32 x kTmRows x kKCT
 bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, int nk) {
   const cuuint64_t dims[3] = {(cuuint64_t)nj, (cuuint64_t)ni, (cuuint64_t)nk};
   const cuuint64_t strides[2] = {(cuuint64_t)nj * 4, (cuuint64_t)nj * ni * 4};
-  const cuuint32_t box[3] = {32, 4, (cuuint32_t)kKCT};
+  const cuuint32_t box[3] = {32, (cuuint32_t)kTmRows, (cuuint32_t)kKCT};
   const cuuint32_t es[3] = {1, 1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,

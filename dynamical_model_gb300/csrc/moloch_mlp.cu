@@ -632,14 +632,12 @@ enum {
   CTL_INTERVAL, CTL_COUNT = 32
 };
 
-__global__ void k_sur_begin(int* __restrict__ ctl, int judge_every, double* __restrict__ jacc) {
+__global__ void k_sur_begin(int* __restrict__ ctl, int judge_every) {
   const int cyc = ctl[CTL_CYCLE]++;
   const int judge = judge_every > 0 && cyc == ctl[CTL_NEXTJUDGE];
   ctl[CTL_JUDGE] = judge;
   ctl[CTL_RUN] = judge || ctl[CTL_ENABLED];
   ctl[CTL_BAD] = 0;
-  if (judge)
-    for (int q = 0; q < 10; ++q) jacc[q] = 0.0;
 }
 
 // every increment finite and within threshold x the envelope of the
@@ -695,7 +693,10 @@ __global__ void k_sur_judge_snapshot(View<float> d, const int* __restrict__ ctl,
 }
 
 // judge cycles, after the plain loop: sums of (predicted - actual)^2 and
-// actual^2 of the increments, per field
+// actual^2 of the increments, per field; block b writes its ten partial
+// sums to jacc[10 b ..], which k_sur_verdict adds in a fixed order (no
+// atomics: the verdict of a cycle near the tolerance must not depend on the
+// order in which blocks finish)
 __global__ void __launch_bounds__(256) k_sur_judge(View<float> d, const int* __restrict__ ctl,
                                                    const float* __restrict__ snap, const float* __restrict__ Y, int ld,
                                                    const float* __restrict__ ymean, const float* __restrict__ ystd,
@@ -731,13 +732,31 @@ __global__ void __launch_bounds__(256) k_sur_judge(View<float> d, const int* __r
   if (threadIdx.x < 10) {
     double v = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
-    atomicAdd(&jacc[threadIdx.x], v);
+    jacc[(size_t)blockIdx.x * 10 + threadIdx.x] = v;
   }
 }
 
-__global__ void k_sur_verdict(int* __restrict__ ctl, const double* __restrict__ jacc, float tol, int judge_every,
-                              int max_interval, unsigned long long* __restrict__ counts) {
+// one block of 256 threads: the judge's per-block partial sums added in a
+// fixed order (strided per thread, then a fixed tree), then the verdict
+__global__ void __launch_bounds__(256) k_sur_verdict(int* __restrict__ ctl, const double* __restrict__ jpart,
+                                                     int nparts, float tol, int judge_every, int max_interval,
+                                                     unsigned long long* __restrict__ counts) {
   if (!ctl[CTL_JUDGE]) return;
+  __shared__ double red[10][256];
+  for (int q = 0; q < 10; ++q) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nparts; b += blockDim.x) v += jpart[(size_t)b * 10 + q];
+    red[q][threadIdx.x] = v;
+  }
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h)
+      for (int q = 0; q < 10; ++q) red[q][threadIdx.x] += red[q][threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  double jacc[10];
+  for (int q = 0; q < 10; ++q) jacc[q] = red[q][0];
   double worst = 0.0;
   for (int f = 0; f < 5; ++f) {
     const double r = jacc[2 * f + 1] > 0.0 ? sqrt(jacc[2 * f] / jacc[2 * f + 1]) : (jacc[2 * f] > 0.0 ? 1e30 : 0.0);
@@ -874,7 +893,8 @@ static int gemm(const void* A, int lda, const void* B, int ldb, float* C, int ld
   return 1;
 }
 
-static int grid1(size_t n) { return (int)std::min<size_t>((n + 255) / 256, 152 * 16); }
+constexpr int kGrid1Max = 152 * 16;  // largest grid of the grid-stride kernels below
+static int grid1(size_t n) { return (int)std::min<size_t>((n + 255) / 256, kGrid1Max); }
 // k_sur_check: at most 16 x 38 blocks of 256 threads
 static dim3 check_grid(int n, int m) { return dim3(std::min((n + 2047) / 2048, 16), std::min(m, 38)); }
 // k_sur_features: work items of 128 columns x 64 features, one wave of
@@ -950,7 +970,7 @@ static void adam_all(Surrogate* s, float lr, int t, cudaStream_t st) {
 
 int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound, int outpar) {
   const int n = v.nj * v.ni;
-  k_sur_begin<<<1, 1, 0, st>>>(s->ctl, s->judge_every, s->jacc);
+  k_sur_begin<<<1, 1, 0, st>>>(s->ctl, s->judge_every);
   const int* run = s->ctl + CTL_RUN;
   k_sur_features<true><<<feature_grid(n, s->kin), 128, 0, st>>>(v, nullptr, n, s->xmean, s->xstd, s->Xinf,
                                                                           s->kin, run);
@@ -968,7 +988,7 @@ int sur_cycle(Surrogate* s, View<float>& v, cudaStream_t st, int nsound, int out
 int sur_after(Surrogate* s, View<float>& v, cudaStream_t st) {
   const size_t n = (size_t)v.nj * v.ni * v.kz;
   k_sur_judge<<<grid1(n), 256, 0, st>>>(v, s->ctl, s->jsnap, s->Yinf, v.nj * v.ni, s->ymean, s->ystd, s->jacc);
-  k_sur_verdict<<<1, 1, 0, st>>>(s->ctl, s->jacc, s->tol, s->judge_every, s->max_interval, s->counts);
+  k_sur_verdict<<<1, 256, 0, st>>>(s->ctl, s->jacc, grid1(n), s->tol, s->judge_every, s->max_interval, s->counts);
   return 2;
 }
 
@@ -1055,7 +1075,7 @@ int moloch_sur_create(int kz, int capacity, int batch, unsigned long long seed, 
     A(&s->dZ[l], (size_t)batch * hid * 2); A(&s->dZT[l], (size_t)batch * hid * 2);
   }
   A((void**)&s->ctl, CTL_COUNT * sizeof(int)); A((void**)&s->counts, 4 * sizeof(unsigned long long));
-  A((void**)&s->jacc, 16 * sizeof(double));
+  A((void**)&s->jacc, (size_t)kGrid1Max * 10 * sizeof(double));  // per-block judge sums
   A((void**)&s->env, (size_t)s->nop * 4);
   if (e == cudaSuccess) {  // envelope 1 until moloch_sur_prepare measures it
     std::vector<float> one(s->nop, 1.f);

@@ -149,7 +149,7 @@ struct View {
 enum KernelKind {
   KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_DAMP, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE,
   KK_SOUND_MOMENTUM, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
-  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_COUNT
+  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_SOUND_COLUMN_TM, KK_COUNT
 };
 
 // Optional event recorder: when a launcher is given one, it records a CUDA
