@@ -54,6 +54,7 @@ ALG_WORDS = {
     "k_sound_damp": 8,        # r: zdiv2a u v fmz s | w: u v zdiv2b
     "k_sound_divdamp": 9,     # r: u v fmz rfw rfs | w: u v s zdiv2b (fused div + damp)
     "k_sound_column": 16,     # r: w fmzf qv tetav pai qsat t zdiv2b fmz qc qwltot qwitot | w: w deltaw tetav pai
+    "k_sound_column_tm": 16,  # the same arrays (the TMA-staged column solve)
     "k_sound_momentum": 7,    # r: u v deltaw tetav pai | w: u v
     "k_waf_vertical": 26,     # r: 7 fields u v w s wafu wafd | w: 10 wz ux vx wx
     "k_waf_horizontal": 36,   # r: 10 wz 10 pp u v wafn wafs wafe wafw | w: 10 pp
@@ -64,10 +65,16 @@ ALG_WORDS = {
 # from an ncu capture of the kernel, and the grid points of that capture;
 # scaled by the point count to the benchmarked size (traffic grows in
 # proportion: one pass over each array per launch)
-NCU_TRAFFIC = {"k_sound_column": (842.8e6, 384 * 384 * 60)}
-# sm__pipe_fp64_cycles_active (% of peak, active) from the same capture
+NCU_TRAFFIC = {"k_sound_column": (847.0e6, 384 * 384 * 60), "k_sound_column_tm": (498.7e6, 384 * 384 * 60)}
+# sm__pipe_fp64_cycles_active (% of peak, active) from the same captures
 NCU_FP64_PIPE = {"k_sound_column": {"pipe_fp64_active_pct": 35.7, "capture": "384x384x60",
-                                    "fp64_operations_per_level": 4}}
+                                    "fp64_operations_per_level": 4},
+                 "k_sound_column_tm": {"pipe_fp64_active_pct": 39.0, "capture": "384x384x60",
+                                       "fp64_operations_per_level": 4}}
+# the FP64 step's dominant kernels are bound by GB300's FP64 rate, not HBM:
+# their FP64-pipe activity from one-launch ncu captures at 256x256x60
+NCU_FP64_STEP = {"k_waf_vertical": {"pipe_fp64_active_pct": 87.2, "dram_pct": 1.8},
+                 "k_waf_horizontal": {"pipe_fp64_active_pct": 83.7, "dram_pct": 2.2}}
 # whole-step algorithmic words per grid point of the fused design target
 # (pre-diag 11 + 3 sound cycles x 91 + 3 advection steps x 23 + post-diag 11)
 B_ALG_WORDS = 364
@@ -325,11 +332,12 @@ def ensemble_members(dm, stream, n=64, seed=2024):
     return out
 
 
-# surrogate training: pairs from the first collect_steps steps of a scratch
-# domain of the same workload (another seed), so the training window covers
-# the timed steps
-SUR = {"collect_steps": 16, "cols_per_cycle": 1024, "iters": 4000, "lr": 1e-3, "batch": 256,
-       "threshold": 4.0, "judge_every": 6, "tol": 0.3}
+# surrogate training: pairs from plain steps of a scratch domain of the same
+# workload (another seed), in `windows` windows of collect_steps steps with
+# `gap` uncollected steps between them, so the training states come from
+# across the run and not only from its start
+SUR = {"collect_steps": 6, "windows": 3, "gap": 12, "cols_per_cycle": 1024, "iters": 4000, "lr": 1e-3,
+       "batch": 256, "threshold": 4.0, "judge_every": 6, "tol": 0.3}
 
 
 def train_surrogate(dm, mode, stream, jx, iy, kz, hills, cfg=SUR):
@@ -338,14 +346,19 @@ def train_surrogate(dm, mode, stream, jx, iy, kz, hills, cfg=SUR):
     t0 = time.perf_counter()
     scratch = dm.Moloch(jx, iy, kz, mode=mode, stream=stream)
     scratch.setup_idealized(hills=hills, pert_amp=0.5, pert_levels=10, seed=SEED + 7, device=True)
-    cap = cfg["collect_steps"] * scratch.params.mo_nadv * cfg["cols_per_cycle"]
+    nwin = cfg.get("windows", 1)
+    cap = nwin * cfg["collect_steps"] * scratch.params.mo_nadv * cfg["cols_per_cycle"]
     sur = dm.Surrogate(kz, capacity=cap, batch=cfg["batch"], seed=1)
-    pairs = sur.collect(scratch, cfg["collect_steps"], cols_per_cycle=cfg["cols_per_cycle"])
+    for w in range(nwin):
+        pairs = sur.collect(scratch, cfg["collect_steps"], cols_per_cycle=cfg["cols_per_cycle"], seed=3 + w)
+        if w + 1 < nwin:
+            scratch.run(cfg.get("gap", 0), graph=True)
     sur.prepare(0.1)
     _, v0 = sur.train(0)
     tl, vl = sur.train(cfg["iters"], lr=cfg["lr"])
     scratch.close()
-    info = {"pairs": pairs, "iters": cfg["iters"], "batch": cfg["batch"], "val_loss_untrained": v0,
+    info = {"pairs": pairs, "windows": f"{nwin} x {cfg['collect_steps']} steps, {cfg.get('gap', 0)} between",
+            "iters": cfg["iters"], "batch": cfg["batch"], "val_loss_untrained": v0,
             "val_loss": vl, "train_loss": tl, "seconds": time.perf_counter() - t0,
             "mlp": f"{45 * kz}->256->256->256->{5 * kz}, SiLU, BF16 operands, FP32 accumulate (tcgen05)"}
     return sur, info
@@ -494,7 +507,7 @@ def main():
         # learned acoustic-cycle surrogate case: 256 x 256 x 40, 20k training pairs
         JX, IY, KZ = 256, 256, 40
         HILLS = ((500.0, (JX + 1) / 2.0, (IY + 1) / 2.0, 10.0),)
-        SUR.update(collect_steps=7, cols_per_cycle=1024, iters=4000)
+        SUR.update(collect_steps=7, windows=1, cols_per_cycle=1024, iters=4000)
     if args.workload == "full1024":
         JX, IY = 1024, 1024
         HILLS = ((1000.0, (JX + 1) / 3.0, (IY + 1) / 2.0, 20.0), (1000.0, 2.0 * (JX + 1) / 3.0, (IY + 1) / 2.0, 20.0))
@@ -587,7 +600,8 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
                 "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind,
                 "alg_bytes_per_launch": alg_bytes, "avg_launch_ms": avg_ms,
                 "traffic": (NCU_TRAFFIC[tname][0] * gp / NCU_TRAFFIC[tname][1]) if tname in NCU_TRAFFIC else None,
-                "traffic_note": "ncu dram bytes of one launch at 384x384x60, scaled by grid points",
+                "traffic_note": "ncu dram bytes of one launch at 384x384x60, scaled by grid points (part of the "
+                                "staged kernel's writes is still in L2 when it ends)",
                 # second roof of the top kernel: its FP64 pivot recurrence (4
                 # FP64 operations per level) keeps the FP64 pipe this busy in
                 # the ncu capture of the same kernel
@@ -597,6 +611,12 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
                    "GBps_alg": (ALG_WORDS.get(k, 0) * esz * gp * v[1] / (v[0] / 1e3) / 1e9) if v[0] > 0 else None}
                for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
     kernels64 = {k: {"ms": round(v[0], 4), "launches": v[1]} for k, v in sorted(prof64.items(), key=lambda kv: -kv[1][0])}
+    top64 = max(prof64.items(), key=lambda kv: kv[1][0])[0]
+    roofline_fp64 = {"bound": "fp64 pipe", "kernel": top64, "unit": "fraction of the FP64 pipe",
+                     "frac": NCU_FP64_STEP.get(top64, {}).get("pipe_fp64_active_pct", float("nan")) / 100.0,
+                     "kernels": NCU_FP64_STEP, "capture": "ncu, one launch each, 256x256x60 FP64",
+                     "share_of_step": sum(v[0] for k, v in prof64.items() if k in NCU_FP64_STEP) /
+                     sum(v[0] for v in prof64.values())}
 
     # ---- end to end through the C ABI with host arrays ----------------------
     e2e = None
@@ -643,6 +663,7 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
                           "inference_ms_per_cycle": inference_ms,
                           "forced_on_error_vs_fp64": forced},
             "roofline": roofline,
+            "roofline_fp64_step": roofline_fp64,
             "kernels": kernels,
             "kernels_fp64": kernels64,
             "cpu_baseline": cpu,

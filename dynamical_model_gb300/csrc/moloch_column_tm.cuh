@@ -81,9 +81,10 @@ __device__ __forceinline__ float narrow_residual(double x) {
 __device__ __forceinline__ uint32_t fbits(float x) { return __float_as_uint(x); }
 __device__ __forceinline__ float bitsf(uint32_t x) { return __uint_as_float(x); }
 
-template <class T>
+template <class T, int LAST>
 __global__ void __launch_bounds__(kTmThreads, 1)
-    k_sound_column_tm(View<T> d, const __grid_constant__ ColumnMaps maps, int nsound, int last) {
+    k_sound_column_tm(View<T> d, const __grid_constant__ ColumnMaps maps, int nsound) {
+  constexpr bool last = LAST != 0;  // the last substep also completes s (Equation 10)
   static_assert(sizeof(T) == 4, "FP32 storage only");
   if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   extern __shared__ uint8_t smem_raw[];
@@ -233,12 +234,7 @@ __global__ void __launch_bounds__(kTmThreads, 1)
         const T fkm = S_(st, 7, q), tm = S_(st, 8, q);
         T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
         zrom1w = zrom1w - (((((T(kCpd) * wk) * fz) * fz) * ns) * dtrdz) * (tkm - tk);
-        if (qvk > T(0.96) * qsk && wk > T(0.1)) {
-          const T zqs = T(0.5) * (qsk + qskm);
-          const T zdth = ((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs) /
-                         ((((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
-          zrom1w = zrom1w + zdth * fz;
-        }
+        zrom1w = zrom1w_moist(zrom1w, qvk, qsk, qskm, wk, fz, pkm, tm, ns1, dts);
         T zwexpl = (wk - (zrom1w * dtrdz) * (pkm - pk)) - egdts;
         zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * prod_sub(pkm, zd_km, pk, zd_k);
         const T zu_t = ((zcs2 * fkm) * zrom1w) * pkm + ff;
@@ -324,7 +320,7 @@ __global__ void __launch_bounds__(kTmThreads, 1)
         const T fqc = S_(st, 4, q), fqwl = S_(st, 5, q), fqwi = S_(st, 6, q);
         T zd = fzd;
         zd = zd + (dtrdz * ffmz) * (wlo - wn);
-        zd = (zd * ((T(1) + T(0.86) * fqv) + T(3.2) * fqc)) / ((T(1) + T(0.96) * fqv) + T(4.8) * fqc);
+        zd = div_corr(zd * ((T(1) + T(0.86) * fqv) + T(3.2) * fqc), (T(1) + T(0.96) * fqv) + T(4.8) * fqc);
         if (own) {
           const size_t qm = (size_t)m * pl;
           tc::st_hint(ptet + qm,

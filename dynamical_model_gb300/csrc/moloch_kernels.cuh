@@ -313,6 +313,43 @@ __device__ __forceinline__ double prod_sub(double a, double b, double c, double 
 __device__ __forceinline__ float prod_add(float a, float b, float c, float d) { return __fmaf_rn(c, d, __fmul_rn(a, b)); }
 __device__ __forceinline__ double prod_add(double a, double b, double c, double d) { return a * b + c * d; }
 
+// Quotient of the Exner/theta update in FP32 storage: the reciprocal
+// estimate q = a * rcp(b) with one residual correction q + (a - b q) rcp(b)
+// (Markstein's quotient correction, P. Markstein, "IA-64 and Elementary
+// Functions", 2000): within one ulp of the IEEE quotient for the normal,
+// well-scaled values it sees here (b = 1 + 0.96 qv + 4.8 qc), with no slow
+// path or branch.  FP64 keeps the IEEE quotient.
+__device__ __forceinline__ float div_corr(float a, float b) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(b));
+  const float q = a * r;
+  return fmaf(fmaf(-b, q, a), r, q);
+}
+__device__ __forceinline__ double div_corr(double a, double b) { return a / b; }
+
+// zrom1w of the implicit w with the latent-heat term of saturated rising
+// air (:641-652).  FP32 storage: the term is evaluated on every level (fast
+// divide) and selected, so the level loop has no data-dependent branch;
+// FP64: the reference's branch and IEEE divide.
+template <class T>
+__device__ __forceinline__ T zrom1w_moist(T zrom1w, T qvk, T qsk, T qskm, T wk, T fz, T pkm, T tm, T ns1, T dts) {
+  if constexpr (sizeof(T) == 4) {
+    const T zqs = T(0.5) * (qsk + qskm);
+    const T zdth = __fdividef((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs,
+                              (((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
+    const T zl = zrom1w + zdth * fz;
+    return (qvk > T(0.96) * qsk && wk > T(0.1)) ? zl : zrom1w;
+  } else {
+    if (qvk > T(0.96) * qsk && wk > T(0.1)) {
+      const T zqs = T(0.5) * (qsk + qskm);
+      const T zdth = ((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs) /
+                     ((((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
+      zrom1w = zrom1w + zdth * fz;
+    }
+    return zrom1w;
+  }
+}
+
 // ---- sound: implicit w (Thomas, :634-686) + Exner/theta (:690-728) -----
 // One thread per column.  Down-sweep k = kz..2 with FP64 pivots in every
 // mode, stash of the FP64 down-sweep values, then back-substitution fused
@@ -394,12 +431,7 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     const T qskm = cur.qskm, zd_km = cur.zdkm, fkm = cur.fkm, tm = cur.tm;
     T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
     zrom1w = zrom1w - (((((T(kCpd) * wk) * fz) * fz) * ns) * dtrdz) * (tkm - tk);
-    if (qvk > T(0.96) * qsk && wk > T(0.1)) {
-      const T zqs = T(0.5) * (qsk + qskm);
-      const T zdth = ((((((T(kEgrav) * wk) * ns1) * dts) * T(kWlhv)) * T(kWlhv)) * zqs) /
-                     ((((T(kCpd) * pkm) * T(kRwat)) * tm) * tm);
-      zrom1w = zrom1w + zdth * fz;
-    }
+    zrom1w = zrom1w_moist(zrom1w, qvk, qsk, qskm, wk, fz, pkm, tm, ns1, dts);
     T zwexpl = (wk - (zrom1w * dtrdz) * (pkm - pk)) - egdts;
     zwexpl = zwexpl + ((T(kRdrcv) * zrom1w) * dtrdz) * prod_sub(pkm, zd_km, pk, zd_k);
     const T zu_t = ((zcs2 * fkm) * zrom1w) * pkm + ff;
@@ -463,7 +495,7 @@ __device__ __forceinline__ void b_sound_column(const View<T>& d, const int bx, c
     const size_t q = (size_t)m * pl;
     T zd = f.zd;
     zd = zd + (dtrdz * f.fmz) * (wl - wh);
-    zd = (zd * ((T(1) + T(0.86) * f.qv) + T(3.2) * f.qc)) / ((T(1) + T(0.96) * f.qv) + T(4.8) * f.qc);
+    zd = div_corr(zd * ((T(1) + T(0.86) * f.qv) + T(3.2) * f.qc), (T(1) + T(0.96) * f.qv) + T(4.8) * f.qc);
     TET[q] = f.tet * (T(1) + (rdrcv * zd) * (prod_add(T(0.25), f.qv, T(4.2), f.qwl) + T(2.1) * f.qwi));
     if (defer_pai) {
       ZD[q] = zd;
@@ -2097,9 +2129,13 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       bool staged = false;
       if constexpr (sizeof(T) == 4) {
         if (column_tm_ok(d)) {
-          MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
-                        k_sound_column_tm<T><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(
-                            d, static_cast<const ColumnMaps*>(d.cmaps)[d.fcur], ns, last));
+          const ColumnMaps& cm = static_cast<const ColumnMaps*>(d.cmaps)[d.fcur];
+          if (last)
+            MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
+                          k_sound_column_tm<T, 1><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(d, cm, ns));
+          else
+            MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
+                          k_sound_column_tm<T, 0><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(d, cm, ns));
           staged = true;
         }
       }

@@ -1,5 +1,6 @@
 // FP64 and FP32-storage kernels with multiply-add contraction allowed.
 #define MOLOCH_KNS kfast
+#include "../../include/moloch_gb300.h"
 #include "moloch_kernels.cuh"
 
 namespace moloch {
@@ -63,7 +64,8 @@ bool build_column_maps(const View<float>& v, void* out) {
   if (!fn) return false;
   static std::once_flag attr;
   std::call_once(attr, [] {
-    cudaFuncSetAttribute(k_sound_column_tm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem);
+    cudaFuncSetAttribute(k_sound_column_tm<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem);
+    cudaFuncSetAttribute(k_sound_column_tm<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem);
   });
   ColumnMaps* cm = static_cast<ColumnMaps*>(out);
   const int nj = v.nj, ni = v.ni, kz = v.kz;
@@ -83,3 +85,27 @@ bool build_column_maps(const View<float>& v, void* out) {
 }
 }  // namespace kfast
 }  // namespace moloch
+
+// ---- arithmetic check of the FP32 quotient with one correction --------------
+namespace moloch {
+namespace kfast {
+__global__ void k_check_division(const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ qc,
+                                 float* __restrict__ qi, int n) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    qc[q] = div_corr(a[q], b[q]);
+    qi[q] = a[q] / b[q];
+  }
+}
+}  // namespace kfast
+}  // namespace moloch
+
+// div_corr (the quotient of the FP32 Exner/theta update) and CUDA's IEEE
+// FP32 quotient of the same device arrays, for tests of its error bound
+extern "C" int moloch_gpu_check_division(const float* a, const float* b, float* q_corr, float* q_ieee, int n,
+                                         void* stream) {
+  if (!a || !b || !q_corr || !q_ieee || n < 0) return MOLOCH_ERR_ARG;
+  if (n == 0) return MOLOCH_OK;
+  const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+  moloch::kfast::k_check_division<<<blocks, 256, 0, (cudaStream_t)stream>>>(a, b, q_corr, q_ieee, n);
+  return cudaPeekAtLastError() == cudaSuccess ? MOLOCH_OK : MOLOCH_ERR_CUDA;
+}

@@ -205,6 +205,13 @@ int moloch_gpu_sync(moloch_handle_t* h);
  * no device waits). */
 int moloch_gpu_set_wait_limit(moloch_handle_t* h, long long cycles, int skip_job);
 
+/* Arithmetic check (tests): for n device values, q_corr = the quotient the
+ * FP32 Exner/theta update uses (reciprocal estimate with one residual
+ * correction) and q_ieee = CUDA's IEEE FP32 quotient a / b, on the given
+ * stream (a cudaStream_t, NULL for the default).  No reference
+ * counterpart. */
+int moloch_gpu_check_division(const float* a, const float* b, float* q_corr, float* q_ieee, int n, void* stream);
+
 /* The stream the handle launches on (a cudaStream_t). */
 void* moloch_gpu_stream(moloch_handle_t* h);
 

@@ -22,8 +22,9 @@ Asserted: the counts add up; the plain FP32 run is within the error budget
 run (its errors are at most those of the surrogate forced on).  The gain
 itself is recorded, not asserted.  Measured on GB300: 10 of 72 cycles
 committed, the judged step 1.10x the plain FP32 step, theta RMSE 0.078 K
-(plain FP32: 0.0009 K) -- the surrogate does not gain on this workload, and
-its few accepted cycles already exceed the error budget.
+(plain FP32: 0.0009 K); forced on for every cycle it diverges (NaN) within
+the 24 steps -- the surrogate does not gain on this workload, and its few
+accepted cycles already exceed the error budget.
 """
 import json
 
@@ -105,8 +106,9 @@ def test_surrogate_gain_is_stated(gpu_lib):
     assert 0 <= c["plain"] <= c["cycles"] and c["judged"] >= 1 and c["judge_rejections"] <= c["judged"]
     e = err["fp32"]
     assert e["theta_K"] <= 0.05 and e["u"] <= 0.05 and e["v"] <= 0.05 and e["w"] <= 0.05, record
-    for f in ("theta_K", "u", "v", "w"):
-        assert err["fp32_surrogate"][f] <= err["fp32_surrogate_forced"][f], (f, record)
+    for f in ("theta_K", "u", "v", "w"):  # a forced run that diverged (NaN) counts as unbounded error
+        ej, ef = err["fp32_surrogate"][f], err["fp32_surrogate_forced"][f]
+        assert np.isfinite(ej) and (not np.isfinite(ef) or ej <= ef), (f, record)
     sur.close()
     for g in (scratch, ref, plain, judged, forced):
         g.close()
