@@ -387,13 +387,16 @@ def surrogate_forced_error(torch, dm, sur, stream, jx, iy, kz, hills, ref_fields
 def run_accuracy(args, torch, dm, stream):
     """Long-run error of the FP32 paths against the FP64 GPU step (which
     matches the FP64 oracle to <= 1e-9 relative L2 after 100 steps): the
-    512 x 512 x 60 workload advanced --steps steps, RMSE checkpoints every
-    --steps/10 steps."""
+    512 x 512 x 60 workload (--workload accuracy) or the 1024 x 1024 x 60
+    full-stack workload with two 1 km hills (--workload accuracy1024)
+    advanced --steps steps, RMSE checkpoints every --steps/10 steps, all
+    three paths with their autotuned launch shapes."""
     sptr = stream.cuda_stream
     sur, sur_train = train_surrogate(dm, "fp32_mixed", sptr, JX, IY, KZ, HILLS)
-    d64 = make_domain(dm, "fp64", sptr)
-    dmix = make_domain(dm, "fp32_mixed", sptr)
+    d64, tune_64 = tuned(dm, "fp64", sptr)
+    dmix, tune_mix = tuned(dm, "fp32_mixed", sptr)
     dsur = make_domain(dm, "fp32_mixed", sptr)
+    dsur.set_tuning(tune_mix)
     sur.attach(dsur, threshold=SUR["threshold"], judge_every=SUR["judge_every"], tol=SUR["tol"])
     every = max(1, args.steps // 10)
     curve = []
@@ -413,6 +416,7 @@ def run_accuracy(args, torch, dm, stream):
                          "w_rmse_ms": rmse(d.get("w"), d64.get("w"))}
         curve.append(row)
     line = {"metric": "RMSE against the FP64 GPU step", "workload": f"{JX}x{IY}x{KZ}", "steps": args.steps,
+            "hills": HILLS, "autotuned": {"fp64": tune_64, "fp32_mixed": tune_mix},
             "target": {"theta_rmse_K": 0.05, "u_v_rmse_ms": 0.05}, "curve": curve,
             "surrogate": {"training": sur_train, "judge": sur.stats_counts()},
             "seconds": time.perf_counter() - t0}
@@ -485,9 +489,10 @@ def main():
                     help="comma-separated launch shapes for --only instead of autotuning (profiling runs under a "
                          "profiler, whose timings would mislead the autotuner), e.g. 32,24,1")
     ap.add_argument("--workload", default="single",
-                    choices=["single", "ensemble", "full1024", "surrogate", "accuracy"],
+                    choices=["single", "ensemble", "full1024", "surrogate", "accuracy", "accuracy1024"],
                     help="single: 512x512x60 (headline); ensemble: 64 uneven members; full1024: 1024x1024x60; "
-                         "surrogate: 256x256x40 surrogate case; accuracy: --steps-long error run vs FP64")
+                         "surrogate: 256x256x40 surrogate case; accuracy: --steps-long error run vs FP64; "
+                         "accuracy1024: the same on the 1024x1024x60 two-hill workload")
     args = ap.parse_args()
     global JX, IY, KZ, HILLS
     if args.size:
@@ -508,7 +513,7 @@ def main():
         JX, IY, KZ = 256, 256, 40
         HILLS = ((500.0, (JX + 1) / 2.0, (IY + 1) / 2.0, 10.0),)
         SUR.update(collect_steps=7, windows=1, cols_per_cycle=1024, iters=4000)
-    if args.workload == "full1024":
+    if args.workload in ("full1024", "accuracy1024"):
         JX, IY = 1024, 1024
         HILLS = ((1000.0, (JX + 1) / 3.0, (IY + 1) / 2.0, 20.0), (1000.0, 2.0 * (JX + 1) / 3.0, (IY + 1) / 2.0, 20.0))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -517,7 +522,7 @@ def main():
     stream = torch.cuda.Stream(device=device)
     sptr = stream.cuda_stream
 
-    if args.workload == "accuracy":
+    if args.workload in ("accuracy", "accuracy1024"):
         return run_accuracy(args, torch, dm, stream) if rank == 0 else 0
     # ---- headline path: FP32 storage + FP64 solve --------------------------
     if args.only:

@@ -11,7 +11,9 @@ Runs from the same initial state, 24 steps each: the FP64 step (the
 reference), the plain FP32 step, FP32 with the surrogate attached under its
 judge (the plain loop every 6th cycle, relative RMS error tolerance 0.3; a
 rejection switches the surrogate off with a doubling interval), and FP32
-with the surrogate forced on for every cycle (no judge, no envelope check).
+with the surrogate forced on for every cycle (no judge, no envelope bound;
+the on-device check still falls back to the plain loop when a prediction
+is not finite).
 
 Stated (printed as one record): cycles committed to the surrogate and their
 fraction, the time per step of the judged and forced runs against the
@@ -97,12 +99,13 @@ def test_surrogate_gain_is_stated(gpu_lib):
     committed = c["cycles"] - c["plain"]
     record = {"workload": f"{JX}x{IY}x{KZ}, {STEPS} steps", "val_loss": [v0, vl],
               "cycles": c["cycles"], "committed": committed, "committed_fraction": committed / c["cycles"],
-              "verdicts": c["judged"], "rejections": c["judge_rejections"], "ms_per_step": ms,
+              "verdicts": c["judged"], "rejections": c["judge_rejections"],
+              "forced_run_fallbacks_on_non_finite_output": cf["plain"], "ms_per_step": ms,
               "step_time_ratio_over_plain": {k: ms[k] / ms["fp32"] for k in ms if k != "fp32"},
               "rmse_vs_fp64": err,
               "gain": "none" if committed == 0 or ms["fp32_surrogate"] >= ms["fp32"] else "faster"}
     print("surrogate gain:", json.dumps(record))
-    assert c["cycles"] == STEPS * nadv and cf["cycles"] == STEPS * nadv and cf["plain"] == 0
+    assert c["cycles"] == STEPS * nadv and cf["cycles"] == STEPS * nadv and cf["judged"] == 0
     assert 0 <= c["plain"] <= c["cycles"] and c["judged"] >= 1 and c["judge_rejections"] <= c["judged"]
     e = err["fp32"]
     assert e["theta_K"] <= 0.05 and e["u"] <= 0.05 and e["v"] <= 0.05 and e["w"] <= 0.05, record
