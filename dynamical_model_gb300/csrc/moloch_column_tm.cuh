@@ -37,7 +37,7 @@
 namespace moloch {
 namespace MOLOCH_KNS {
 
-constexpr int kKCT = 4;                          // levels per staged chunk
+constexpr int kKCT = 4;                          // levels per staged chunk (a multiple of 4)
 constexpr int kTmStages = 4;                     // ring depth
 constexpr int kTmSlots = 9;                      // arrays per stage
 constexpr int kTmRows = 8;                       // rows (i) per tile = compute warps
@@ -264,7 +264,8 @@ __global__ void __launch_bounds__(kTmThreads, 1)
           uint32_t rec[4 * kKCT];
 #pragma unroll
           for (int u = 0; u < kKCT; ++u) dn_level(st, kKCT - 1 - u, kk_hi - u, rec + 4 * (kKCT - 1 - u));
-          tc::tmem_st16(trow + (uint32_t)(4 * kk_lo), rec);
+#pragma unroll
+          for (int h = 0; h < kKCT / 4; ++h) tc::tmem_st16p(trow + (uint32_t)(4 * kk_lo + 16 * h), rec + 16 * h);
         } else {
           for (int kk = kk_hi; kk >= 1; --kk) {
             uint32_t rec[4];
@@ -294,7 +295,10 @@ __global__ void __launch_bounds__(kTmThreads, 1)
         fzd = bitsf(r0[3]);
       }
       uint32_t cur[4 * kKCT], nxt[4 * kKCT];
-      if (nfull > 0) tc::tmem_ld16u(trow + 4u, nxt);
+      if (nfull > 0) {
+#pragma unroll
+        for (int h = 0; h < kKCT / 4; ++h) tc::tmem_ld16p(trow + 4u + 16u * h, nxt + 16 * h);
+      }
       T* __restrict__ pw = d.w + c;
       T* __restrict__ pdw = d.deltaw + c;
       T* __restrict__ ptet = d.tetav + c;
@@ -338,10 +342,14 @@ __global__ void __launch_bounds__(kTmThreads, 1)
         if (!st) break;
         const int kk0 = cc * kKCT + 1;
         if (cc < nfull) {
-          tc::tmem_wait_ld16(nxt);
+#pragma unroll
+          for (int h = 0; h < kKCT / 4; ++h) tc::tmem_wait_ld16p(nxt + 16 * h);
 #pragma unroll
           for (int e = 0; e < 4 * kKCT; ++e) cur[e] = nxt[e];
-          if (cc + 1 < nfull) tc::tmem_ld16u(trow + (uint32_t)(4 * (kk0 + kKCT)), nxt);
+          if (cc + 1 < nfull) {
+#pragma unroll
+            for (int h = 0; h < kKCT / 4; ++h) tc::tmem_ld16p(trow + (uint32_t)(4 * (kk0 + kKCT) + 16 * h), nxt + 16 * h);
+          }
 #pragma unroll
           for (int u = 0; u < kKCT; ++u) up_level(st, u, kk0 + u, cur + 4 * u);
         } else {

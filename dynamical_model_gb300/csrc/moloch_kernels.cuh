@@ -566,6 +566,7 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4)
 }  // namespace MOLOCH_KNS
 }  // namespace moloch
 #include "moloch_column_tm.cuh"
+#include "moloch_momentum_tm.cuh"
 namespace moloch {
 namespace MOLOCH_KNS {
 
@@ -2142,7 +2143,20 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       if (!staged) MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
-    if (d.kmarch & 8) {
+    bool mstaged = false;
+    if constexpr (sizeof(T) == 4) {
+      if ((d.kmarch & 64) && d.mmaps) {
+        const MomentumMaps& mm = *static_cast<const MomentumMaps*>(d.mmaps);
+        MomentumSel sel;
+        sel.u = mm.m[MM_U0 + d.cur]; sel.v = mm.m[MM_V0 + d.cur];
+        sel.tet = mm.m[MM_T0 + d.fcur]; sel.pai = mm.m[MM_P0 + d.fcur]; sel.dw = mm.m[MM_DW];
+        const dim3 mg((d.nj + 31) / 32, (d.ni + kMtRows - 1) / kMtRows);
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM_TM, st, k_momentum_tm<T><<<mg, kMtThreads, kMtSmem, st>>>(d, sel));
+        mstaged = true;
+      }
+    }
+    if (mstaged) {
+    } else if (d.kmarch & 8) {
       const int nstrips = ((d.nj + kMomJ - 1) / kMomJ) * ((d.ni + kMomR - 1) / kMomR);
       MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
     } else if (d.kmarch & 4)
