@@ -567,6 +567,7 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4)
 }  // namespace moloch
 #include "moloch_column_tm.cuh"
 #include "moloch_momentum_tm.cuh"
+#include "moloch_divdamp_tm.cuh"
 namespace moloch {
 namespace MOLOCH_KNS {
 
@@ -2106,8 +2107,22 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   for (int ns = 1; ns <= fl.nsound; ++ns) {
     const int last = ns == fl.nsound;
     if (d.kmarch & 16) {
-      const int nstrips = ((d.nj + kDDJ - 1) / kDDJ) * ((d.ni + kDDR - 1) / kDDR);
-      MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
+      bool dstaged = false;
+      if constexpr (sizeof(T) == 4) {
+        if ((d.kmarch & 128) && d.dmaps) {
+          const DivdampMaps& dm = *static_cast<const DivdampMaps*>(d.dmaps);
+          DivdampSel sel;
+          sel.u = dm.m[DM_U0 + d.cur]; sel.v = dm.m[DM_V0 + d.cur];
+          sel.rfw = dm.m[DM_RFW]; sel.rfs = dm.m[DM_RFS]; sel.fmz = dm.m[DM_FMZ];
+          const dim3 dg((d.nj + 31) / 32, (d.ni + kDtRows - 1) / kDtRows);
+          MOLOCH_LAUNCH(KK_SOUND_DIVDAMP_TM, st, k_divdamp_tm<T><<<dg, kDtThreads, kDtSmem, st>>>(d, sel));
+          dstaged = true;
+        }
+      }
+      if (!dstaged) {
+        const int nstrips = ((d.nj + kDDJ - 1) / kDDJ) * ((d.ni + kDDR - 1) / kDDR);
+        MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
+      }
       d.cur ^= 1;  // the damped u, v are in the other buffer
       ++n;
     } else {

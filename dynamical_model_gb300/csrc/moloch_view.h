@@ -113,7 +113,8 @@ struct View {
   int kmarch;      // sound kernel variants, bit mask: 1 divergence, 2 damping, 4 momentum
                    // k-marching; 8 momentum as warp strips; 16 divergence + damping fused;
                    // 32 column solve staged by TMA with its column state in TMEM;
-                   // 64 momentum as TMA-staged k-marching tiles (overrides 4 and 8)
+                   // 64 momentum as TMA-staged k-marching tiles (overrides 4 and 8);
+                   // 128 with 16: the fused divergence/damping as TMA-staged tiles
   int vfields;     // advected fields per thread of k_waf_vertical: 1, 2, 5 or 10
 
   // set when a learned surrogate stands in for sound(): the plain sound
@@ -125,8 +126,10 @@ struct View {
   // the two sets of TMA tensor maps (one per advected-field buffer set),
   // nullptr when the kernel cannot run on this domain
   const void* cmaps;
-  // the same for the staged momentum kernel (k_momentum_tm)
+  // the same for the staged momentum kernel (k_momentum_tm) and the staged
+  // divergence/damping kernel (k_divdamp_tm)
   const void* mmaps;
+  const void* dmaps;
   // device word set by a bounded wait that gave up (MOLOCH_ERR_TIMEOUT)
   int* kerr;
   long long spin_cycles;  // limit of every such wait, in SM clock cycles
@@ -152,7 +155,7 @@ struct View {
 enum KernelKind {
   KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_DAMP, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE,
   KK_SOUND_MOMENTUM, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
-  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_SOUND_COLUMN_TM, KK_SOUND_MOMENTUM_TM, KK_COUNT
+  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_SOUND_COLUMN_TM, KK_SOUND_MOMENTUM_TM, KK_SOUND_DIVDAMP_TM, KK_COUNT
 };
 
 // Optional event recorder: when a launcher is given one, it records a CUDA

@@ -249,7 +249,9 @@ const char* moloch_gpu_kernel_name(int kind);
  *               kz <= 64; elsewhere the bit is ignored), 64 the momentum
  *               update as TMA-staged tiles of 32 x 8 columns marching down
  *               the levels (FP32 storage, jx a multiple of 4; overrides 4
- *               and 8); 0 = one level per thread;
+ *               and 8), 128 (with 16) the fused divergence/damping as
+ *               TMA-staged tiles of the same kind (FP32 storage, jx a
+ *               multiple of 4); 0 = one level per thread;
  *   choice[2] = advected fields per thread of the vertical WAF kernel:
  *               1, 2, 5 or 10 (the fields of a thread share the velocity
  *               loads and terms).

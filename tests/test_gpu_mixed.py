@@ -23,12 +23,13 @@ def rmse(a, b):
     return float(np.sqrt(np.mean((np.asarray(a) - np.asarray(b)) ** 2)))
 
 
-@pytest.mark.parametrize("tuning", [[1, 0], [32, 11], [32, 24], [32, 56], [32, 120]])
+@pytest.mark.parametrize("tuning", [[1, 0], [32, 11], [32, 24], [32, 56], [32, 120], [32, 240]])
 def test_mixed_100_steps_vs_oracle(oracle_mod, gpu_lib, tuning):
     """Default kernels, and the FP32 variants the autotuner picks on GB300
     (warp strips for the horizontal WAF and the momentum, k-marching or
     fused warp-strip divergence and damping, the column solve staged by
-    TMA with its state in TMEM, the momentum update staged by TMA)."""
+    TMA with its state in TMEM, the momentum update and the fused
+    divergence/damping staged by TMA)."""
     o, g = pair(oracle_mod, gpu_lib, 100, 100, 30, mode="fp32_mixed")
     g.set_tuning(tuning)
     for s in range(1, 101):
