@@ -37,8 +37,8 @@
 namespace moloch {
 namespace MOLOCH_KNS {
 
-constexpr int kKCT = 4;                          // levels per staged chunk (a multiple of 4)
-constexpr int kTmStages = 4;                     // ring depth
+constexpr int kKCT = 8;                          // levels per staged chunk (a multiple of 4)
+constexpr int kTmStages = 3;                     // ring depth
 constexpr int kTmSlots = 9;                      // arrays per stage
 constexpr int kTmRows = 8;                       // rows (i) per tile = compute warps
 constexpr int kTmSlotBytes = kKCT * kTmRows * 32 * 4;  // one 32 x 8 x kKCT FP32 box

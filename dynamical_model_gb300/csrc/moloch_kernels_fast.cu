@@ -87,6 +87,8 @@ bool build_divdamp_maps(const View<float>& v, void* out) {
   if (v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;
   EncodeTiledFn fn = encode_tiled();
   if (!fn) return false;
+  static std::once_flag attr;
+  std::call_once(attr, [] { cudaFuncSetAttribute(k_divdamp_tm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDtSmem); });
   DivdampMaps* dm = static_cast<DivdampMaps*>(out);
   const int nj = v.nj, ni = v.ni, kz = v.kz;
   const bool ok = map_div(fn, &dm->m[DM_U0], v.ubuf[0], nj, ni, kz) && map_div(fn, &dm->m[DM_U1], v.ubuf[1], nj, ni, kz) &&
@@ -100,6 +102,8 @@ bool build_momentum_maps(const View<float>& v, void* out) {
   if (v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;
   EncodeTiledFn fn = encode_tiled();
   if (!fn) return false;
+  static std::once_flag attr;
+  std::call_once(attr, [] { cudaFuncSetAttribute(k_momentum_tm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMtSmem); });
   MomentumMaps* mm = static_cast<MomentumMaps*>(out);
   const int nj = v.nj, ni = v.ni, kz = v.kz;
   const bool ok = map_mom(fn, &mm->m[MM_U0], v.ubuf[0], nj, ni, kz) && map_mom(fn, &mm->m[MM_U1], v.ubuf[1], nj, ni, kz) &&
