@@ -228,8 +228,6 @@ struct moloch_handle {
   // TMA tensor maps of the staged column kernel (FP32 storage), one set per
   // advected-field buffer set
   alignas(64) unsigned char cmaps[4096];
-  alignas(64) unsigned char mmaps[2048];  // and of the staged momentum kernel
-  alignas(64) unsigned char dmaps[1024];  // and of the staged divergence/damping kernel
   int nj() const { return grid.jx; }
   int ni() const { return grid.iy; }
   int kz() const { return grid.kz; }
@@ -298,8 +296,6 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.vfields = 1;
   v.sur_skip = nullptr;
   v.cmaps = nullptr;
-  v.mmaps = nullptr;
-  v.dmaps = nullptr;
   v.spin_cycles = kDefaultSpinCycles;
   v.fault_skip_job = -1;
   return off + 256;
@@ -668,12 +664,6 @@ int init_impl(moloch_handle* h, View<T>& v) {
     v.cmaps = nullptr;
     if (kfast::column_maps_bytes() <= (int)sizeof(h->cmaps) && kfast::build_column_maps(v, h->cmaps))
       v.cmaps = h->cmaps;
-    v.mmaps = nullptr;
-    if (kfast::momentum_maps_bytes() <= (int)sizeof(h->mmaps) && kfast::build_momentum_maps(v, h->mmaps))
-      v.mmaps = h->mmaps;
-    v.dmaps = nullptr;
-    if (kfast::divdamp_maps_bytes() <= (int)sizeof(h->dmaps) && kfast::build_divdamp_maps(v, h->dmaps))
-      v.dmaps = h->dmaps;
   }
   return MOLOCH_OK;
 }
@@ -1284,7 +1274,7 @@ long long moloch_gpu_kernel_count(moloch_handle_t* h) { return h ? h->kernels : 
 static const char* const kKindNames[KK_COUNT] = {
     "k_prediag", "k_sound_div", "k_sound_damp", "k_sound_column", "k_lap_filter", "k_pai_update",
     "k_sound_momentum", "k_waf_vertical", "k_waf_horizontal", "k_stag_from_x",
-    "k_filter_increment", "k_postdiag", "k_diag", "k_sound_divdamp", "k_sound_column_tm", "k_momentum_tm", "k_divdamp_tm"};
+    "k_filter_increment", "k_postdiag", "k_diag", "k_sound_divdamp", "k_sound_column_tm"};
 
 int moloch_gpu_kernel_kinds(void) { return KK_COUNT; }
 
@@ -1350,7 +1340,7 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     h->vf.hz_levels = choice[0];
   }
   if (n > 1) {
-    if (choice[1] < 0 || choice[1] > 255) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 63) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     h->vd.kmarch = choice[1];
     h->vf.kmarch = choice[1];
   }
@@ -1404,14 +1394,10 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   double best1 = 1e30;
   int pick1 = h->elem == 8 ? h->vd.kmarch : h->vf.kmarch;
   const bool staged_ok = h->elem == 4 && h->vf.cmaps != nullptr;
-  const bool mstaged_ok = h->elem == 4 && h->vf.mmaps != nullptr;
-  const bool dstaged_ok = h->elem == 4 && h->vf.dmaps != nullptr;
-  for (int cand = 0; cand < 256; ++cand) {
-    if ((cand & 128) && (!dstaged_ok || !(cand & 16))) continue;  // staged divergence/damping: the fused kernel
+  for (int cand = 0; cand < 64; ++cand) {
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both
     if ((cand & 32) && !staged_ok) continue;  // staged column solve: FP32 domains with tensor maps
-    if ((cand & 64) && (!mstaged_ok || (cand & 12))) continue;  // staged momentum replaces 4 and 8
     h->vd.kmarch = cand;
     h->vf.kmarch = cand;
     float ms = 0.f, tot = 0.f;

@@ -566,8 +566,6 @@ __global__ void __launch_bounds__(kColBX* kColBY, sizeof(T) == 4 ? 8 : 4)
 }  // namespace MOLOCH_KNS
 }  // namespace moloch
 #include "moloch_column_tm.cuh"
-#include "moloch_momentum_tm.cuh"
-#include "moloch_divdamp_tm.cuh"
 namespace moloch {
 namespace MOLOCH_KNS {
 
@@ -2107,22 +2105,8 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
   for (int ns = 1; ns <= fl.nsound; ++ns) {
     const int last = ns == fl.nsound;
     if (d.kmarch & 16) {
-      bool dstaged = false;
-      if constexpr (sizeof(T) == 4) {
-        if ((d.kmarch & 128) && d.dmaps) {
-          const DivdampMaps& dm = *static_cast<const DivdampMaps*>(d.dmaps);
-          DivdampSel sel;
-          sel.u = dm.m[DM_U0 + d.cur]; sel.v = dm.m[DM_V0 + d.cur];
-          sel.rfw = dm.m[DM_RFW]; sel.rfs = dm.m[DM_RFS]; sel.fmz = dm.m[DM_FMZ];
-          const dim3 dg((d.nj + 31) / 32, (d.ni + kDtRows - 1) / kDtRows);
-          MOLOCH_LAUNCH(KK_SOUND_DIVDAMP_TM, st, k_divdamp_tm<T><<<dg, kDtThreads, kDtSmem, st>>>(d, sel));
-          dstaged = true;
-        }
-      }
-      if (!dstaged) {
-        const int nstrips = ((d.nj + kDDJ - 1) / kDDJ) * ((d.ni + kDDR - 1) / kDDR);
-        MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
-      }
+      const int nstrips = ((d.nj + kDDJ - 1) / kDDJ) * ((d.ni + kDDR - 1) / kDDR);
+      MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
       d.cur ^= 1;  // the damped u, v are in the other buffer
       ++n;
     } else {
@@ -2158,20 +2142,7 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       if (!staged) MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
-    bool mstaged = false;
-    if constexpr (sizeof(T) == 4) {
-      if ((d.kmarch & 64) && d.mmaps) {
-        const MomentumMaps& mm = *static_cast<const MomentumMaps*>(d.mmaps);
-        MomentumSel sel;
-        sel.u = mm.m[MM_U0 + d.cur]; sel.v = mm.m[MM_V0 + d.cur];
-        sel.tet = mm.m[MM_T0 + d.fcur]; sel.pai = mm.m[MM_P0 + d.fcur]; sel.dw = mm.m[MM_DW];
-        const dim3 mg((d.nj + 31) / 32, (d.ni + kMtRows - 1) / kMtRows);
-        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM_TM, st, k_momentum_tm<T><<<mg, kMtThreads, kMtSmem, st>>>(d, sel));
-        mstaged = true;
-      }
-    }
-    if (mstaged) {
-    } else if (d.kmarch & 8) {
+    if (d.kmarch & 8) {
       const int nstrips = ((d.nj + kMomJ - 1) / kMomJ) * ((d.ni + kMomR - 1) / kMomR);
       MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
     } else if (d.kmarch & 4)

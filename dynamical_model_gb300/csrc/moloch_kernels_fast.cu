@@ -57,64 +57,6 @@ bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, i
 }  // namespace
 
 int column_maps_bytes() { return (int)(2 * sizeof(ColumnMaps)); }
-int momentum_maps_bytes() { return (int)sizeof(MomentumMaps); }
-
-// dense FP32 field (nj, ni, nk) as 40 x 10 x 1 boxes (a momentum tile with its halo)
-static bool map_mom(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, int nk) {
-  const cuuint64_t dims[3] = {(cuuint64_t)nj, (cuuint64_t)ni, (cuuint64_t)nk};
-  const cuuint64_t strides[2] = {(cuuint64_t)nj * 4, (cuuint64_t)nj * ni * 4};
-  const cuuint32_t box[3] = {(cuuint32_t)kMtBoxJ, (cuuint32_t)kMtBoxI, 1};
-  const cuuint32_t es[3] = {1, 1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-int divdamp_maps_bytes() { return (int)sizeof(DivdampMaps); }
-
-// dense FP32 field (nj, ni, nk) as 40 x 11 x 1 boxes (a divergence/damping tile with its halo)
-static bool map_div(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, int nk) {
-  const cuuint64_t dims[3] = {(cuuint64_t)nj, (cuuint64_t)ni, (cuuint64_t)nk};
-  const cuuint64_t strides[2] = {(cuuint64_t)nj * 4, (cuuint64_t)nj * ni * 4};
-  const cuuint32_t box[3] = {(cuuint32_t)kDtBoxJ, (cuuint32_t)kDtBoxI, 1};
-  const cuuint32_t es[3] = {1, 1, 1};
-  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
-}
-
-bool build_divdamp_maps(const View<float>& v, void* out) {
-  if (v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;
-  EncodeTiledFn fn = encode_tiled();
-  if (!fn) return false;
-  static std::once_flag attr;
-  std::call_once(attr, [] { cudaFuncSetAttribute(k_divdamp_tm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kDtSmem); });
-  DivdampMaps* dm = static_cast<DivdampMaps*>(out);
-  const int nj = v.nj, ni = v.ni, kz = v.kz;
-  const bool ok = map_div(fn, &dm->m[DM_U0], v.ubuf[0], nj, ni, kz) && map_div(fn, &dm->m[DM_U1], v.ubuf[1], nj, ni, kz) &&
-                  map_div(fn, &dm->m[DM_V0], v.vbuf[0], nj, ni, kz) && map_div(fn, &dm->m[DM_V1], v.vbuf[1], nj, ni, kz) &&
-                  map_div(fn, &dm->m[DM_RFW], v.rfw, nj, ni, kz) && map_div(fn, &dm->m[DM_RFS], v.rfs, nj, ni, kz) &&
-                  map_div(fn, &dm->m[DM_FMZ], v.fmz, nj, ni, kz);
-  return ok && cudaGetLastError() == cudaSuccess;
-}
-
-bool build_momentum_maps(const View<float>& v, void* out) {
-  if (v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;
-  EncodeTiledFn fn = encode_tiled();
-  if (!fn) return false;
-  static std::once_flag attr;
-  std::call_once(attr, [] { cudaFuncSetAttribute(k_momentum_tm<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, kMtSmem); });
-  MomentumMaps* mm = static_cast<MomentumMaps*>(out);
-  const int nj = v.nj, ni = v.ni, kz = v.kz;
-  const bool ok = map_mom(fn, &mm->m[MM_U0], v.ubuf[0], nj, ni, kz) && map_mom(fn, &mm->m[MM_U1], v.ubuf[1], nj, ni, kz) &&
-                  map_mom(fn, &mm->m[MM_V0], v.vbuf[0], nj, ni, kz) && map_mom(fn, &mm->m[MM_V1], v.vbuf[1], nj, ni, kz) &&
-                  map_mom(fn, &mm->m[MM_T0], v.fset[0][0], nj, ni, kz) &&
-                  map_mom(fn, &mm->m[MM_T1], v.fset[1][0], nj, ni, kz) &&
-                  map_mom(fn, &mm->m[MM_P0], v.fset[0][1], nj, ni, kz) &&
-                  map_mom(fn, &mm->m[MM_P1], v.fset[1][1], nj, ni, kz) &&
-                  map_mom(fn, &mm->m[MM_DW], v.deltaw, nj, ni, kz + 1);
-  return ok && cudaGetLastError() == cudaSuccess;
-}
 
 bool build_column_maps(const View<float>& v, void* out) {
   if (v.kz > kTmMaxKz || v.kz < 2 || v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;

@@ -27,13 +27,6 @@ namespace kfast {
 // jx not a multiple of 4) or the driver cannot encode them
 int column_maps_bytes();
 bool build_column_maps(const View<float>& v, void* out);
-// tensor maps of the staged momentum kernel (momentum_maps_bytes() bytes,
-// 64-byte aligned); false when jx is not a multiple of 4
-int momentum_maps_bytes();
-bool build_momentum_maps(const View<float>& v, void* out);
-// and of the staged divergence/damping kernel
-int divdamp_maps_bytes();
-bool build_divdamp_maps(const View<float>& v, void* out);
 template <class T> int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& cur, int& fcur);
 template <class T> int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur);
 }

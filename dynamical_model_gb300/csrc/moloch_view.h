@@ -126,10 +126,6 @@ struct View {
   // the two sets of TMA tensor maps (one per advected-field buffer set),
   // nullptr when the kernel cannot run on this domain
   const void* cmaps;
-  // the same for the staged momentum kernel (k_momentum_tm) and the staged
-  // divergence/damping kernel (k_divdamp_tm)
-  const void* mmaps;
-  const void* dmaps;
   // device word set by a bounded wait that gave up (MOLOCH_ERR_TIMEOUT)
   int* kerr;
   long long spin_cycles;  // limit of every such wait, in SM clock cycles
@@ -155,7 +151,7 @@ struct View {
 enum KernelKind {
   KK_PREDIAG = 0, KK_SOUND_DIV, KK_SOUND_DAMP, KK_SOUND_COLUMN, KK_LAP_FILTER, KK_PAI_UPDATE,
   KK_SOUND_MOMENTUM, KK_WAF_VERTICAL, KK_WAF_HORIZONTAL, KK_STAG_FROM_X,
-  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_SOUND_COLUMN_TM, KK_SOUND_MOMENTUM_TM, KK_SOUND_DIVDAMP_TM, KK_COUNT
+  KK_FILTER_INCREMENT, KK_POSTDIAG, KK_DIAG, KK_SOUND_DIVDAMP, KK_SOUND_COLUMN_TM, KK_COUNT
 };
 
 // Optional event recorder: when a launcher is given one, it records a CUDA
