@@ -105,6 +105,11 @@ _PROTOS = {
                                                     ctypes.POINTER(ctypes.c_double), ctypes.c_int]),
     "moloch_gpu_ensemble_set_tuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_ensemble_kernel_count": (ctypes.c_longlong, [ctypes.c_void_p]),
+    "moloch_gpu_ensemble_set_persistent": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "moloch_gpu_ensemble_persistent": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_ensemble_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int,
+                                                          ctypes.c_int]),
+    "moloch_gpu_ensemble_sync": (ctypes.c_int, [ctypes.c_void_p]),
     "moloch_gpu_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "moloch_tc_gemm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
@@ -398,8 +403,11 @@ class Moloch:
 
 
 class Ensemble:
-    """Members (Moloch handles on one stream) advanced together: one batched
-    launch per kernel over all members, one CUDA graph per ensemble step."""
+    """Members (Moloch handles on one stream) advanced together, one CUDA
+    graph per ensemble step: one batched launch per kernel over all members,
+    or (persistent mode) one cooperative launch per step whose blocks walk
+    the step's kernels as phases between grid barriers, taking (member,
+    tile) items from a device-side work queue."""
 
     def __init__(self, members):
         self.L = lib()
@@ -426,6 +434,24 @@ class Ensemble:
     @property
     def kernel_count(self):
         return self.L.moloch_gpu_ensemble_kernel_count(self.h)
+
+    def set_persistent(self, on=True):
+        _check(self.L.moloch_gpu_ensemble_set_persistent(self.h, int(bool(on))))
+
+    @property
+    def persistent(self):
+        return bool(self.L.moloch_gpu_ensemble_persistent(self.h))
+
+    def set_wait_limit(self, cycles=0, skip_block=-1, skip_barrier=-1):
+        """Limit of the persistent kernel's grid-barrier waits (SM cycles,
+        0: default); skip_block/skip_barrier make that block leave at that
+        barrier without arriving (test hook)."""
+        _check(self.L.moloch_gpu_ensemble_set_wait_limit(self.h, int(cycles), int(skip_block), int(skip_barrier)))
+
+    def sync(self):
+        """Wait for the stream; MolochError (MOLOCH_ERR_TIMEOUT) when a
+        barrier wait of the persistent kernel gave up."""
+        _check(self.L.moloch_gpu_ensemble_sync(self.h))
 
     def close(self):
         if getattr(self, "h", None):

@@ -1,8 +1,9 @@
 """Build libmoloch_gb300.so in-tree for sm_103a.
 
-Six translation units compiled in parallel:
+Translation units compiled in parallel:
   csrc/moloch_kernels_exact.cu  nvcc, FP64, --fmad=false (reference evaluation order)
   csrc/moloch_kernels_fast.cu   nvcc, FP64 + FP32, multiply-add contraction allowed
+  csrc/moloch_persist.cu        nvcc, the persistent ensemble kernel (contraction allowed)
   csrc/moloch_noalloc.cu        nvcc, FP64, --fmad=false (allocation-free WAF entry point)
   csrc/moloch_mlp.cu            nvcc, tcgen05 GEMM and the surrogate MLP kernels
   csrc/moloch_api.cpp           host C ABI, -ffp-contract=off
@@ -58,6 +59,7 @@ def build(force=False, verbose=False):
                      "-o", os.path.join(BUILD, "kexact.o")],
         nv_common + ["-c", os.path.join(CSRC, "moloch_kernels_fast.cu"),
                      "-o", os.path.join(BUILD, "kfast.o")],
+        nv_common + ["-c", os.path.join(CSRC, "moloch_persist.cu"), "-o", os.path.join(BUILD, "persist.o")],
         nv_common + ["--fmad=false", "-c", os.path.join(CSRC, "moloch_noalloc.cu"),
                      "-o", os.path.join(BUILD, "noalloc.o")],
         nv_common + ["-c", os.path.join(CSRC, "moloch_mlp.cu"), "-o", os.path.join(BUILD, "mlp.o")],
@@ -80,7 +82,7 @@ def build(force=False, verbose=False):
         raise RuntimeError("build failed:\n" + msg)
     tmp = LIB + ".tmp"
     link = [nvcc, ARCH, "-shared", "-o", tmp] + [os.path.join(BUILD, o) for o in
-                                                 ("kexact.o", "kfast.o", "noalloc.o", "mlp.o", "init.o", "api.o", "ideal.o")] + ["-lcudart", "-Xcompiler", "-pthread"]
+                                                 ("kexact.o", "kfast.o", "persist.o", "noalloc.o", "mlp.o", "init.o", "api.o", "ideal.o")] + ["-lcudart", "-Xcompiler", "-pthread"]
     r = subprocess.run(link, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + r.stdout.decode(errors="replace"))

@@ -25,6 +25,7 @@
 #include "../../include/moloch_gb300.h"
 #include "moloch_constants.h"
 #include "moloch_launch.h"
+#include "moloch_persist.h"
 #include "moloch_sur.h"
 #include "moloch_view.h"
 
@@ -1467,6 +1468,17 @@ struct moloch_ensemble {
   long long kernels = 0;
   int kernels_per_step = 0;
   PhaseFlags fl{};
+  // persistent mode: one cooperative launch per step walking a phase
+  // program (one per field-set parity at the step's start)
+  int persistent = 0;
+  const persist::Phase* prog[2] = {nullptr, nullptr};
+  int nphases = 0;
+  persist::Ctl* ctl = nullptr;
+  int* perr = nullptr;
+  int pgrid = 0;
+  size_t psmem = 0;
+  long long pspin = kDefaultSpinCycles;
+  int skip_block = -1, skip_barrier = -1;
 };
 
 namespace {
@@ -1500,6 +1512,13 @@ void ens_tiles(moloch_ensemble* e) {
     for (int z = 0; z < (kz + kKC - 1) / kKC; ++z)
       for (int y = 0; y < (ni + 7) / 8; ++y)
         for (int x = 0; x < tj; ++x) e->tiles[TK_CHUNK].push_back(make_int4(q, x, y, z));
+    // the persistent kernel's 32 x 8 blocks: column tiles 8 rows high
+    // (by = 2 by8 for the 32 x 4 column bodies), 8 strips per item
+    for (int y = 0; y < (ni + 7) / 8; ++y)
+      for (int x = 0; x < tj; ++x) e->tiles[TK_COLUMN8].push_back(make_int4(q, x, 2 * y, 0));
+    for (int y = 0; y < (ni + 7) / 8; ++y)
+      for (int x = 0; x < tj * (kNumAdvected / e->vfields); ++x)
+        e->tiles[TK_VERTICAL8].push_back(make_int4(q, x, 2 * y, 0));
     {
       const int nstrips = ((nj + kMomJ - 1) / kMomJ) * ((ni + kMomR - 1) / kMomR);
       for (int z = 0; z < kz; ++z)
@@ -1507,6 +1526,10 @@ void ens_tiles(moloch_ensemble* e) {
       const int ndstrips = ((nj + kDDJ - 1) / kDDJ) * ((ni + kDDR - 1) / kDDR);
       for (int z = 0; z < kz; ++z)
         for (int x = 0; x < (ndstrips + 3) / 4; ++x) e->tiles[TK_DSTRIP].push_back(make_int4(q, x, z, 0));
+      for (int z = 0; z < kz; ++z)
+        for (int x = 0; x < (nstrips + 7) / 8; ++x) e->tiles[TK_MSTRIP8].push_back(make_int4(q, x, z, 0));
+      for (int z = 0; z < kz; ++z)
+        for (int x = 0; x < (ndstrips + 7) / 8; ++x) e->tiles[TK_DSTRIP8].push_back(make_int4(q, x, z, 0));
     }
     if (e->hz_levels >= 16) {  // warp strips: 4 strips of hz_levels rows per block, every level
       const int nstrips = ((nj + 27) / 28) * ((ni + e->hz_levels - 1) / e->hz_levels);
@@ -1527,9 +1550,15 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
   const int n = (int)e->m.size();
   size_t bytes = 4 * n * sizeof(View<T>);
   for (int t = 0; t < TK_COUNT; ++t) bytes += ((e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255));
+  // persistent mode: two phase programs, the barrier/queue words, the error word
+  const size_t prog_bytes = ((sizeof(persist::Phase) * persist::kMaxPhases + 255) & ~size_t(255));
+  const size_t pbytes = 2 * prog_bytes + ((sizeof(persist::Ctl) + 255) & ~size_t(255)) + 256;
   if (e->dev) cudaFree(e->dev);
   e->dev = nullptr;
-  CUDA_TRY(cudaMalloc(&e->dev, bytes + 1024));
+  e->prog[0] = e->prog[1] = nullptr;
+  e->ctl = nullptr;
+  e->perr = nullptr;
+  CUDA_TRY(cudaMalloc(&e->dev, bytes + pbytes + 1024));
   std::vector<View<T>> hv(4 * (size_t)n);
   for (int cur = 0; cur < 2; ++cur)
     for (int fc = 0; fc < 2; ++fc)
@@ -1556,6 +1585,30 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     b.vfields = e->vfields;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
+  // persistent-mode programs (empty when the tuning has a variant the
+  // persistent kernel does not carry)
+  e->nphases = 0;
+  for (int f = 0; f < 2; ++f) {
+    std::vector<persist::Phase> prog;
+    const int prc = persist::program<T>(b, e->fl, f, prog);
+    if (prc == 0) {
+      CUDA_TRY(cudaMemcpy(p + off, prog.data(), prog.size() * sizeof(persist::Phase), cudaMemcpyHostToDevice));
+      e->prog[f] = (const persist::Phase*)(p + off);
+      e->nphases = (int)prog.size();
+    }
+    off += prog_bytes;
+  }
+  e->ctl = (persist::Ctl*)(p + off);
+  off += (sizeof(persist::Ctl) + 255) & ~size_t(255);
+  e->perr = (int*)(p + off);
+  CUDA_TRY(cudaMemset(e->perr, 0, sizeof(int)));
+  if (!e->pgrid) {
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    e->pgrid = persist::blocks_per_sm<T>(&e->psmem) * sms;
+  }
+  if (e->persistent && (!e->nphases || !e->pgrid)) e->persistent = 0;
   return MOLOCH_OK;
 }
 
@@ -1565,7 +1618,28 @@ int ens_build(moloch_ensemble* e) {
   return e->elem == 8 ? ens_upload(e, e->bd, &moloch_handle::vd) : ens_upload(e, e->bf, &moloch_handle::vf);
 }
 
+template <class T>
+int ens_step_persistent(moloch_ensemble* e, const Batch<T>& b) {
+  persist::Args<T> a;
+  a.views = b.views[0][0];  // the four parities follow one another, n views each
+  a.nmembers = (int)e->m.size();
+  a.prog = e->prog[e->fcur];
+  a.nphases = e->nphases;
+  a.ctl = e->ctl;
+  a.err = e->perr;
+  a.spin = e->pspin;
+  a.skip_block = e->skip_block;
+  a.skip_barrier = e->skip_barrier;
+  cudaMemsetAsync(e->ctl, 0, persist::ctl_bytes(e->nphases), e->stream);
+  persist::launch<T>(a, e->pgrid, e->psmem, e->stream);
+  e->fcur ^= (e->fl.nadv & 1);
+  e->cur = 0;
+  return 1;
+}
+
 int ens_step_kernels(moloch_ensemble* e) {
+  if (e->persistent)
+    return e->elem == 8 ? ens_step_persistent(e, e->bd) : ens_step_persistent(e, e->bf);
   return e->elem == 8 ? kfast::blaunch_step(e->bd, e->stream, e->fl, e->cur, e->fcur)
                       : kfast::blaunch_step(e->bf, e->stream, e->fl, e->cur, e->fcur);
 }
@@ -1731,6 +1805,42 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
     if (tot < best2) { best2 = tot; pick2 = cand; }
   }
   e->vfields = pick2;
+  // one cooperative launch per step (the persistent kernel) against one
+  // launch per kernel, timed on whole steps, when the persistent kernel
+  // carries the chosen variants
+  const bool pok = e->elem == 8 ? persist::supports<double>(e->hz_levels, e->kmarch, e->vfields)
+                                : persist::supports<float>(e->hz_levels, e->kmarch, e->vfields);
+  double tmode[2] = {0.0, 1e30};
+  for (int mode = 0; mode < (pok ? 2 : 1); ++mode) {
+    e->persistent = mode;
+    int rc = ens_build(e);
+    if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+    if (mode && !e->persistent) break;  // no resident blocks: stays off
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, e->stream);
+      e->kernels += ens_step_kernels(e);
+      cudaEventRecord(e1, e->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "ensemble autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    tmode[mode] = tot;
+  }
+  if (pok && e->perr) {
+    int v = 0;
+    CUDA_TRY(cudaMemcpy(&v, e->perr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) {
+      CUDA_TRY(cudaMemset(e->perr, 0, sizeof(int)));
+      cudaEventDestroy(e0); cudaEventDestroy(e1);
+      e->persistent = 0;
+      return fail(MOLOCH_ERR_TIMEOUT, "ensemble autotune: a grid-barrier wait of the persistent kernel gave up");
+    }
+  }
+  e->persistent = (pok && tmode[1] < tmode[0]) ? 1 : 0;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   choice[0] = pick;
@@ -1760,6 +1870,56 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
 }
 
 long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e) { return e ? e->kernels : -1; }
+
+int moloch_gpu_ensemble_set_persistent(moloch_ensemble_t* e, int on) {
+  g_err.clear();
+  if (!e) return fail(MOLOCH_ERR_ARG, "null ensemble");
+  if (on) {
+    const bool ok = e->elem == 8 ? persist::supports<double>(e->hz_levels, e->kmarch, e->vfields)
+                                 : persist::supports<float>(e->hz_levels, e->kmarch, e->vfields);
+    if (!ok)
+      return fail(MOLOCH_ERR_ARG,
+                  "the persistent kernel does not carry this tuning (hz_levels %d, kmarch %d, vfields %d): "
+                  "horizontal WAF tiles (1-8 levels), 1 or 2 vertical fields per thread, no %s",
+                  e->hz_levels, e->kmarch, e->vfields,
+                  e->elem == 8 ? "fused divergence/damping strips" : "k-marching momentum");
+  }
+  e->persistent = on ? 1 : 0;
+  int rc = ens_build(e);
+  if (rc) return rc;
+  if (on && !e->persistent) return fail(MOLOCH_ERR_CUDA, "persistent kernel: no resident blocks or no program");
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_ensemble_persistent(moloch_ensemble_t* e) { return e ? e->persistent : -1; }
+
+int moloch_gpu_ensemble_set_wait_limit(moloch_ensemble_t* e, long long cycles, int skip_block, int skip_barrier) {
+  g_err.clear();
+  if (!e) return fail(MOLOCH_ERR_ARG, "null ensemble");
+  e->pspin = cycles > 0 ? cycles : kDefaultSpinCycles;
+  e->skip_block = skip_block;
+  e->skip_barrier = skip_barrier;
+  ens_drop_graphs(e);  // the launch arguments are baked into captured graphs
+  return MOLOCH_OK;
+}
+
+int moloch_gpu_ensemble_sync(moloch_ensemble_t* e) {
+  g_err.clear();
+  if (!e) return fail(MOLOCH_ERR_ARG, "null ensemble");
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  int rc = check_launch("ensemble");
+  if (rc) return rc;
+  if (e->perr) {
+    int v = 0;
+    CUDA_TRY(cudaMemcpy(&v, e->perr, sizeof(int), cudaMemcpyDeviceToHost));
+    if (v) {
+      CUDA_TRY(cudaMemset(e->perr, 0, sizeof(int)));
+      return fail(MOLOCH_ERR_TIMEOUT, "a grid-barrier wait of the persistent ensemble kernel gave up; "
+                                      "the steps since the last sync did not complete");
+    }
+  }
+  return MOLOCH_OK;
+}
 
 int moloch_gpu_ensemble_destroy(moloch_ensemble_t* e) {
   if (!e) return MOLOCH_OK;

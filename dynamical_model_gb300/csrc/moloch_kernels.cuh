@@ -61,6 +61,17 @@ __device__ __forceinline__ int wm1(int x, int n) { return x == 0 ? n - 1 : x - 1
 __device__ __forceinline__ int wp1(int x, int n) { return x == n - 1 ? 0 : x + 1; }
 __device__ __forceinline__ int wm2(int x, int n) { int y = x - 2; return y < 0 ? y + n : y; }
 __device__ __forceinline__ int wp2(int x, int n) { int y = x + 2; return y >= n ? y - n : y; }
+
+// a*b - c*d and a*b + c*d with the multiply-add contraction fixed in FP32
+// storage: left to the compiler either product may be fused, and which one
+// it fuses depends on the code around the expression, so the same body in
+// two kernels (k_sound_column and k_sound_column_tm; a batched kernel and
+// the persistent ensemble kernel) could round differently.  FP64 keeps the
+// expression as written (the exact build contracts nothing).
+__device__ __forceinline__ float prod_sub(float a, float b, float c, float d) { return __fmaf_rn(a, b, -__fmul_rn(c, d)); }
+__device__ __forceinline__ double prod_sub(double a, double b, double c, double d) { return a * b - c * d; }
+__device__ __forceinline__ float prod_add(float a, float b, float c, float d) { return __fmaf_rn(c, d, __fmul_rn(a, b)); }
+__device__ __forceinline__ double prod_add(double a, double b, double c, double d) { return a * b + c * d; }
 __device__ __forceinline__ int wrapn(int x, int n) { int y = x % n; return y < 0 ? y + n : y; }
 // periodic index for -n <= x < 2n (no integer division)
 __device__ __forceinline__ int wrap2(int x, int n) { return x < 0 ? x + n : (x >= n ? x - n : x); }
@@ -174,8 +185,8 @@ __device__ __forceinline__ void b_sound_div(const View<T>& d, const int bx, cons
   const T hx0 = d.hx[c], hx1 = d.hx[ce], hy0 = d.hy[c], hy1 = d.hy[cn];
   if (kk > 0) {  // s(k), k = 2..kz  (:557-570)
     const T u0p = u[c + o - pl], u1p = u[ce + o - pl], v0p = v[c + o - pl], v1p = v[cn + o - pl];
-    T zuh = (u0 + u0p) * hx0 + (u1 + u1p) * hx1;
-    T zvh = (v0 + v0p) * hy0 + (v1 + v1p) * hy1;
+    T zuh = prod_add(u0 + u0p, hx0, u1 + u1p, hx1);
+    T zvh = prod_add(v0 + v0p, hy0, v1 + v1p, hy1);
     d.s[c + o] = -((T(0.25) * (zuh + zvh)) * d.gzitak[kk]);
   }
   const T dtrdx = d.dtrdx, dtrdy = d.dtrdy;
@@ -183,27 +194,25 @@ __device__ __forceinline__ void b_sound_div(const View<T>& d, const int bx, cons
   const T zrfmzum = d.rfw[c + o], zrfmzup = d.rfw[ce + o];
   const T zrfmzvm = d.rfs[c + o], zrfmzvp = d.rfs[cn + o];
   const T rmv0 = d.rmv[c], rmv1 = d.rmv[cn];
+  // zum = (dtrdx u0) zrfmzum etc.; zup - zum and zvp - zvm with the
+  // contraction fixed
   if (d.rotllr) {
-    const T zum = (dtrdx * u0) * zrfmzum;
-    const T zup = (dtrdx * u1) * zrfmzup;
-    const T zvm = ((dtrdy * v0) * zrfmzvm) * rmv0;
-    const T zvp = ((dtrdy * v1) * zrfmzvp) * rmv1;
-    d.zdiv2a[c + o] = (f * d.mx[c]) * ((zup - zum) + (zvp - zvm));
+    const T du = prod_sub(dtrdx * u1, zrfmzup, dtrdx * u0, zrfmzum);
+    const T dv = prod_sub((dtrdy * v1) * zrfmzvp, rmv1, (dtrdy * v0) * zrfmzvm, rmv0);
+    d.zdiv2a[c + o] = (f * d.mx[c]) * (du + dv);
   } else {
     const T rmu0 = d.rmu[c], rmu1 = d.rmu[ce];
-    const T zum = ((dtrdx * u0) * rmu0) * zrfmzum;
-    const T zup = ((dtrdx * u1) * rmu1) * zrfmzup;
-    const T zvm = ((dtrdy * v0) * rmv0) * zrfmzvm;
-    const T zvp = ((dtrdy * v1) * rmv1) * zrfmzvp;
-    d.zdiv2a[c + o] = (d.mx2[c] * f) * ((zup - zum) + (zvp - zvm));
+    const T du = prod_sub((dtrdx * u1) * rmu1, zrfmzup, (dtrdx * u0) * rmu0, zrfmzum);
+    const T dv = prod_sub((dtrdy * v1) * rmv1, zrfmzvp, (dtrdy * v0) * rmv0, zrfmzvm);
+    d.zdiv2a[c + o] = (d.mx2[c] * f) * (du + dv);
   }
   if (jj == 0) d.eu_j[ii + (size_t)ni * kk] = u0;
   if (ii == ni - 1) d.eu_i[jj + (size_t)nj * kk] = u0;
   if (jj == nj - 1) d.ev_j[ii + (size_t)ni * kk] = v0;
   if (ii == 0) d.ev_i[jj + (size_t)nj * kk] = v0;
   if (kk == kz - 1) {  // surface w(kz+1), s(kz+1)
-    T zuh = u0 * hx0 + u1 * hx1;
-    T zvh = v0 * hy0 + v1 * hy1;
+    T zuh = prod_add(u0, hx0, u1, hx1);
+    T zvh = prod_add(v0, hy0, v1, hy1);
     T ws = T(0.5) * (zuh + zvh);
     d.w[c + (size_t)kz * pl] = ws;
     d.s[c + (size_t)kz * pl] = -ws;
@@ -254,7 +263,7 @@ __device__ __forceinline__ void b_sound_damp(const View<T>& d, const int bx, con
     v[c + o] = v[c + o] + cd * (zc - zs);
   else
     v[c + o] = v[c + o] + ((cd * d.mv[c]) * (zc - zs));
-  const T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
+  const T p2d = prod_sub(T(0.125), ((zw + ze) + zs) + zn, T(0.5), zc);
   T zd = zc + d.ddamp2 * p2d;
   zd = zd + (d.fmz[c + o] * d.dtrdz) * (d.s[c + o] - d.s[c + o + pl]);
   d.zdiv2b[c + o] = zd;
@@ -303,15 +312,6 @@ __device__ __forceinline__ float narrow_trunc(double x) {
   return __uint_as_float(m | (hi & 0x80000000u));
 }
 
-// a*b - c*d and a*b + c*d with the multiply-add contraction fixed in FP32
-// storage: left to the compiler either product may be fused, and two
-// kernels doing the same arithmetic (k_sound_column, k_sound_column_tm)
-// could round differently.  FP64 keeps the expression as written (the
-// exact build contracts nothing).
-__device__ __forceinline__ float prod_sub(float a, float b, float c, float d) { return __fmaf_rn(a, b, -__fmul_rn(c, d)); }
-__device__ __forceinline__ double prod_sub(double a, double b, double c, double d) { return a * b - c * d; }
-__device__ __forceinline__ float prod_add(float a, float b, float c, float d) { return __fmaf_rn(c, d, __fmul_rn(a, b)); }
-__device__ __forceinline__ double prod_add(double a, double b, double c, double d) { return a * b + c * d; }
 
 // Quotient of the Exner/theta update in FP32 storage: the reciprocal
 // estimate q = a * rcp(b) with one residual correction q + (a - b q) rcp(b)
@@ -587,7 +587,7 @@ __device__ __forceinline__ void b_lap_filter(const View<T>& d, const int bx, con
   T aw = a[o + wm1(jj, nj) + (size_t)nj * ii], ae = a[o + wp1(jj, nj) + (size_t)nj * ii];
   T as = a[o + jj + (size_t)nj * wm1(ii, ni)], an = a[o + jj + (size_t)nj * wp1(ii, ni)];
   T ac = a[o + c];
-  T p2d = T(0.125) * (((aw + ae) + as) + an) - T(0.5) * ac;
+  T p2d = prod_sub(T(0.125), ((aw + ae) + as) + an, T(0.5), ac);
   const T coef = d.anu2 * d.xknu[bz];
   out[o + c] = ac + coef * p2d;
 }
@@ -659,7 +659,7 @@ __device__ __forceinline__ void b_filter_increment(const View<T>& d, const int b
   };
   T xw = X(wm1(jj, nj), ii), xe = X(wp1(jj, nj), ii), xs = X(jj, wm1(ii, ni)), xn = X(jj, wp1(ii, ni));
   T xc = X(jj, ii);
-  T p2d = T(0.125) * (((xw + xe) + xs) + xn) - T(0.5) * xc;
+  T p2d = prod_sub(T(0.125), ((xw + xe) + xs) + xn, T(0.5), xc);
   const size_t c = o + jj + (size_t)nj * ii;
   out[c] = (xc + T(kNupaitq) * p2d) + ref[c];
 }
@@ -799,31 +799,27 @@ __device__ __forceinline__ void b_sound_div_km(const View<T>& d, const int bx, c
     const size_t o = (size_t)kk * pl;
     const T u0 = cur.u0, u1 = cur.u1, v0 = cur.v0, v1 = cur.v1;
     if (kk > 0) {  // s(k), k = 2..kz  (:557-570)
-      T zuh = (u0 + u0p) * hx0 + (u1 + u1p) * hx1;
-      T zvh = (v0 + v0p) * hy0 + (v1 + v1p) * hy1;
+      T zuh = prod_add(u0 + u0p, hx0, u1 + u1p, hx1);
+      T zvh = prod_add(v0 + v0p, hy0, v1 + v1p, hy1);
       d.s[c + o] = -((T(0.25) * (zuh + zvh)) * cur.gz);
     }
     const T f = cur.f;
     if (rot) {
-      const T zum = (dtrdx * u0) * cur.rfw0;
-      const T zup = (dtrdx * u1) * cur.rfw1;
-      const T zvm = ((dtrdy * v0) * cur.rfs0) * rmv0;
-      const T zvp = ((dtrdy * v1) * cur.rfs1) * rmv1;
-      d.zdiv2a[c + o] = (f * mxc) * ((zup - zum) + (zvp - zvm));
+      const T du = prod_sub(dtrdx * u1, cur.rfw1, dtrdx * u0, cur.rfw0);
+      const T dv = prod_sub((dtrdy * v1) * cur.rfs1, rmv1, (dtrdy * v0) * cur.rfs0, rmv0);
+      d.zdiv2a[c + o] = (f * mxc) * (du + dv);
     } else {
-      const T zum = ((dtrdx * u0) * rmu0) * cur.rfw0;
-      const T zup = ((dtrdx * u1) * rmu1) * cur.rfw1;
-      const T zvm = ((dtrdy * v0) * rmv0) * cur.rfs0;
-      const T zvp = ((dtrdy * v1) * rmv1) * cur.rfs1;
-      d.zdiv2a[c + o] = (mxc * f) * ((zup - zum) + (zvp - zvm));
+      const T du = prod_sub((dtrdx * u1) * rmu1, cur.rfw1, (dtrdx * u0) * rmu0, cur.rfw0);
+      const T dv = prod_sub((dtrdy * v1) * rmv1, cur.rfs1, (dtrdy * v0) * rmv0, cur.rfs0);
+      d.zdiv2a[c + o] = (mxc * f) * (du + dv);
     }
     if (jj == 0) d.eu_j[ii + (size_t)ni * kk] = u0;
     if (ii == ni - 1) d.eu_i[jj + (size_t)nj * kk] = u0;
     if (jj == nj - 1) d.ev_j[ii + (size_t)ni * kk] = v0;
     if (ii == 0) d.ev_i[jj + (size_t)nj * kk] = v0;
     if (kk == kz - 1) {  // surface w(kz+1), s(kz+1)
-      T zuh = u0 * hx0 + u1 * hx1;
-      T zvh = v0 * hy0 + v1 * hy1;
+      T zuh = prod_add(u0, hx0, u1, hx1);
+      T zvh = prod_add(v0, hy0, v1, hy1);
       T ws = T(0.5) * (zuh + zvh);
       d.w[c + (size_t)kz * pl] = ws;
       d.s[c + (size_t)kz * pl] = -ws;
@@ -872,7 +868,7 @@ __device__ __forceinline__ void b_sound_damp_km(const View<T>& d, const int bx, 
       v[c + o] = cur.vc + cd * (zc - zs);
     else
       v[c + o] = cur.vc + ((cd * mvc) * (zc - zs));
-    const T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
+    const T p2d = prod_sub(T(0.125), ((zw + ze) + zs) + zn, T(0.5), zc);
     T zd = zc + ddamp2 * p2d;
     zd = zd + (cur.fz * dtrdz) * (s_k - cur.s1);
     d.zdiv2b[c + o] = zd;
@@ -997,16 +993,19 @@ __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_gr
 // and rows, as in k_sound_momentum.
 constexpr int kMomS = 6;  // row slots: rows i-1, i, i+1 and three in flight
 template <class T>
-using MomRing = T[4][kMomS][6][32];  // [warp][slot][array][lane]
+using MomSlots = T[kMomS][6][32];  // one warp's ring: [slot][array][lane]
+template <class T>
+using MomRing = MomSlots<T>[4];    // [warp] of a 128-thread block
 
+// bx: block of nw strips, wid: this warp's strip in it, rg: its ring
 template <class T>
 __device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx, const int k, const int R,
-                                                 MomRing<T>& ring) {
+                                                 MomSlots<T>& rg, const int wid, const int nw) {
   if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int nj = d.nj, ni = d.ni, pl = d.pl;
   const int nsj = (nj + kMomJ - 1) / kMomJ, nsi = (ni + R - 1) / R;
-  const int w = bx * (blockDim.x >> 5) + wid;
+  const int w = bx * nw + wid;
   if (w >= nsj * nsi) return;  // whole warp
   const int sj = w % nsj, si = w / nsj;
   const int jl = sj * kMomJ - 1 + lane;
@@ -1027,7 +1026,6 @@ __device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx,
   const T gzh = d.gzitakh[k];
   const bool rot = d.rotllr;
   const int jm = wm1(jj, nj), jp = wp1(jj, nj);
-  T(*const rg)[6][32] = ring[wid];
   // rows i_s-1 .. i_e stream through the slots in order; the slot indices
   // rotate by one per row
   auto nxt = [](int q) { return q + 1 == kMomS ? 0 : q + 1; };
@@ -1133,7 +1131,7 @@ __device__ __forceinline__ void b_momentum_strip(const View<T>& d, const int bx,
 template <class T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 4) k_momentum_strip(View<T> d, int R) {
   __shared__ __align__(16) MomRing<T> ring;
-  b_momentum_strip<T>(d, blockIdx.x, blockIdx.y, R, ring);
+  b_momentum_strip<T>(d, blockIdx.x, blockIdx.y, R, ring[threadIdx.x >> 5], threadIdx.x >> 5, 4);
 }
 
 template <class T>
@@ -1144,7 +1142,7 @@ __global__ void __launch_bounds__(128)
   const int4 t = tiles[blockIdx.x];
   copy_view(&sv, views + t.x);
   __syncthreads();
-  b_momentum_strip<T>(sv, t.y, t.z, R, ring);
+  b_momentum_strip<T>(sv, t.y, t.z, R, ring[threadIdx.x >> 5], threadIdx.x >> 5, 4);
 }
 
 // ---- divergence + divdamp as warp strips (:514-597, :853-895, :627-630) ---
@@ -1162,13 +1160,14 @@ __global__ void __launch_bounds__(128)
 // lanes and rows store the pre-damping edge values the momentum step reads
 // as the stale ud/vd halo (:730-735), as k_sound_div does.
 template <class T>
-__device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, const int k, const int R) {
+__device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, const int k, const int R,
+                                                const int wid, const int nw) {
   if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
   const size_t pl = d.pl;
   const int nsj = (nj + kDDJ - 1) / kDDJ, nsi = (ni + R - 1) / R;
-  const int w = bx * (blockDim.x >> 5) + wid;
+  const int w = bx * nw + wid;
   if (w >= nsj * nsi) return;  // whole warp
   const int sj = w % nsj, si = w / nsj;
   const int jl = sj * kDDJ - 1 + lane;
@@ -1221,35 +1220,31 @@ __device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, 
     const T rmu_e = __shfl_down_sync(0xffffffffu, a.rmu, 1);
     Zr r;
     if (has_up) {
-      const T zuh = (a.uk + a.um) * a.hx + (uk_e + um_e) * hx_e;
-      const T zvh = (b.vk + b.vm) * b.hy + (bn.vk + bn.vm) * bn.hy;
+      const T zuh = prod_add(a.uk + a.um, a.hx, uk_e + um_e, hx_e);
+      const T zvh = prod_add(b.vk + b.vm, b.hy, bn.vk + bn.vm, bn.hy);
       r.sk = -((T(0.25) * (zuh + zvh)) * gzk);
     } else {
       r.sk = a.s0;
     }
     if (has_dn) {
-      const T zuh = (a.up + a.uk) * a.hx + (up_e + uk_e) * hx_e;
-      const T zvh = (b.vp + b.vk) * b.hy + (bn.vp + bn.vk) * bn.hy;
+      const T zuh = prod_add(a.up + a.uk, a.hx, up_e + uk_e, hx_e);
+      const T zvh = prod_add(b.vp + b.vk, b.hy, bn.vp + bn.vk, bn.hy);
       r.sk1 = -((T(0.25) * (zuh + zvh)) * gzk1);
       r.ws = T(0);
     } else {  // surface w(kz+1) and s(kz+1) (:536-549)
-      const T zuh = a.uk * a.hx + uk_e * hx_e;
-      const T zvh = b.vk * b.hy + bn.vk * bn.hy;
+      const T zuh = prod_add(a.uk, a.hx, uk_e, hx_e);
+      const T zvh = prod_add(b.vk, b.hy, bn.vk, bn.hy);
       r.ws = T(0.5) * (zuh + zvh);
       r.sk1 = -r.ws;
     }
     if (rot) {
-      const T zum = (dtrdx * a.uk) * a.rfw;
-      const T zup = (dtrdx * uk_e) * rfw_e;
-      const T zvm = ((dtrdy * b.vk) * b.rfs) * b.rmv;
-      const T zvp = ((dtrdy * bn.vk) * bn.rfs) * bn.rmv;
-      r.z = (a.fmz * a.mx) * ((zup - zum) + (zvp - zvm));
+      const T du = prod_sub(dtrdx * uk_e, rfw_e, dtrdx * a.uk, a.rfw);
+      const T dv = prod_sub((dtrdy * bn.vk) * bn.rfs, bn.rmv, (dtrdy * b.vk) * b.rfs, b.rmv);
+      r.z = (a.fmz * a.mx) * (du + dv);
     } else {
-      const T zum = ((dtrdx * a.uk) * a.rmu) * a.rfw;
-      const T zup = ((dtrdx * uk_e) * rmu_e) * rfw_e;
-      const T zvm = ((dtrdy * b.vk) * b.rmv) * b.rfs;
-      const T zvp = ((dtrdy * bn.vk) * bn.rmv) * bn.rfs;
-      r.z = (a.mx * a.fmz) * ((zup - zum) + (zvp - zvm));
+      const T du = prod_sub((dtrdx * uk_e) * rmu_e, rfw_e, (dtrdx * a.uk) * a.rmu, a.rfw);
+      const T dv = prod_sub((dtrdy * bn.vk) * bn.rmv, bn.rfs, (dtrdy * b.vk) * b.rmv, b.rfs);
+      r.z = (a.mx * a.fmz) * (du + dv);
     }
     return r;
   };
@@ -1293,7 +1288,7 @@ __device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, 
         vo[c] = v0 + cd * (zc - zs);
       else
         vo[c] = v0 + ((cd * ucur.mv) * (zc - zs));
-      const T p2d = T(0.125) * (((zw + ze) + zs) + zn) - T(0.5) * zc;
+      const T p2d = prod_sub(T(0.125), ((zw + ze) + zs) + zn, T(0.5), zc);
       T zd = zc + ddamp2 * p2d;
       zd = zd + (ucur.fmz * dtrdz) * (zcur.sk - zcur.sk1);
       d.zdiv2b[o + c] = zd;
@@ -1310,7 +1305,7 @@ __device__ __forceinline__ void b_divdamp_strip(const View<T>& d, const int bx, 
 // 2.74 against 2.56 ms per step)
 template <class T>
 __global__ void __launch_bounds__(128) k_divdamp_strip(View<T> d, int R) {
-  b_divdamp_strip<T>(d, blockIdx.x, blockIdx.y, R);
+  b_divdamp_strip<T>(d, blockIdx.x, blockIdx.y, R, threadIdx.x >> 5, 4);
 }
 
 template <class T>
@@ -1320,7 +1315,7 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3)
   const int4 t = tiles[blockIdx.x];
   copy_view(&sv, views + t.x);
   __syncthreads();
-  b_divdamp_strip<T>(sv, t.y, t.z, R);
+  b_divdamp_strip<T>(sv, t.y, t.z, R, threadIdx.x >> 5, 4);
 }
 
 // ---- advection: vertical WAF, two passes at dt/2 (:966-1073) ------------

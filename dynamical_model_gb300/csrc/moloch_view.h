@@ -176,11 +176,18 @@ struct KernelTimer {
 // TK_CHUNK tiles cover kKC levels each (the k-marching sound kernels);
 // TK_MSTRIP tiles are blocks of 4 momentum warp strips (30 columns x kMomR
 // rows) of one level; TK_DSTRIP tiles blocks of 4 divergence/damping warp
-// strips (29 columns x kDDR rows)
+// strips (29 columns x kDDR rows).  The persistent ensemble kernel runs
+// 32 x 8 thread blocks: its column tiles (TK_COLUMN8, TK_VERTICAL8) are 8
+// rows high, given as (member, bx, 2 by8, .) so that the 32 x 4 column
+// bodies' row index by * 4 + threadIdx.y covers rows 8 by8 .. 8 by8 + 7, and
+// its strip tiles (TK_MSTRIP8, TK_DSTRIP8) are blocks of 8 warp strips.
 constexpr int kKC = 4;
 constexpr int kMomJ = 30, kMomR = 32;
 constexpr int kDDJ = 29, kDDR = 32;
-enum TileKind { TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_DSTRIP, TK_COUNT };
+enum TileKind {
+  TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_DSTRIP,
+  TK_COLUMN8, TK_VERTICAL8, TK_MSTRIP8, TK_DSTRIP8, TK_COUNT
+};
 template <class T>
 struct Batch {
   const View<T>* views[2][2];   // device arrays, one view per member

@@ -261,10 +261,18 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int nc
 int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int nchoice);
 
 /* ---- ensembles --------------------------------------------------------------
- * Many domains of uneven size (jx, iy, kz may all differ) advanced together:
- * each kernel of the step is ONE launch whose 1-D grid walks a table of
- * (member, tile) entries over all members, heaviest column tiles first, and
- * one step of the whole ensemble is one CUDA graph.  Members are ordinary
+ * Many domains of uneven size (jx, iy, kz may all differ) advanced together,
+ * one step of the whole ensemble as one CUDA graph, in one of two modes:
+ *   - per kernel: each kernel of the step is ONE launch whose 1-D grid walks
+ *     a table of (member, tile) entries over all members, heaviest column
+ *     tiles first;
+ *   - persistent (moloch_gpu_ensemble_set_persistent): the whole step is ONE
+ *     cooperative launch of as many blocks as fit on the GPU at once, walking
+ *     the kernels of the step as phases separated by grid barriers; within a
+ *     phase blocks take (member, tile) items from a device-side work queue.
+ *     Same kernel bodies, so the same results as the per-kernel mode.
+ *     Barrier waits are bounded (moloch_gpu_ensemble_set_wait_limit); one that
+ *     gives up abandons the step, and moloch_gpu_ensemble_sync reports it.  Members are ordinary
  * handles created by the caller on the same stream with the same mode,
  * mo_nadv, mo_nsound and filter switches (the theta/pai filters are not
  * supported in ensembles), each initialized (setup_idealized or uploads +
@@ -280,6 +288,24 @@ int moloch_gpu_ensemble_run(moloch_ensemble_t* e, int nsteps, int use_graph);
 int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best_ms, int nchoice);
 int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int nchoice);
 long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);
+/* persistent mode on (1) or off (0).  It carries the horizontal WAF as tiles
+ * (choice[0] 1..8), 1 or 2 vertical-WAF fields per thread, and in FP32 no
+ * k-marching momentum (choice[1] bit 4 without 8), in FP64 no fused
+ * divergence/damping strips (bit 16); other tunings give MOLOCH_ERR_ARG.
+ * moloch_gpu_ensemble_autotune times both modes on whole steps and keeps the
+ * faster; moloch_gpu_ensemble_persistent returns the mode in use. */
+int moloch_gpu_ensemble_set_persistent(moloch_ensemble_t* e, int on);
+int moloch_gpu_ensemble_persistent(moloch_ensemble_t* e);
+/* Limit of every grid-barrier wait of the persistent kernel, in SM clock
+ * cycles (<= 0: the default 2e9, about one second).  skip_block/skip_barrier
+ * (-1: off) are a test hook: that block leaves the launch at that barrier
+ * without arriving, so the other blocks' waits run out. */
+int moloch_gpu_ensemble_set_wait_limit(moloch_ensemble_t* e, long long cycles, int skip_block, int skip_barrier);
+/* Block until the ensemble's stream is idle.  MOLOCH_ERR_TIMEOUT when a
+ * barrier wait of the persistent kernel gave up since the last sync (those
+ * steps, and the ones after them up to this call, did not complete; the
+ * flag is cleared, so later steps run again). */
+int moloch_gpu_ensemble_sync(moloch_ensemble_t* e);
 int moloch_gpu_ensemble_destroy(moloch_ensemble_t* e);
 
 /* ---- tensor-core GEMM (tcgen05) used by the acoustic-cycle surrogate --------

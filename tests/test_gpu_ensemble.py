@@ -92,3 +92,89 @@ def test_ensemble_strip_shape_matches_members(gpu_lib, stream, tuning):
     e.close()
     for m in ms + solo:
         m.close()
+
+
+# ---- persistent mode: one cooperative launch per ensemble step ------------
+# FP32: default shapes; horizontal tiles of 2 levels with the fused
+# divergence/damping and momentum strips and 2 vertical fields per thread;
+# the k-marching divergence and damping.  FP64: default; k-marching
+# divergence, damping and momentum with 8-level horizontal tiles.
+PERSIST_CASES = [("fp32_mixed", [4, 0, 1]), ("fp32_mixed", [2, 24, 2]), ("fp32_mixed", [8, 3, 1]),
+                 ("fp64", [4, 0, 1]), ("fp64", [8, 7, 1])]
+
+
+@pytest.mark.parametrize("mode,tuning", PERSIST_CASES)
+@pytest.mark.parametrize("graph", [False, True])
+def test_persistent_matches_per_kernel(gpu_lib, stream, mode, tuning, graph):
+    """The persistent kernel runs the per-kernel launches' bodies in the
+    same order on the same tiles (column tiles 8 rows high, 8 strips per
+    item), so the two modes agree bit for bit."""
+    per_kernel = members(gpu_lib, mode, stream=stream.cuda_stream)
+    pers = members(gpu_lib, mode, stream=stream.cuda_stream)
+    e0 = gpu_lib.Ensemble(per_kernel)
+    e0.set_tuning(tuning)
+    e1 = gpu_lib.Ensemble(pers)
+    e1.set_tuning(tuning)
+    e1.set_persistent(True)
+    assert e1.persistent and not e0.persistent
+    e0.run(3, graph=graph)
+    k0 = e1.kernel_count
+    e1.run(3, graph=graph)
+    e1.sync()
+    assert e1.kernel_count - k0 == 3  # one launch per step
+    for a, b in zip(pers, per_kernel):
+        for f in FIELDS:
+            x, y = a.get(f), b.get(f)
+            assert np.array_equal(x, y), (f, float(np.max(np.abs(x - y))), a.jx, a.iy, a.kz)
+    e0.close()
+    e1.close()
+    for m in per_kernel + pers:
+        m.close()
+
+
+def test_persistent_rejects_variants_it_does_not_carry(gpu_lib, stream):
+    ms = members(gpu_lib, "fp32_mixed", stream=stream.cuda_stream)
+    e = gpu_lib.Ensemble(ms)
+    for tuning in ([32, 0, 1], [4, 4, 1], [4, 0, 5]):  # strips, k-marching momentum, 5 fields
+        e.set_tuning(tuning)
+        with pytest.raises(gpu_lib.MolochError):
+            e.set_persistent(True)
+        assert not e.persistent
+    e.close()
+    for m in ms:
+        m.close()
+
+
+def test_persistent_barrier_wait_runs_out(gpu_lib, stream):
+    """Block 0 leaves at the fourth grid barrier without arriving: every
+    other block's wait gives up after its limit (about 1 ms here), the step
+    is abandoned and sync reports MOLOCH_ERR_TIMEOUT; launches made while
+    the flag is set return at once.  With the hook off, steps run again."""
+    ms = members(gpu_lib, "fp32_mixed", stream=stream.cuda_stream)
+    e = gpu_lib.Ensemble(ms)
+    e.set_persistent(True)
+    e.set_wait_limit(cycles=2_000_000, skip_block=0, skip_barrier=3)
+    e.run(2, graph=False)
+    with pytest.raises(gpu_lib.MolochError) as err:
+        e.sync()
+    assert err.value.code == 6, err.value  # MOLOCH_ERR_TIMEOUT
+    e.set_wait_limit()
+    e.run(1, graph=False)
+    e.sync()
+    e.close()
+    for m in ms:
+        m.close()
+
+
+def test_persistent_autotune_picks_a_mode(gpu_lib, stream):
+    ms = members(gpu_lib, "fp32_mixed", stream=stream.cuda_stream)
+    e = gpu_lib.Ensemble(ms)
+    e.autotune()
+    e.run(2, graph=True)
+    e.sync()
+    for m in ms:
+        assert np.isfinite(m.get("t")).all()
+    print("persistent" if e.persistent else "per kernel")
+    e.close()
+    for m in ms:
+        m.close()
