@@ -110,6 +110,8 @@ _PROTOS = {
     "moloch_gpu_ensemble_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int,
                                                           ctypes.c_int]),
     "moloch_gpu_ensemble_sync": (ctypes.c_int, [ctypes.c_void_p]),
+    "moloch_gpu_ensemble_profile_step": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                                        ctypes.POINTER(ctypes.c_int), ctypes.c_int]),
     "moloch_gpu_ensemble_destroy": (ctypes.c_int, [ctypes.c_void_p]),
     "moloch_tc_gemm": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_int,
@@ -435,12 +437,23 @@ class Ensemble:
     def kernel_count(self):
         return self.L.moloch_gpu_ensemble_kernel_count(self.h)
 
+    def profile_step(self):
+        """One step timed per kernel kind: {kernel: (ms, launches or phases)}."""
+        n = self.L.moloch_gpu_kernel_kinds()
+        ms = (ctypes.c_double * n)()
+        cnt = (ctypes.c_int * n)()
+        _check(self.L.moloch_gpu_ensemble_profile_step(self.h, ms, cnt, n))
+        return {self.L.moloch_gpu_kernel_name(k).decode(): (ms[k], cnt[k]) for k in range(n) if cnt[k]}
+
     def set_persistent(self, on=True):
-        _check(self.L.moloch_gpu_ensemble_set_persistent(self.h, int(bool(on))))
+        """on: False/0 off; True/1 on; 2, 3, 4: on, with the kernel built for
+        that many resident blocks per SM."""
+        _check(self.L.moloch_gpu_ensemble_set_persistent(self.h, int(on)))
 
     @property
     def persistent(self):
-        return bool(self.L.moloch_gpu_ensemble_persistent(self.h))
+        """0 when off, else the resident blocks per SM of the build in use."""
+        return self.L.moloch_gpu_ensemble_persistent(self.h)
 
     def set_wait_limit(self, cycles=0, skip_block=-1, skip_barrier=-1):
         """Limit of the persistent kernel's grid-barrier waits (SM cycles,

@@ -1475,6 +1475,8 @@ struct moloch_ensemble {
   int nphases = 0;
   persist::Ctl* ctl = nullptr;
   int* perr = nullptr;
+  unsigned long long* pstamps = nullptr;  // per-phase timestamps (profiling)
+  int pvariant = 1;  // persistent kernel built for 3 blocks per SM
   int pgrid = 0;
   size_t psmem = 0;
   long long pspin = kDefaultSpinCycles;
@@ -1552,7 +1554,8 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
   for (int t = 0; t < TK_COUNT; ++t) bytes += ((e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255));
   // persistent mode: two phase programs, the barrier/queue words, the error word
   const size_t prog_bytes = ((sizeof(persist::Phase) * persist::kMaxPhases + 255) & ~size_t(255));
-  const size_t pbytes = 2 * prog_bytes + ((sizeof(persist::Ctl) + 255) & ~size_t(255)) + 256;
+  const size_t stamp_bytes = sizeof(unsigned long long) * (persist::kMaxPhases + 1);
+  const size_t pbytes = 2 * prog_bytes + ((sizeof(persist::Ctl) + 255) & ~size_t(255)) + 256 + stamp_bytes;
   if (e->dev) cudaFree(e->dev);
   e->dev = nullptr;
   e->prog[0] = e->prog[1] = nullptr;
@@ -1585,12 +1588,18 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     b.vfields = e->vfields;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
+  if (!e->pgrid) {
+    int dev = 0, sms = 0;
+    CUDA_TRY(cudaGetDevice(&dev));
+    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    e->pgrid = persist::blocks_per_sm<T>(e->pvariant, &e->psmem) * sms;
+  }
   // persistent-mode programs (empty when the tuning has a variant the
   // persistent kernel does not carry)
   e->nphases = 0;
   for (int f = 0; f < 2; ++f) {
     std::vector<persist::Phase> prog;
-    const int prc = persist::program<T>(b, e->fl, f, prog);
+    const int prc = persist::program<T>(b, e->fl, f, e->pgrid, prog);
     if (prc == 0) {
       CUDA_TRY(cudaMemcpy(p + off, prog.data(), prog.size() * sizeof(persist::Phase), cudaMemcpyHostToDevice));
       e->prog[f] = (const persist::Phase*)(p + off);
@@ -1601,13 +1610,9 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
   e->ctl = (persist::Ctl*)(p + off);
   off += (sizeof(persist::Ctl) + 255) & ~size_t(255);
   e->perr = (int*)(p + off);
+  off += 256;
+  e->pstamps = (unsigned long long*)(p + off);
   CUDA_TRY(cudaMemset(e->perr, 0, sizeof(int)));
-  if (!e->pgrid) {
-    int dev = 0, sms = 0;
-    CUDA_TRY(cudaGetDevice(&dev));
-    CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    e->pgrid = persist::blocks_per_sm<T>(&e->psmem) * sms;
-  }
   if (e->persistent && (!e->nphases || !e->pgrid)) e->persistent = 0;
   return MOLOCH_OK;
 }
@@ -1619,7 +1624,7 @@ int ens_build(moloch_ensemble* e) {
 }
 
 template <class T>
-int ens_step_persistent(moloch_ensemble* e, const Batch<T>& b) {
+int ens_step_persistent(moloch_ensemble* e, const Batch<T>& b, bool stamps = false) {
   persist::Args<T> a;
   a.views = b.views[0][0];  // the four parities follow one another, n views each
   a.nmembers = (int)e->m.size();
@@ -1630,8 +1635,9 @@ int ens_step_persistent(moloch_ensemble* e, const Batch<T>& b) {
   a.spin = e->pspin;
   a.skip_block = e->skip_block;
   a.skip_barrier = e->skip_barrier;
+  a.stamps = stamps ? e->pstamps : nullptr;
   cudaMemsetAsync(e->ctl, 0, persist::ctl_bytes(e->nphases), e->stream);
-  persist::launch<T>(a, e->pgrid, e->psmem, e->stream);
+  persist::launch<T>(a, e->pvariant, e->pgrid, e->psmem, e->stream);
   e->fcur ^= (e->fl.nadv & 1);
   e->cur = 0;
   return 1;
@@ -1810,12 +1816,19 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   // carries the chosen variants
   const bool pok = e->elem == 8 ? persist::supports<double>(e->hz_levels, e->kmarch, e->vfields)
                                 : persist::supports<float>(e->hz_levels, e->kmarch, e->vfields);
-  double tmode[2] = {0.0, 1e30};
-  for (int mode = 0; mode < (pok ? 2 : 1); ++mode) {
-    e->persistent = mode;
+  // mode 0: one launch per kernel; 1 + v: the persistent kernel built for
+  // 2 + v blocks per SM
+  double tmode[1 + persist::kVariants];
+  for (double& t : tmode) t = 1e30;
+  for (int mode = 0; mode < (pok ? 1 + persist::kVariants : 1); ++mode) {
+    e->persistent = mode ? 1 : 0;
+    if (mode && e->pvariant != mode - 1) {
+      e->pvariant = mode - 1;
+      e->pgrid = 0;
+    }
     int rc = ens_build(e);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
-    if (mode && !e->persistent) break;  // no resident blocks: stays off
+    if (mode && !e->persistent) continue;  // no resident blocks
     float ms = 0.f, tot = 0.f;
     for (int rep = 0; rep < 3; ++rep) {
       cudaEventRecord(e0, e->stream);
@@ -1840,7 +1853,14 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
       return fail(MOLOCH_ERR_TIMEOUT, "ensemble autotune: a grid-barrier wait of the persistent kernel gave up");
     }
   }
-  e->persistent = (pok && tmode[1] < tmode[0]) ? 1 : 0;
+  int bestm = 0;
+  for (int mode = 1; mode < 1 + persist::kVariants; ++mode)
+    if (tmode[mode] < tmode[bestm]) bestm = mode;
+  e->persistent = bestm ? 1 : 0;
+  if (bestm && e->pvariant != bestm - 1) {
+    e->pvariant = bestm - 1;
+    e->pgrid = 0;
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   choice[0] = pick;
@@ -1874,6 +1894,7 @@ long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e) { return e ? e-
 int moloch_gpu_ensemble_set_persistent(moloch_ensemble_t* e, int on) {
   g_err.clear();
   if (!e) return fail(MOLOCH_ERR_ARG, "null ensemble");
+  if (on < 0 || on > 4) return fail(MOLOCH_ERR_ARG, "persistent %d: 0 off, 1 default, 2-4 blocks per SM", on);
   if (on) {
     const bool ok = e->elem == 8 ? persist::supports<double>(e->hz_levels, e->kmarch, e->vfields)
                                  : persist::supports<float>(e->hz_levels, e->kmarch, e->vfields);
@@ -1884,6 +1905,10 @@ int moloch_gpu_ensemble_set_persistent(moloch_ensemble_t* e, int on) {
                   e->hz_levels, e->kmarch, e->vfields,
                   e->elem == 8 ? "fused divergence/damping strips" : "k-marching momentum");
   }
+  if (on >= 2 && on - 2 != e->pvariant) {
+    e->pvariant = on - 2;
+    e->pgrid = 0;  // resident blocks of the other build
+  }
   e->persistent = on ? 1 : 0;
   int rc = ens_build(e);
   if (rc) return rc;
@@ -1891,7 +1916,65 @@ int moloch_gpu_ensemble_set_persistent(moloch_ensemble_t* e, int on) {
   return MOLOCH_OK;
 }
 
-int moloch_gpu_ensemble_persistent(moloch_ensemble_t* e) { return e ? e->persistent : -1; }
+int moloch_gpu_ensemble_persistent(moloch_ensemble_t* e) { return e ? (e->persistent ? e->pvariant + 2 : 0) : -1; }
+
+int moloch_gpu_ensemble_profile_step(moloch_ensemble_t* e, double* ms_by_kind, int* launches_by_kind, int nkinds) {
+  g_err.clear();
+  if (!e) return fail(MOLOCH_ERR_ARG, "null ensemble");
+  CUDA_TRY(cudaStreamSynchronize(e->stream));
+  if (e->persistent) {
+    const int np = e->nphases;
+    const int f0 = e->fcur;
+    e->kernels += e->elem == 8 ? ens_step_persistent(e, e->bd, true) : ens_step_persistent(e, e->bf, true);
+    int rc = check_launch("ensemble profile");
+    if (rc) return rc;
+    std::vector<unsigned long long> st(np + 1);
+    std::vector<persist::Phase> prog(np);
+    CUDA_TRY(cudaMemcpyAsync(st.data(), e->pstamps, st.size() * sizeof(unsigned long long), cudaMemcpyDeviceToHost,
+                             e->stream));
+    CUDA_TRY(cudaMemcpyAsync(prog.data(), e->prog[f0], prog.size() * sizeof(persist::Phase), cudaMemcpyDeviceToHost,
+                             e->stream));
+    CUDA_TRY(cudaStreamSynchronize(e->stream));
+    for (int p = 0; p < np; ++p) {
+      const int k = persist::phase_kernel_kind(prog[p].kind);
+      if (k < nkinds) {
+        if (ms_by_kind) ms_by_kind[k] += (double)(st[p + 1] - st[p]) * 1e-6;
+        if (launches_by_kind) launches_by_kind[k] += 1;
+      }
+    }
+    ens_sync_members(e);
+    return moloch_gpu_ensemble_sync(e);
+  }
+  KernelTimer* tm = new KernelTimer();
+  for (int q = 0; q < KernelTimer::kCap; ++q)
+    if (cudaEventCreate(&tm->ev[q]) != cudaSuccess) {
+      for (int r = 0; r < q; ++r) cudaEventDestroy(tm->ev[r]);
+      delete tm;
+      return fail(MOLOCH_ERR_CUDA, "event create");
+    }
+  kfast::set_timer(tm);
+  int n = ens_step_kernels(e);
+  kfast::set_timer(nullptr);
+  e->kernels += n;
+  int rc = check_launch("ensemble profile");
+  if (!rc && cudaStreamSynchronize(e->stream) != cudaSuccess) rc = fail(MOLOCH_ERR_CUDA, "ensemble profile sync");
+  if (!rc && !tm->ok) rc = fail(MOLOCH_ERR_ARG, "too many kernels to profile one step");
+  if (!rc) {
+    for (int q = 0; q + 1 < tm->n; q += 2) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, tm->ev[q], tm->ev[q + 1]);
+      const int k = tm->kind[q / 2];
+      if (k < nkinds) {
+        if (ms_by_kind) ms_by_kind[k] += ms;
+        if (launches_by_kind) launches_by_kind[k] += 1;
+      }
+    }
+  }
+  for (int q = 0; q < KernelTimer::kCap; ++q) cudaEventDestroy(tm->ev[q]);
+  delete tm;
+  ens_sync_members(e);
+  return rc;
+}
 
 int moloch_gpu_ensemble_set_wait_limit(moloch_ensemble_t* e, long long cycles, int skip_block, int skip_barrier) {
   g_err.clear();

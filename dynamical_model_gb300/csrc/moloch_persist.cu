@@ -12,10 +12,11 @@
 // own kernels; the 32 x 4 column bodies get tiles 8 rows high (see
 // TK_COLUMN8); the warp-strip bodies get 8 strips per item, one per warp,
 // with the momentum strips' cp.async rings in dynamic shared memory.  The
-// register budget is that of 3 blocks per SM in FP32 (85 registers) and 2
-// in FP64 (128): the variants above it (FP32 k-marching momentum, FP64
-// fused divergence/damping strips, horizontal WAF strips, 5 or 10
-// vertical-WAF fields per thread) are not carried.
+// kernel is built for 2, 3 and 4 resident blocks per SM (register budgets
+// of 128, 80 and 64; the ensemble autotuner picks one).  Body variants that
+// need far more than the budget of 3 blocks in FP32 or 2 in FP64 (FP32
+// k-marching momentum, FP64 fused divergence/damping strips, horizontal WAF
+// strips, 5 or 10 vertical-WAF fields per thread) are not carried.
 //
 // Grid barrier: thread 0 of each block fences, takes the arrival counter,
 // and the last arrival resets the counter and bumps the generation; the
@@ -27,6 +28,8 @@
 #include "../../include/moloch_gb300.h"
 #include "moloch_kernels.cuh"
 #include "moloch_persist.h"
+
+#include <algorithm>
 
 namespace moloch {
 namespace persist {
@@ -67,6 +70,12 @@ __device__ __forceinline__ void run_item(const View<T>& d, const Phase& ph, cons
   }
 }
 
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
 // barrier after phase p; false when the step is abandoned (a wait gave up
 // here or elsewhere, or this block is the test hook's)
 template <class T>
@@ -101,8 +110,8 @@ __device__ __forceinline__ bool grid_barrier(const Args<T>& a, const int p, int*
   return *s_ok != 0;
 }
 
-template <class T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_ensemble_persistent(const __grid_constant__ Args<T> a) {
+template <class T, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_ensemble_persistent(const __grid_constant__ Args<T> a) {
   extern __shared__ __align__(16) unsigned char persist_smem[];
   MomSlots<T>* ring = reinterpret_cast<MomSlots<T>*>(persist_smem);  // one per warp
   __shared__ View<T> sv;
@@ -110,26 +119,36 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_ensemble_persis
   __shared__ int s_ok;
   if (*(volatile int*)a.err) return;  // an earlier step gave up: nothing runs until the host clears it
   const int tid = threadIdx.x + 32 * threadIdx.y;
+  const bool stamp = a.stamps != nullptr && blockIdx.x == 0 && tid == 0;
+  if (stamp) a.stamps[0] = globaltimer_ns();
   int have = -1;  // which view sv holds
   for (int p = 0; p < a.nphases; ++p) {
     const Phase ph = a.prog[p];
+    // chunks of ph.chunk items; the claim of the next chunk is in flight
+    // while this one runs.  Claim slots alternate: thread 0 rewrites a slot
+    // one chunk after the others read it, with a barrier between.
+    if (tid == 0) s_item[0] = atomicAdd(&a.ctl->q[p], ph.chunk);
+    __syncthreads();
     for (int it = 0;; ++it) {
-      // item slots alternate: a slot is rewritten two items later, after a
-      // barrier every thread has passed since reading it
-      if (tid == 0) s_item[it & 1] = atomicAdd(&a.ctl->q[p], 1);
-      __syncthreads();
-      const int item = s_item[it & 1];
-      if (item >= ph.ntiles) break;
-      const int4 t = ph.tiles[item];
-      const int vid = ph.par * a.nmembers + t.x;
-      if (vid != have) {
-        copy_view(&sv, a.views + vid);
-        __syncthreads();
-        have = vid;
+      const int start = s_item[it & 1];
+      if (start >= ph.ntiles) break;
+      if (tid == 0) s_item[(it + 1) & 1] = atomicAdd(&a.ctl->q[p], ph.chunk);
+      const int end = min(start + ph.chunk, ph.ntiles);
+      for (int item = start; item < end; ++item) {
+        const int4 t = ph.tiles[item];
+        const int vid = ph.par * a.nmembers + t.x;
+        if (vid != have) {  // block-uniform
+          __syncthreads();  // every thread is done with the previous view
+          copy_view(&sv, a.views + vid);
+          __syncthreads();
+          have = vid;
+        }
+        run_item<T>(sv, ph, t, ring);
       }
-      run_item<T>(sv, ph, t, ring);
+      __syncthreads();  // the next claim is visible
     }
     if (!grid_barrier(a, p, &s_ok)) return;
+    if (stamp) a.stamps[p + 1] = globaltimer_ns();
   }
 }
 
@@ -142,9 +161,9 @@ bool supports(int hz_levels, int kmarch, int vfields) {
 }
 
 template <class T>
-int program(const Batch<T>& b, const PhaseFlags& fl, int fcur, std::vector<Phase>& out) {
+int program(const Batch<T>& b, const PhaseFlags& fl, int fcur, int grid, std::vector<Phase>& out) {
   out.clear();
-  if (b.hstrip || !supports<T>(4, b.kmarch, b.vfields)) return 1;
+  if (b.hstrip || !supports<T>(4, b.kmarch, b.vfields) || grid < 1) return 1;
   int cur = 0;
   auto P = [&](int kind, int tk, int a0 = 0, int a1 = 0, int a2 = 0) {
     Phase ph;
@@ -155,6 +174,7 @@ int program(const Batch<T>& b, const PhaseFlags& fl, int fcur, std::vector<Phase
     ph.a0 = a0;
     ph.a1 = a1;
     ph.a2 = a2;
+    ph.chunk = std::max(1, ph.ntiles / (8 * grid));
     out.push_back(ph);
   };
   // the order of the per-kernel launches (blaunch_step)
@@ -194,20 +214,30 @@ int program(const Batch<T>& b, const PhaseFlags& fl, int fcur, std::vector<Phase
 template <class T>
 static size_t ring_bytes() { return sizeof(MomSlots<T>) * kWarps; }
 
+// the kernel instantiated for 2, 3 and 4 resident blocks per SM (register
+// budgets of 128, 80 and 64 per thread)
 template <class T>
-int blocks_per_sm(size_t* smem) {
+static const void* kernel_of(int variant) {
+  switch (variant) {
+    case 0: return (const void*)k_ensemble_persistent<T, 2>;
+    case 2: return (const void*)k_ensemble_persistent<T, 4>;
+    default: return (const void*)k_ensemble_persistent<T, 3>;
+  }
+}
+
+template <class T>
+int blocks_per_sm(int variant, size_t* smem) {
   const size_t s = ring_bytes<T>();
   if (smem) *smem = s;
-  if (cudaFuncSetAttribute(k_ensemble_persistent<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s) !=
-      cudaSuccess)
-    return 0;
+  const void* k = kernel_of<T>(variant);
+  if (cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s) != cudaSuccess) return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_ensemble_persistent<T>, 256, s) != cudaSuccess) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, 256, s) != cudaSuccess) return 0;
   return nb;
 }
 
 template <class T>
-cudaError_t launch(const Args<T>& a, int grid, size_t smem, cudaStream_t st) {
+cudaError_t launch(const Args<T>& a, int variant, int grid, size_t smem, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
   cfg.blockDim = dim3(32, 8);
@@ -218,17 +248,21 @@ cudaError_t launch(const Args<T>& a, int grid, size_t smem, cudaStream_t st) {
   at[0].val.cooperative = 1;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_ensemble_persistent<T>, a);
+  switch (variant) {
+    case 0: return cudaLaunchKernelEx(&cfg, k_ensemble_persistent<T, 2>, a);
+    case 2: return cudaLaunchKernelEx(&cfg, k_ensemble_persistent<T, 4>, a);
+    default: return cudaLaunchKernelEx(&cfg, k_ensemble_persistent<T, 3>, a);
+  }
 }
 
 template bool supports<float>(int, int, int);
 template bool supports<double>(int, int, int);
-template int program<float>(const Batch<float>&, const PhaseFlags&, int, std::vector<Phase>&);
-template int program<double>(const Batch<double>&, const PhaseFlags&, int, std::vector<Phase>&);
-template int blocks_per_sm<float>(size_t*);
-template int blocks_per_sm<double>(size_t*);
-template cudaError_t launch<float>(const Args<float>&, int, size_t, cudaStream_t);
-template cudaError_t launch<double>(const Args<double>&, int, size_t, cudaStream_t);
+template int program<float>(const Batch<float>&, const PhaseFlags&, int, int, std::vector<Phase>&);
+template int program<double>(const Batch<double>&, const PhaseFlags&, int, int, std::vector<Phase>&);
+template int blocks_per_sm<float>(int, size_t*);
+template int blocks_per_sm<double>(int, size_t*);
+template cudaError_t launch<float>(const Args<float>&, int, int, size_t, cudaStream_t);
+template cudaError_t launch<double>(const Args<double>&, int, int, size_t, cudaStream_t);
 
 }  // namespace persist
 }  // namespace moloch

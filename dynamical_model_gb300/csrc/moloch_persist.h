@@ -35,6 +35,7 @@ struct Phase {
   const int4* tiles;  // device tile table (member, bx, by, bz)
   int par;            // views of parity (cur, fcur) = (par >> 1, par & 1)
   int a0, a1, a2;     // body arguments (strip rows; nsound, last, defer_pai; filter switches)
+  int chunk;          // items a block takes from the queue at a time
 };
 
 constexpr int kMaxPhases = 1024;
@@ -61,25 +62,49 @@ struct Args {
   long long spin;        // limit of a barrier wait, SM clock cycles
   int skip_block;        // test hook: this block leaves at barrier skip_barrier
   int skip_barrier;      // without arriving (-1: none)
+  unsigned long long* stamps;  // profiling (nullptr: off): global timer (ns) at the
+                               // start [0] and as block 0 leaves barrier p [p + 1]
 };
+
+// the per-kernel timing bucket (KernelKind) of each phase kind
+inline int phase_kernel_kind(int ph) {
+  switch (ph) {
+    case PH_PREDIAG: return KK_PREDIAG;
+    case PH_DIVDAMP_STRIP: return KK_SOUND_DIVDAMP;
+    case PH_DIV: case PH_DIV_KM: return KK_SOUND_DIV;
+    case PH_DAMP: case PH_DAMP_KM: return KK_SOUND_DAMP;
+    case PH_COLUMN: return KK_SOUND_COLUMN;
+    case PH_LAP_FILTER: return KK_LAP_FILTER;
+    case PH_PAI_UPDATE: return KK_PAI_UPDATE;
+    case PH_MOM_STRIP: case PH_MOM: case PH_MOM_KM: return KK_SOUND_MOMENTUM;
+    case PH_WAF_VERTICAL1: case PH_WAF_VERTICAL2: return KK_WAF_VERTICAL;
+    case PH_WAF_HORIZONTAL: return KK_WAF_HORIZONTAL;
+    case PH_STAG: return KK_STAG_FROM_X;
+    default: return KK_POSTDIAG;
+  }
+}
 
 // The step as a phase program for the batch's tuning, starting at field-set
 // parity fcur (u/v parity 0).  Returns 0, or a nonzero code when the tuning
 // asks for a kernel variant the persistent kernel does not carry (FP32: the
 // k-marching momentum; FP64: the fused divergence/damping strips; both: the
 // horizontal WAF strips and 5 or 10 vertical-WAF fields per thread).
+// grid: blocks of the launch (sets each phase's chunk to about an eighth of
+// a block's share of the items).
 template <class T>
-int program(const Batch<T>& b, const PhaseFlags& fl, int fcur, std::vector<Phase>& out);
+int program(const Batch<T>& b, const PhaseFlags& fl, int fcur, int grid, std::vector<Phase>& out);
 // whether the persistent kernel carries the variants of this tuning
 template <class T>
 bool supports(int hz_levels, int kmarch, int vfields);
-// resident blocks per SM of the persistent kernel (0 if it cannot run) and
-// its dynamic shared memory
+// Kernel variants: built for 2, 3 or 4 resident blocks of 256 threads per
+// SM (variant 0, 1, 2).  Resident blocks per SM of a variant (0 if it
+// cannot run) and its dynamic shared memory.
+constexpr int kVariants = 3;
 template <class T>
-int blocks_per_sm(size_t* smem);
+int blocks_per_sm(int variant, size_t* smem);
 // one cooperative launch of grid blocks of 32 x 8 threads
 template <class T>
-cudaError_t launch(const Args<T>& a, int grid, size_t smem, cudaStream_t st);
+cudaError_t launch(const Args<T>& a, int variant, int grid, size_t smem, cudaStream_t st);
 
 }  // namespace persist
 }  // namespace moloch

@@ -288,14 +288,23 @@ int moloch_gpu_ensemble_run(moloch_ensemble_t* e, int nsteps, int use_graph);
 int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best_ms, int nchoice);
 int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int nchoice);
 long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);
-/* persistent mode on (1) or off (0).  It carries the horizontal WAF as tiles
+/* persistent mode: 0 off; 2, 3 or 4 on, with the kernel built for that many
+ * resident blocks of 256 threads per SM (register budgets 128, 80, 64);
+ * 1 on with the last build chosen (3 at first).  It carries the horizontal WAF as tiles
  * (choice[0] 1..8), 1 or 2 vertical-WAF fields per thread, and in FP32 no
  * k-marching momentum (choice[1] bit 4 without 8), in FP64 no fused
  * divergence/damping strips (bit 16); other tunings give MOLOCH_ERR_ARG.
- * moloch_gpu_ensemble_autotune times both modes on whole steps and keeps the
- * faster; moloch_gpu_ensemble_persistent returns the mode in use. */
+ * moloch_gpu_ensemble_autotune times one launch per kernel and the three
+ * builds on whole steps and keeps the fastest; moloch_gpu_ensemble_persistent
+ * returns the blocks per SM of the build in use, 0 when the mode is off. */
 int moloch_gpu_ensemble_set_persistent(moloch_ensemble_t* e, int on);
 int moloch_gpu_ensemble_persistent(moloch_ensemble_t* e);
+/* One ensemble step (not graph-captured) timed per kernel kind, in the
+ * buckets of moloch_gpu_profile_step: per-kernel mode, CUDA events around
+ * every launch; persistent mode, the GPU global timer read by block 0 as it
+ * leaves each grid barrier (a phase's time includes its barrier).  Adds to
+ * ms_by_kind / launches_by_kind (phases per kind in persistent mode). */
+int moloch_gpu_ensemble_profile_step(moloch_ensemble_t* e, double* ms_by_kind, int* launches_by_kind, int nkinds);
 /* Limit of every grid-barrier wait of the persistent kernel, in SM clock
  * cycles (<= 0: the default 2e9, about one second).  skip_block/skip_barrier
  * (-1: off) are a test hook: that block leaves the launch at that barrier
