@@ -118,6 +118,7 @@ _PROTOS = {
                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_void_p]),
     "moloch_tc_status": (ctypes.c_int, []),
+    "moloch_tc_set_wait_limit": (ctypes.c_int, [ctypes.c_longlong, ctypes.c_int, ctypes.c_int]),
     "moloch_gpu_wafone_noalloc": (ctypes.c_int, [ctypes.c_void_p] * 9 + [ctypes.c_int] * 3 +
                                   [ctypes.c_double] * 3 + [ctypes.c_int, ctypes.c_void_p]),
     "moloch_gpu_output_start": (ctypes.c_int, [ctypes.c_void_p]),

@@ -18,6 +18,7 @@
 
 #include "../../include/moloch_gb300.h"
 #include "moloch_tc.cuh"
+#include "moloch_view.h"
 
 extern "C" void moloch_internal_set_error(const char* msg);
 
@@ -37,6 +38,13 @@ constexpr int kEpiThreads = 256;
 enum Act { ACT_NONE = 0, ACT_SILU = 1 };
 
 static __device__ int g_tc_error;  // set when a bounded wait gives up
+// limit of every mbarrier wait of k_gemm_tc, SM clock cycles
+static __device__ long long g_tc_spin = kDefaultSpinCycles;
+// test hook: the loader of CTA g_tc_skip_cta leaves its K-chunk number
+// g_tc_skip_it (counted over the CTA's tiles) unarmed and unissued, so the
+// MMA wait for it finds nothing in flight and runs out (-1: off)
+static __device__ int g_tc_skip_cta = -1;
+static __device__ int g_tc_skip_it = -1;
 
 // x * sigmoid(x) with the fast reciprocal divide (relative error ~1e-7,
 // far below the BF16 rounding of the stored activation); exp(-x) = inf
@@ -66,6 +74,8 @@ __global__ void __launch_bounds__(kThreads, 1)
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nm = (M + kTileM - 1) / kTileM, nn = (N + kTileN - 1) / kTileN, ntiles = nm * nn;
   const int nk = K / kChunkK;
+  const long long lim = g_tc_spin;
+  const int skip_it = (int)blockIdx.x == g_tc_skip_cta ? g_tc_skip_it : -1;
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   if (tid == 32) {
     for (int s = 0; s < kStages; ++s) {
@@ -94,10 +104,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int m0 = (t % nm) * kTileM, n0 = (t / nm) * kTileN;
       for (int kc = 0; kc < nk; ++kc, ++it) {
         const int s = it % kStages;
-        if (it >= kStages && !tc::mbar_wait(&empty[s], ((it / kStages) - 1) & 1)) {
+        if (it >= kStages && !tc::mbar_wait_cycles(&empty[s], ((it / kStages) - 1) & 1, lim)) {
           s_fail = 1;
           break;
         }
+        if (it == skip_it) continue;  // test hook: this stage stays unarmed
         uint8_t* sa = smem + s * (kAStage + kBStage);
         tc::mbar_arrive_expect_tx(&full[s], stage_bytes);
         tc::tma_load_2d(sa, &tmA, kc * kChunkK, m0, &full[s]);
@@ -113,7 +124,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int nt = min(kTileN, N - n0);
       const uint32_t idesc = tc::idesc_bf16(nt);
       const int b = lt & 1;
-      if (lt >= 2 && !tc::mbar_wait(&acc_empty[b], ((lt >> 1) - 1) & 1)) {
+      if (lt >= 2 && !tc::mbar_wait_cycles(&acc_empty[b], ((lt >> 1) - 1) & 1, lim)) {
         s_fail = 1;
         break;
       }
@@ -121,7 +132,7 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t dacc = tbase + (uint32_t)(b * kTileN);
       for (int kc = 0; kc < nk; ++kc, ++it) {
         const int s = it % kStages;
-        if (!tc::mbar_wait(&full[s], (it / kStages) & 1)) {
+        if (!tc::mbar_wait_cycles(&full[s], (it / kStages) & 1, lim)) {
           s_fail = 1;
           break;
         }
@@ -148,7 +159,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     int lt = 0;
     for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++lt) {
       const int b = lt & 1;
-      if (!tc::mbar_wait(&acc_full[b], (lt >> 1) & 1)) {
+      if (!tc::mbar_wait_cycles(&acc_full[b], (lt >> 1) & 1, lim)) {
         s_fail = 1;
         break;
       }
@@ -218,10 +229,10 @@ __global__ void __launch_bounds__(kThreads, 1)
   if (tid == 0) {
     // every MMA has completed before TMEM is released; loads still in
     // flight after a failed wait are drained (all waits bounded)
-    if (!tc::mbar_wait(&done, 0)) s_fail = 1;
+    if (!tc::mbar_wait_cycles(&done, 0, lim)) s_fail = 1;
     if (s_fail) {
       atomicExch(&g_tc_error, 1);
-      for (int it = s_consumed; it < s_issued; ++it) tc::mbar_wait(&full[it % kStages], (it / kStages) & 1);
+      for (int it = s_consumed; it < s_issued; ++it) tc::mbar_wait_cycles(&full[it % kStages], (it / kStages) & 1, lim);
     }
   }
   tc::tc_fence_before();
@@ -319,6 +330,19 @@ extern "C" int moloch_tc_gemm(const void* A, int lda, const void* B, int ldb, fl
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     moloch_internal_set_error(cudaGetErrorString(e));
+    return MOLOCH_ERR_CUDA;
+  }
+  return MOLOCH_OK;
+}
+
+// Limit of the GEMM's mbarrier waits (SM cycles, <= 0: the default) and the
+// test hook that leaves one K chunk of one CTA unissued (-1: off).
+extern "C" int moloch_tc_set_wait_limit(long long cycles, int skip_cta, int skip_chunk) {
+  const long long c = cycles > 0 ? cycles : moloch::kDefaultSpinCycles;
+  if (cudaMemcpyToSymbol(g_tc_spin, &c, sizeof(c)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_tc_skip_cta, &skip_cta, sizeof(int)) != cudaSuccess ||
+      cudaMemcpyToSymbol(g_tc_skip_it, &skip_chunk, sizeof(int)) != cudaSuccess) {
+    moloch_internal_set_error("tc_set_wait_limit: cudaMemcpyToSymbol failed");
     return MOLOCH_ERR_CUDA;
   }
   return MOLOCH_OK;
@@ -546,9 +570,13 @@ __global__ void k_transpose_bf16(const TI* __restrict__ in, int rows, int cols, 
 }
 
 // MSE gradient: dY = 2 (Y - T) / (n * m) over the first m columns (zero in
-// the padding), BF16; accumulates the squared error into *loss
-__global__ void k_sur_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, int n, int ld, int m,
-                                __nv_bfloat16* __restrict__ dY, float* __restrict__ loss) {
+// the padding), BF16; the block's sum of squared errors into lpart[block]
+// (summed in a fixed order by k_sum_parts, so the reported loss does not
+// depend on the order blocks finish in).  256 threads per block.
+__global__ void __launch_bounds__(256) k_sur_loss_grad(const float* __restrict__ Y, const float* __restrict__ T, int n,
+                                                       int ld, int m, __nv_bfloat16* __restrict__ dY,
+                                                       float* __restrict__ lpart) {
+  __shared__ float wsum[8];
   float acc = 0.f;
   const float sc = 2.0f / ((float)n * (float)m);
   const size_t tot = (size_t)n * ld;
@@ -563,7 +591,27 @@ __global__ void k_sur_loss_grad(const float* __restrict__ Y, const float* __rest
     dY[q] = __float2bfloat16_rn(g);
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, acc);
+  if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float b = 0.f;
+    for (int w = 0; w < 8; ++w) b += wsum[w];
+    lpart[blockIdx.x] = b;
+  }
+}
+
+// *out = sum of part[0 .. n), in a fixed order (one block of 256 threads)
+__global__ void __launch_bounds__(256) k_sum_parts(const float* __restrict__ part, int n, float* __restrict__ out) {
+  __shared__ float red[256];
+  float v = 0.f;
+  for (int b = threadIdx.x; b < n; b += 256) v += part[b];
+  red[threadIdx.x] = v;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] += red[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = red[0];
 }
 
 // dZ = dH * silu'(Z), BF16
@@ -928,8 +976,9 @@ static int forward(Surrogate* s, const void* X, int n, void* const* H, float* co
 // gradients into L[*].gW/gb, loss sum into *s->loss
 static void backward(Surrogate* s, cudaStream_t st) {
   const int B = s->batch, hid = s->hid, nop = s->nop;
-  cudaMemsetAsync(s->loss, 0, sizeof(float), st);
-  k_sur_loss_grad<<<grid1((size_t)B * nop), 256, 0, st>>>(s->Y, s->Tbat, B, nop, s->nout, (__nv_bfloat16*)s->dY, s->loss);
+  const int lg = grid1((size_t)B * nop);
+  k_sur_loss_grad<<<lg, 256, 0, st>>>(s->Y, s->Tbat, B, nop, s->nout, (__nv_bfloat16*)s->dY, s->lpart);
+  k_sum_parts<<<1, 256, 0, st>>>(s->lpart, lg, s->loss);
   // layer 4: gW4 = dY^T H3, gb4 = colsum dY, dH3 = dY W4
   transpose(s->dY, B, nop, nop, s->dYT, B, st);
   transpose(s->H[2], B, hid, hid, s->HT[2], B, st);
@@ -998,7 +1047,7 @@ static void free_sur(Surrogate* s) {
     F(L.W); F(L.b); F(L.gW); F(L.gb); F(L.mW); F(L.vW); F(L.mb); F(L.vb); F(L.Wb); F(L.WT);
   }
   F(s->xmean); F(s->xstd); F(s->ymean); F(s->ystd); F(s->Xraw); F(s->Xb); F(s->T); F(s->snap); F(s->cols);
-  F(s->Xbat); F(s->XbatT); F(s->Tbat); F(s->Y); F(s->dY); F(s->dYT); F(s->loss); F(s->perm);
+  F(s->Xbat); F(s->XbatT); F(s->Tbat); F(s->Y); F(s->dY); F(s->dYT); F(s->loss); F(s->lpart); F(s->perm);
   for (int l = 0; l < 3; ++l) { F(s->H[l]); F(s->HT[l]); F(s->Z[l]); F(s->dH[l]); F(s->dZ[l]); F(s->dZT[l]); F(s->Hinf[l]); }
   F(s->Xinf); F(s->Yinf); F(s->ctl); F(s->counts); F(s->env); F(s->jacc); F(s->jsnap);
 }
@@ -1068,7 +1117,7 @@ int moloch_sur_create(int kz, int capacity, int batch, unsigned long long seed, 
   A(&s->Xbat, (size_t)batch * s->kin * 2); A(&s->XbatT, (size_t)batch * s->kin * 2);
   A((void**)&s->Tbat, (size_t)batch * s->nop * 4); A((void**)&s->Y, (size_t)batch * s->nop * 4);
   A(&s->dY, (size_t)batch * s->nop * 2); A(&s->dYT, (size_t)batch * s->nop * 2);
-  A((void**)&s->loss, 16); A((void**)&s->perm, (size_t)capacity * 4);
+  A((void**)&s->loss, 16); A((void**)&s->lpart, sizeof(float) * kGrid1Max); A((void**)&s->perm, (size_t)capacity * 4);
   for (int l = 0; l < 3; ++l) {
     A(&s->H[l], (size_t)batch * hid * 2); A(&s->HT[l], (size_t)batch * hid * 2);
     A((void**)&s->Z[l], (size_t)batch * hid * 4); A((void**)&s->dH[l], (size_t)batch * hid * 4);
@@ -1233,10 +1282,10 @@ static int eval_loss(Surrogate* s, int r0, int r1, double* out, cudaStream_t st)
   long long cnt = 0;
   for (int r = r0; r + B <= r1; r += B) {
     forward(s, (const __nv_bfloat16*)s->Xb + (size_t)r * s->kin, B, s->H, nullptr, s->Y, st);
-    cudaMemsetAsync(s->loss, 0, 4, st);
     cudaMemcpyAsync(s->Tbat, s->T + (size_t)r * s->nop, (size_t)B * s->nop * 4, cudaMemcpyDeviceToDevice, st);
-    k_sur_loss_grad<<<grid1((size_t)B * s->nop), 256, 0, st>>>(s->Y, s->Tbat, B, s->nop, s->nout,
-                                                                (__nv_bfloat16*)s->dY, s->loss);
+    const int lg = grid1((size_t)B * s->nop);
+    k_sur_loss_grad<<<lg, 256, 0, st>>>(s->Y, s->Tbat, B, s->nop, s->nout, (__nv_bfloat16*)s->dY, s->lpart);
+    k_sum_parts<<<1, 256, 0, st>>>(s->lpart, lg, s->loss);
     float l = 0.f;
     SUR_TRY(cudaMemcpyAsync(&l, s->loss, 4, cudaMemcpyDeviceToHost, st));
     SUR_TRY(cudaStreamSynchronize(st));

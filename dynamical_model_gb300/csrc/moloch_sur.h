@@ -38,6 +38,7 @@ struct Surrogate {
   void *Xbat = nullptr, *XbatT = nullptr, *dY = nullptr, *dYT = nullptr;
   void *H[3] = {}, *HT[3] = {}, *dZ[3] = {}, *dZT[3] = {};
   float *Tbat = nullptr, *Y = nullptr, *loss = nullptr;
+  float* lpart = nullptr;  // per-block partial sums of the loss
   float *Z[3] = {}, *dH[3] = {};
   int* perm = nullptr;
   int adam_t = 0;  // Adam step count

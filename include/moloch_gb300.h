@@ -328,6 +328,14 @@ int moloch_tc_gemm(const void* A, int lda, const void* B, int ldb, float* C, int
 /* MOLOCH_ERR_TIMEOUT if a bounded tensor-core wait gave up since the last
  * call (synchronises the device and clears the flag), else MOLOCH_OK. */
 int moloch_tc_status(void);
+/* Limit of every mbarrier wait of the GEMM kernel (loader, MMA issuer,
+ * epilogue, final drain), in SM clock cycles (<= 0: the default 2e9, about
+ * one second); a wait that runs out sets the flag moloch_tc_status reads,
+ * and the kernel drains its loads in flight and frees its tensor memory
+ * before it returns.  skip_cta / skip_chunk (-1: off) are a test hook: that
+ * CTA's loader leaves that K chunk (counted over the CTA's tiles) unarmed
+ * and unissued, so the MMA wait for it runs out.  Process-wide settings. */
+int moloch_tc_set_wait_limit(long long cycles, int skip_cta, int skip_chunk);
 
 /* ---- learned acoustic-cycle surrogate ---------------------------------------
  * A per-column MLP that replaces one sound() call (the mo_nsound acoustic

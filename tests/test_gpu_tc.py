@@ -58,3 +58,33 @@ def test_tc_gemm_rejects_bad_shapes(gpu_lib):
     L = gpu_lib.lib()
     dummy = ctypes.c_void_p(16)
     assert L.moloch_tc_gemm(dummy, 72, dummy, 72, dummy, 24, None, 0, None, 128, 24, 72, 0, None) == 1
+
+
+def test_tc_gemm_wait_runs_out(gpu_lib):
+    """CTA 0's loader leaves its second K chunk unarmed and unissued (test
+    hook), with the wait limit at 2e6 SM cycles: the MMA issuer's wait for
+    that chunk, then the loader's wait for the stage it never frees, the
+    epilogue's wait for the accumulator and the final drain's wait for the
+    unissued chunk all run out.  moloch_tc_status reports MOLOCH_ERR_TIMEOUT,
+    and the next GEMM, with the hook off, is correct (the kernel drained its
+    loads in flight and freed its tensor memory)."""
+    torch = pytest.importorskip("torch")
+    L = gpu_lib.lib()
+    M, N, K = 256, 64, 512
+    g = torch.Generator(device="cpu").manual_seed(3)
+    A = torch.randn(M, K, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(N, K, generator=g).to(torch.bfloat16).cuda()
+    C = torch.zeros(M, N, device="cuda")
+    P = lambda t: ctypes.c_void_p(t.data_ptr())
+    assert L.moloch_tc_set_wait_limit(2_000_000, 0, 1) == 0
+    try:
+        assert L.moloch_tc_gemm(P(A), K, P(B), K, P(C), N, None, 0, None, M, N, K, 0, None) == 0
+        assert L.moloch_tc_status() == 6  # MOLOCH_ERR_TIMEOUT
+    finally:
+        assert L.moloch_tc_set_wait_limit(0, -1, -1) == 0
+    C.zero_()
+    assert L.moloch_tc_gemm(P(A), K, P(B), K, P(C), N, None, 0, None, M, N, K, 0, None) == 0
+    assert L.moloch_tc_status() == 0
+    ref = A.float() @ B.float().T
+    err = (C - ref).norm() / ref.norm()
+    assert err.item() <= 1e-5, err.item()
