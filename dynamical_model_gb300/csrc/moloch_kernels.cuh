@@ -1145,6 +1145,175 @@ __global__ void __launch_bounds__(128)
   b_momentum_strip<T>(sv, t.y, t.z, R, ring[threadIdx.x >> 5], threadIdx.x >> 5, 4);
 }
 
+// ---- momentum as warp strips, two columns per lane (FP32, jx even) --------
+// b_momentum_strip with each lane on a pair of adjacent columns: strip s
+// computes columns 62 s - 1 .. 62 s + 60 (inside the domain), lane l holds
+// columns 62 s - 2 + 2 l and the next one, so a warp covers 62 output
+// columns with 64 loaded.  The six state arrays of a row arrive as one
+// 8-byte cp.async copy per array and lane, the metric fields as 8-byte
+// loads; a west or east neighbour is the lane's own other column or one
+// shuffle of the lane beside (half the copies, shared loads, shuffles and
+// address arithmetic per point of the one-column strips).  Pairs start at
+// even columns, and with jx even a pair never straddles the periodic seam,
+// so every copy and load is 8-byte aligned.  The same expressions in the
+// same order as b_momentum_strip: the results are bit-identical.
+constexpr int kMom2J = 62;
+constexpr int kMom2S = 6;  // row slots: rows i-1, i, i+1 and three in flight
+using Mom2Slots = float[kMom2S][6][64];  // one warp's ring: [slot][array][column]
+
+__device__ __forceinline__ void cp_async_8(void* dst_smem, const void* src) {
+  const uint32_t dst = static_cast<uint32_t>(__cvta_generic_to_shared(dst_smem));
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+
+__device__ __forceinline__ void b_momentum_strip2(const View<float>& d, const int bx, const int k, const int R,
+                                                  Mom2Slots& rg, const int wid, const int nw) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const int lane = threadIdx.x & 31;
+  const int nj = d.nj, ni = d.ni, pl = d.pl;
+  const int nsj = (nj + 1 + kMom2J - 1) / kMom2J, nsi = (ni + R - 1) / R;
+  const int w = bx * nw + wid;
+  if (w >= nsj * nsi) return;  // whole warp
+  const int sj = w % nsj, si = w / nsj;
+  const int cl = kMom2J * sj - 2 + 2 * lane;  // first column of the pair, before wrapping
+  const int ja = wrapn(cl, nj), jb = ja + 1;  // ja even, so jb < nj
+  const bool out0 = lane >= 1 && cl >= 0 && cl < nj;
+  const bool out1 = lane <= 30 && cl + 1 >= 0 && cl + 1 < nj;
+  const int i_s = si * R, i_e = min(i_s + R, ni);
+  const size_t o = (size_t)k * pl, o1 = o + pl;
+  const float* __restrict__ u = d.ubuf[d.cur] + o;
+  const float* __restrict__ v = d.vbuf[d.cur] + o;
+  float* __restrict__ uo = d.ubuf[d.cur ^ 1] + o;
+  float* __restrict__ vo = d.vbuf[d.cur ^ 1] + o;
+  const float* __restrict__ tet = d.tetav + o;
+  const float* __restrict__ pai = d.pai + o;
+  const float* __restrict__ dw0 = d.deltaw + o;
+  const float* __restrict__ dw1 = d.deltaw + o1;
+  const float dts = d.dts, egdts = d.egdts, dtrdx = d.dtrdx, dtrdy = d.dtrdy;
+  const float hcpd = 0.5f * float(kCpd);
+  const float gzh = d.gzitakh[k];
+  const bool rot = d.rotllr;
+  auto nxt = [](int q) { return q + 1 == kMom2S ? 0 : q + 1; };
+  auto issue = [&](int r, int q) {  // copies of row r into slot q (nothing past i_e); one group either way
+    if (r <= i_e) {
+      const size_t c = (size_t)ja + (size_t)nj * wrap2(r, ni);
+      float(*const sl)[64] = rg[q];
+      cp_async_8(&sl[0][2 * lane], u + c);
+      cp_async_8(&sl[1][2 * lane], v + c);
+      cp_async_8(&sl[2][2 * lane], tet + c);
+      cp_async_8(&sl[3][2 * lane], pai + c);
+      cp_async_8(&sl[4][2 * lane], dw0 + c);
+      cp_async_8(&sl[5][2 * lane], dw1 + c);
+    }
+    cp_async_commit();
+  };
+  struct Row2 { float2 coru, corv, hx, hy, mu, mv; };
+  auto ld2 = [](const float* p) { return *reinterpret_cast<const float2*>(p); };
+  auto load2 = [&](int i, Row2& x) {
+    const size_t c = (size_t)ja + (size_t)nj * wrap2(i, ni);
+    x.coru = ld2(d.coru + c); x.corv = ld2(d.corv + c); x.hx = ld2(d.hx + c); x.hy = ld2(d.hy + c);
+    x.mu = ld2(d.mu + c);
+    x.mv = rot ? make_float2(0.f, 0.f) : ld2(d.mv + c);
+  };
+  for (int r = i_s - 1, q = 0; r <= i_s + kMom2S - 3; ++r, ++q) issue(r, q);
+  Row2 c2, n2;
+  load2(i_s, n2);
+  int qb = 0, qc = 1, qn = 2, qi = kMom2S - 1;
+  const bool interior = sj != 0 && sj != nsj - 1 && i_s != 0 && i_e != ni;
+  // one column: its values, its west / east neighbours and metric terms
+  struct Col { float cu, cv, ct, cp, cd0, cd1, us, ts, ps, ds0, ds1, vn; };
+  auto point = [&](const int jj, const int ii, const Col& x, const float vw, const float vwn, const float tw,
+                   const float pw, const float dw0w, const float dw1w, const float ue, const float ues,
+                   const float coru, const float corv, const float hx, const float hy, const float mu,
+                   const float mv, auto edge, float& un, float& vnew) {
+    constexpr bool EDGE = decltype(edge)::value;
+    // Equation 17
+    {
+      const float zcx = dtrdx * mu;
+      const float zfz = egdts + 0.25f * (((dw0w + dw1w) + x.cd0) + x.cd1);
+      const float zrom1u = hcpd * (tw + x.ct);
+      float vdw = vw, vdwn = vwn, vdn = x.vn, paw = pw;
+      if (EDGE) {
+        const int ip = wp1(ii, ni), jm = wm1(jj, nj);
+        vdw = jj == 0 ? d.ev_j[ii + (size_t)ni * k] : vw;
+        vdwn = jj == 0 ? d.ev_j[ip + (size_t)ni * k] : (ii == ni - 1 ? d.ev_i[jm + (size_t)nj * k] : vwn);
+        vdn = ii == ni - 1 ? d.ev_i[jj + (size_t)nj * k] : x.vn;
+        paw = jj == 0 ? d.ep_j[ii + (size_t)ni * k] : pw;
+      }
+      const float zcor1u = ((coru * dts) * 0.25f) * (((x.cv + vdw) + vdwn) + vdn);
+      un = ((x.cu + zcor1u) - (zfz * hx) * gzh) - (zcx * zrom1u) * (x.cp - paw);
+    }
+    // Equation 18
+    {
+      const float zcy = rot ? dtrdy : dtrdy * mv;
+      const float zfz = egdts + 0.25f * (((x.ds0 + x.ds1) + x.cd0) + x.cd1);
+      const float zrom1v = hcpd * (x.ts + x.ct);
+      float uds = x.us, ude = ue, udes = ues, pas = x.ps;
+      if (EDGE) {
+        const int im = wm1(ii, ni), jp = wp1(jj, nj);
+        uds = ii == 0 ? d.eu_i[jj + (size_t)nj * k] : x.us;
+        ude = jj == nj - 1 ? d.eu_j[ii + (size_t)ni * k] : ue;
+        udes = jj == nj - 1 ? d.eu_j[im + (size_t)ni * k] : (ii == 0 ? d.eu_i[jp + (size_t)nj * k] : ues);
+        pas = ii == 0 ? d.ep_i[jj + (size_t)nj * k] : x.ps;
+      }
+      const float zcor1v = ((corv * dts) * 0.25f) * (((x.cu + uds) + ude) + udes);
+      vnew = ((x.cv - zcor1v) - (zfz * hy) * gzh) - (zcy * zrom1v) * (x.cp - pas);
+    }
+  };
+  auto row = [&](const int i, auto edge) {
+    issue(i + kMom2S - 2, qi);   // into the slot of row i-2
+    cp_async_wait<kMom2S - 3>();  // rows up to i+1 have landed
+    c2 = n2;
+    if (i + 1 < i_e) load2(i + 1, n2);
+    auto lds2 = [&](int q, int a) { return *reinterpret_cast<const float2*>(&rg[q][a][2 * lane]); };
+    const float2 cu = lds2(qc, 0), cv = lds2(qc, 1), ct = lds2(qc, 2), cp = lds2(qc, 3);
+    const float2 cd0 = lds2(qc, 4), cd1 = lds2(qc, 5);
+    const float2 us = lds2(qb, 0), ts = lds2(qb, 2), ps = lds2(qb, 3), ds0 = lds2(qb, 4), ds1 = lds2(qb, 5);
+    const float2 vn = lds2(qn, 1);
+    // east neighbours of the second column: the next lane's first
+    const float ue1 = __shfl_down_sync(0xffffffffu, cu.x, 1);
+    const float ues1 = __shfl_down_sync(0xffffffffu, us.x, 1);
+    // west neighbours of the first column: the previous lane's second
+    const float vw0 = __shfl_up_sync(0xffffffffu, cv.y, 1);
+    const float vwn0 = __shfl_up_sync(0xffffffffu, vn.y, 1);
+    const float tw0 = __shfl_up_sync(0xffffffffu, ct.y, 1);
+    const float pw0 = __shfl_up_sync(0xffffffffu, cp.y, 1);
+    const float dw0w0 = __shfl_up_sync(0xffffffffu, cd0.y, 1);
+    const float dw1w0 = __shfl_up_sync(0xffffffffu, cd1.y, 1);
+    const Col xa{cu.x, cv.x, ct.x, cp.x, cd0.x, cd1.x, us.x, ts.x, ps.x, ds0.x, ds1.x, vn.x};
+    const Col xb{cu.y, cv.y, ct.y, cp.y, cd0.y, cd1.y, us.y, ts.y, ps.y, ds0.y, ds1.y, vn.y};
+    float ua = 0.f, va = 0.f, ub = 0.f, vb = 0.f;
+    if (out0)
+      point(ja, i, xa, vw0, vwn0, tw0, pw0, dw0w0, dw1w0, cu.y, us.y, c2.coru.x, c2.corv.x, c2.hx.x, c2.hy.x,
+            c2.mu.x, c2.mv.x, edge, ua, va);
+    if (out1)
+      point(jb, i, xb, cv.x, vn.x, ct.x, cp.x, cd0.x, cd1.x, ue1, ues1, c2.coru.y, c2.corv.y, c2.hx.y, c2.hy.y,
+            c2.mu.y, c2.mv.y, edge, ub, vb);
+    const size_t c = (size_t)ja + (size_t)nj * i;
+    if (out0 && out1) {
+      *reinterpret_cast<float2*>(uo + c) = make_float2(ua, ub);
+      *reinterpret_cast<float2*>(vo + c) = make_float2(va, vb);
+    } else if (out0) {
+      uo[c] = ua;
+      vo[c] = va;
+    } else if (out1) {
+      uo[c + 1] = ub;
+      vo[c + 1] = vb;
+    }
+    qb = qc; qc = qn; qn = nxt(qn); qi = nxt(qi);
+  };
+  if (interior)
+    for (int i = i_s; i < i_e; ++i) row(i, std::false_type());
+  else
+    for (int i = i_s; i < i_e; ++i) row(i, std::true_type());
+  cp_async_wait<0>();  // no copy outlives the kernel
+}
+
+__global__ void __launch_bounds__(128, 5) k_momentum_strip2(View<float> d, int R) {
+  __shared__ __align__(16) Mom2Slots ring[4];
+  b_momentum_strip2(d, blockIdx.x, blockIdx.y, R, ring[threadIdx.x >> 5], threadIdx.x >> 5, 4);
+}
+
 // ---- divergence + divdamp as warp strips (:514-597, :853-895, :627-630) ---
 // The work of k_sound_div and k_sound_damp in one pass.  One warp per strip
 // of kDDJ output columns x R rows of one level k, lanes on columns
@@ -1487,12 +1656,14 @@ __device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, c
 }
 
 // Blocks per SM by bulk type and fields per thread.  FP32, one field per
-// thread: 14 (32 registers, a few spilled), 1.58 against 1.79 ms per step at
-// the 10 blocks that 48 registers allow; the other variants keep the
-// occupancy of their unconstrained register counts.
+// thread: 12 (40 registers, 32 to 64 bytes spilled per field-group path):
+// 1.88 ms per step at 512 x 512 x 60, against 1.99 at 14 blocks (32
+// registers, several hundred bytes spilled by the groups that form ux, vx,
+// wx) and 2.08 at 10 (48 registers); the other variants keep the occupancy
+// of their unconstrained register counts.
 template <class T, int F>
 constexpr int vert_min_blocks() {
-  if (sizeof(T) == 4) return F == 1 ? 14 : F == 2 ? 9 : F == 5 ? 5 : 3;
+  if (sizeof(T) == 4) return F == 1 ? 12 : F == 2 ? 9 : F == 5 ? 5 : 3;
   return F == 1 ? 6 : F == 2 ? 4 : F == 5 ? 2 : 1;
 }
 
@@ -2137,7 +2308,16 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       if (!staged) MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, k_sound_column<T><<<cg, cb, 0, st>>>(d, ns, last, 0));
       ++n;
     }
-    if (d.kmarch & 8) {
+    bool pairs = false;
+    if constexpr (sizeof(T) == 4) {
+      if ((d.kmarch & 8) && (d.kmarch & 64) && d.nj % 2 == 0) {  // two columns per lane
+        const int nstrips = ((d.nj + 1 + kMom2J - 1) / kMom2J) * ((d.ni + kMomR - 1) / kMomR);
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip2<<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
+        pairs = true;
+      }
+    }
+    if (pairs) {
+    } else if (d.kmarch & 8) {
       const int nstrips = ((d.nj + kMomJ - 1) / kMomJ) * ((d.ni + kMomR - 1) / kMomR);
       MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
     } else if (d.kmarch & 4)

@@ -246,8 +246,11 @@ const char* moloch_gpu_kernel_name(int kind);
  *               one warp-strip kernel (29 columns x 32 rows; overrides 1
  *               and 2), 32 the implicit-w column solve staged by TMA with
  *               its column state in TMEM (FP32 storage, jx a multiple of 4,
- *               kz <= 64; elsewhere the bit is ignored); 0 = one level per
- *               thread;
+ *               kz <= 64; elsewhere the bit is ignored), 64 (with 8) the
+ *               momentum strips with two columns per lane (62 columns x 32
+ *               rows per warp, 8-byte copies; FP32 storage, jx even;
+ *               elsewhere, and in ensembles, the one-column strips); 0 =
+ *               one level per thread;
  *   choice[2] = advected fields per thread of the vertical WAF kernel:
  *               1, 2, 5 or 10 (the fields of a thread share the velocity
  *               loads and terms).
