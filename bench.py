@@ -267,7 +267,7 @@ def time_steps(torch, d, stream, steps, graph=True):
     return e0.elapsed_time(e1), d.kernel_count - k0
 
 
-def e2e_steps(torch, dm, d, stream, steps, warmup=3):
+def e2e_steps(torch, dm, d, stream, steps, warmup=3, reps=3):
     """Through the reference-facing C ABI with host arrays, as a driver time
     loop does it: every step uploads the prognostic state (u, v, w, pai, t,
     qx), runs one moloch() call and reads back the output fields t and ps
@@ -293,26 +293,41 @@ def e2e_steps(torch, dm, d, stream, steps, warmup=3):
         d.output_finish(t_out, ps_out)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    d.sync()
-    e0.record(stream)
-    t0 = time.perf_counter()
+    runs = []
     out = None
-    for s in range(steps):
-        for n in names_in:
-            d.upload(n, host[n])
-        d.moloch(s + 1)
-        if s > 0:
-            out = d.output_finish(t_out, ps_out)
-        d.output_start()
-    out = d.output_finish(t_out, ps_out)
-    e1.record(stream)
-    e1.synchronize()
-    wall = time.perf_counter() - t0
+    for rep in range(reps):  # the host side of the copies varies with the machine's other work
+        d.sync()
+        e0.record(stream)
+        t0 = time.perf_counter()
+        for s in range(steps):
+            for n in names_in:
+                d.upload(n, host[n])
+            d.moloch(s + 1)
+            if s > 0:
+                out = d.output_finish(t_out, ps_out)
+            d.output_start()
+        out = d.output_finish(t_out, ps_out)
+        e1.record(stream)
+        e1.synchronize()
+        wall = time.perf_counter() - t0
+        runs.append(max(e0.elapsed_time(e1), 1e3 * wall))
+    # the raw DMA rate from one registered host array in the same process,
+    # for reading a slow run
+    src = torch.from_numpy(host["t"].reshape(-1))
+    dst = torch.empty(src.numel(), dtype=src.dtype, device=torch.device("cuda", torch.cuda.current_device()))
+    dma = 0.0
+    for _ in range(3):
+        with torch.cuda.stream(stream):
+            e0.record(stream)
+            dst.copy_(src, non_blocking=True)
+            e1.record(stream)
+        e1.synchronize()
+        dma = max(dma, src.numel() * src.element_size() / (e0.elapsed_time(e1) / 1e3) / 1e9)
     for a in list(host.values()) + [t_out, ps_out]:
         d.host_unregister(a)
     h2d = sum(host[n].nbytes for n in names_in)
     d2h = out[0].nbytes + out[1].nbytes
-    return max(e0.elapsed_time(e1), 1e3 * wall), h2d, d2h
+    return sorted(runs), h2d, d2h, dma
 
 
 def ensemble_members(dm, stream, n=64, seed=2024):
@@ -659,10 +674,13 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
     e2e = None
     if not args.no_e2e:
         n_e2e = max(2, args.steps)
-        ms_e2e, h2d, d2h = e2e_steps(torch, dm, dsur, stream, n_e2e, args.warmup)
-        ms_e2e = reduce_max(dist, ms_e2e, device)
+        runs, h2d, d2h, dma = e2e_steps(torch, dm, dsur, stream, n_e2e, args.warmup)
+        ms_e2e = reduce_max(dist, runs[len(runs) // 2], device)
         e2e = {"value": n_dom * gp * n_e2e / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": n_e2e,
+               "repeats": "median of %d timed loops of %d steps" % (len(runs), n_e2e),
+               "ms_per_step_runs": [round(r / n_e2e, 3) for r in runs],
+               "h2d_dma_GBps": round(dma, 1),
                "path": "moloch_gpu_upload(u,v,w,pai,t,qx) from registered (pinned) FP64 host arrays + "
                        "moloch_gpu_step + moloch_gpu_output_start/finish(t,ps) into registered arrays, "
                        "FP32 + surrogate handle"}
