@@ -2295,13 +2295,29 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
       bool staged = false;
       if constexpr (sizeof(T) == 4) {
         if (column_tm_ok(d)) {
-          const ColumnMaps& cm = static_cast<const ColumnMaps*>(d.cmaps)[d.fcur];
-          if (last)
-            MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
-                          k_sound_column_tm<T, 1><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(d, cm, ns));
-          else
-            MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
-                          k_sound_column_tm<T, 0><<<column_tm_grid(d), kTmThreads, kTmSmem, st>>>(d, cm, ns));
+          // bits 128 / 256: two words of column state a level, 12 / 16 rows
+          const int cfg = (d.kmarch & 256) ? 2 : (d.kmarch & 128) ? 1 : 0;
+          const ColumnMaps& cm = static_cast<const ColumnMaps*>(d.cmaps)[2 * cfg + d.fcur];
+          const int grid = column_tm_grid(d);
+          if (cfg == 2) {
+            if (last)
+              MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
+                            k_sound_column_tw<T, 1, 16><<<grid, TwCfg<16>::threads, TwCfg<16>::smem, st>>>(d, cm, ns));
+            else
+              MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
+                            k_sound_column_tw<T, 0, 16><<<grid, TwCfg<16>::threads, TwCfg<16>::smem, st>>>(d, cm, ns));
+          } else if (cfg == 1) {
+            if (last)
+              MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
+                            k_sound_column_tw<T, 1, 12><<<grid, TwCfg<12>::threads, TwCfg<12>::smem, st>>>(d, cm, ns));
+            else
+              MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st,
+                            k_sound_column_tw<T, 0, 12><<<grid, TwCfg<12>::threads, TwCfg<12>::smem, st>>>(d, cm, ns));
+          } else if (last) {
+            MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st, k_sound_column_tm<T, 1><<<grid, kTmThreads, kTmSmem, st>>>(d, cm, ns));
+          } else {
+            MOLOCH_LAUNCH(KK_SOUND_COLUMN_TM, st, k_sound_column_tm<T, 0><<<grid, kTmThreads, kTmSmem, st>>>(d, cm, ns));
+          }
           staged = true;
         }
       }

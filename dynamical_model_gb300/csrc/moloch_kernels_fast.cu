@@ -44,11 +44,11 @@ EncodeTiledFn encode_tiled() {
   });
   return fn;
 }
-// dense FP32 field (nj, ni, nk), j fastest, as boxes of 32 x kTmRows x kKCT
-bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, int nk) {
+// dense FP32 field (nj, ni, nk), j fastest, as boxes of 32 x rows x levels
+bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, int nk, int rows, int levels) {
   const cuuint64_t dims[3] = {(cuuint64_t)nj, (cuuint64_t)ni, (cuuint64_t)nk};
   const cuuint64_t strides[2] = {(cuuint64_t)nj * 4, (cuuint64_t)nj * ni * 4};
-  const cuuint32_t box[3] = {32, (cuuint32_t)kTmRows, (cuuint32_t)kKCT};
+  const cuuint32_t box[3] = {32, (cuuint32_t)rows, (cuuint32_t)levels};
   const cuuint32_t es[3] = {1, 1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, es,
             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -56,7 +56,12 @@ bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, i
 }
 }  // namespace
 
-int column_maps_bytes() { return (int)(2 * sizeof(ColumnMaps)); }
+int column_maps_bytes() { return (int)(2 * kColumnMapConfigs * sizeof(ColumnMaps)); }
+
+// the box shapes of the staged column kernels, in the order of the configs
+// (ColumnMaps sets 2 cfg + buffer-set parity)
+static const int kMapRows[kColumnMapConfigs] = {kTmRows, 12, 16};
+static const int kMapLevels[kColumnMapConfigs] = {kKCT, TwCfg<12>::kct, TwCfg<16>::kct};
 
 bool build_column_maps(const View<float>& v, void* out) {
   if (v.kz > kTmMaxKz || v.kz < 2 || v.nj % 4 != 0 || ((uintptr_t)out & 63)) return false;
@@ -66,20 +71,32 @@ bool build_column_maps(const View<float>& v, void* out) {
   std::call_once(attr, [] {
     cudaFuncSetAttribute(k_sound_column_tm<float, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem);
     cudaFuncSetAttribute(k_sound_column_tm<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, kTmSmem);
+    cudaFuncSetAttribute(k_sound_column_tw<float, 0, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TwCfg<12>::smem);
+    cudaFuncSetAttribute(k_sound_column_tw<float, 1, 12>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TwCfg<12>::smem);
+    cudaFuncSetAttribute(k_sound_column_tw<float, 0, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TwCfg<16>::smem);
+    cudaFuncSetAttribute(k_sound_column_tw<float, 1, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TwCfg<16>::smem);
   });
   ColumnMaps* cm = static_cast<ColumnMaps*>(out);
   const int nj = v.nj, ni = v.ni, kz = v.kz;
-  for (int set = 0; set < 2; ++set) {
-    CUtensorMap* m = cm[set].m;
-    const bool ok =
-        map3(fn, &m[CM_W], v.w, nj, ni, kz + 1) && map3(fn, &m[CM_FMZF], v.fmzf, nj, ni, kz + 1) &&
-        map3(fn, &m[CM_QV], v.fset[set][5], nj, ni, kz) && map3(fn, &m[CM_TET], v.fset[set][0], nj, ni, kz) &&
-        map3(fn, &m[CM_PAI], v.fset[set][1], nj, ni, kz) && map3(fn, &m[CM_QSAT], v.qsat, nj, ni, kz) &&
-        map3(fn, &m[CM_ZD], v.zdiv2b, nj, ni, kz) && map3(fn, &m[CM_FMZ], v.fmz, nj, ni, kz) &&
-        map3(fn, &m[CM_T], v.t, nj, ni, kz) && map3(fn, &m[CM_QC], v.fset[set][6], nj, ni, kz) &&
-        map3(fn, &m[CM_QWL], v.qwltot, nj, ni, kz) && map3(fn, &m[CM_QWI], v.qwitot, nj, ni, kz) &&
-        map3(fn, &m[CM_S], v.s, nj, ni, kz + 1);
-    if (!ok) return false;
+  for (int cfg = 0; cfg < kColumnMapConfigs; ++cfg) {
+    const int r = kMapRows[cfg], l = kMapLevels[cfg];
+    for (int set = 0; set < 2; ++set) {
+      CUtensorMap* m = cm[2 * cfg + set].m;
+      const bool ok =
+          map3(fn, &m[CM_W], v.w, nj, ni, kz + 1, r, l) && map3(fn, &m[CM_FMZF], v.fmzf, nj, ni, kz + 1, r, l) &&
+          map3(fn, &m[CM_QV], v.fset[set][5], nj, ni, kz, r, l) &&
+          map3(fn, &m[CM_TET], v.fset[set][0], nj, ni, kz, r, l) &&
+          map3(fn, &m[CM_PAI], v.fset[set][1], nj, ni, kz, r, l) && map3(fn, &m[CM_QSAT], v.qsat, nj, ni, kz, r, l) &&
+          map3(fn, &m[CM_ZD], v.zdiv2b, nj, ni, kz, r, l) && map3(fn, &m[CM_FMZ], v.fmz, nj, ni, kz, r, l) &&
+          map3(fn, &m[CM_T], v.t, nj, ni, kz, r, l) && map3(fn, &m[CM_QC], v.fset[set][6], nj, ni, kz, r, l) &&
+          map3(fn, &m[CM_QWL], v.qwltot, nj, ni, kz, r, l) && map3(fn, &m[CM_QWI], v.qwitot, nj, ni, kz, r, l) &&
+          map3(fn, &m[CM_S], v.s, nj, ni, kz + 1, r, l);
+      if (!ok) return false;
+    }
   }
   return cudaGetLastError() == cudaSuccess;
 }

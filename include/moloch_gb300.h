@@ -249,8 +249,12 @@ const char* moloch_gpu_kernel_name(int kind);
  *               kz <= 64; elsewhere the bit is ignored), 64 (with 8) the
  *               momentum strips with two columns per lane (62 columns x 32
  *               rows per warp, 8-byte copies; FP32 storage, jx even;
- *               elsewhere, and in ensembles, the one-column strips); 0 =
- *               one level per thread;
+ *               elsewhere, and in ensembles, the one-column strips), 128
+ *               or 256 (with 32) the staged column solve with two words of
+ *               column state a level in TMEM and 12 or 16 compute warps
+ *               per SM (the old w and zdiv2b staged again for the
+ *               back-substitution; bit-identical to bit 32 alone; not both,
+ *               and not in ensembles); 0 = one level per thread;
  *   choice[2] = advected fields per thread of the vertical WAF kernel:
  *               1, 2, 5 or 10 (the fields of a thread share the velocity
  *               loads and terms).

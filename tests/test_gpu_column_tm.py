@@ -1,6 +1,7 @@
 """The implicit-w column solve staged by TMA with its column state in TMEM
-(k_sound_column_tm, tuning bit 32, FP32 storage) against the
-one-thread-per-column kernel and the oracle, and its bounded waits.
+(k_sound_column_tm, tuning bit 32, FP32 storage; k_sound_column_tw with
+bit 128 or 256) against the one-thread-per-column kernel and the oracle,
+and its bounded waits.
 
   * Against k_sound_column<float> on the same state: the same FP32/FP64
     arithmetic per level in the same order, so the steps agree to the last
@@ -50,6 +51,32 @@ def test_staged_column_matches_column_kernel(gpu_lib, jx, iy, kz):
     b.close()
 
 
+@pytest.mark.parametrize("rows_bit", [128, 256])
+@pytest.mark.parametrize("jx,iy,kz", [(64, 44, 30), (36, 29, 13), (96, 37, 60), (128, 64, 64), (40, 33, 41)])
+def test_two_word_staged_column_matches_staged(gpu_lib, jx, iy, kz, rows_bit):
+    """k_sound_column_tw (tuning bit 128: 12 compute warps, bit 256: 16;
+    two words of column state a level in TMEM, the old w and zdiv2b staged
+    again for the back-substitution, chunks of 4 levels) against
+    k_sound_column_tm: the same arithmetic per level, so the same bits.
+    Sizes cover partial tiles in both directions, kz not a multiple of the
+    chunk and the largest kz the TMEM columns hold (64)."""
+    a, b = _pair(gpu_lib, jx, iy, kz, 24, ((500.0, jx / 2, iy / 2, 5.0),), u0=6.0, v0=-4.0)
+    a.set_tuning([16, 56])
+    b.set_tuning([16, 56 | rows_bit])
+    for s in (1, 2, 3):
+        a.moloch(s)
+        b.moloch(s)
+    b.run(2, graph=True)
+    a.run(2, graph=True)
+    worst = {n: rel_l2(b.get(n), a.get(n)) for n in FIELDS}
+    same = all(np.array_equal(b.get(n), a.get(n)) for n in FIELDS)
+    print(f"{jx}x{iy}x{kz} two-word ({rows_bit}) vs four-word staged solve: bit-identical {same}",
+          {k: f"{v:.1e}" for k, v in worst.items()})
+    assert all(v <= 1e-6 for v in worst.values()), worst
+    a.close()
+    b.close()
+
+
 def test_staged_column_is_used_only_where_it_fits(gpu_lib):
     """jx not a multiple of 4 (no TMA row stride) and kz > 64 (TMEM full)
     fall back to the one-thread kernel: results identical to it."""
@@ -64,14 +91,15 @@ def test_staged_column_is_used_only_where_it_fits(gpu_lib):
         b.close()
 
 
-def test_staged_column_wait_runs_out(gpu_lib):
+@pytest.mark.parametrize("variant", [56, 56 | 128, 56 | 256])
+def test_staged_column_wait_runs_out(gpu_lib, variant):
     jx, iy, kz = 64, 48, 20
     hills = ((400.0, 32.0, 24.0, 4.0),)
     g = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     ref = gpu_lib.Moloch(jx, iy, kz, mode="fp32_mixed")
     for x in (g, ref):
         x.setup_idealized(hills=hills, u0=4.0)
-        x.set_tuning([16, 56])
+        x.set_tuning([16, variant])
     # each CTA's staged chunk 3 is never issued: the compute warps' wait on
     # it and the loader's wait for that stage to drain both give up after
     # 2e6 cycles (about 1 ms); the kernel reports, drains and returns

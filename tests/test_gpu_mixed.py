@@ -23,7 +23,7 @@ def rmse(a, b):
     return float(np.sqrt(np.mean((np.asarray(a) - np.asarray(b)) ** 2)))
 
 
-@pytest.mark.parametrize("tuning", [[1, 0], [32, 11], [32, 24], [32, 56]])
+@pytest.mark.parametrize("tuning", [[1, 0], [32, 11], [32, 24], [32, 56], [32, 184], [32, 312]])
 def test_mixed_100_steps_vs_oracle(oracle_mod, gpu_lib, tuning):
     """Default kernels, and the FP32 variants the autotuner picks on GB300
     (warp strips for the horizontal WAF and the momentum, k-marching or
