@@ -1341,7 +1341,7 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     h->vf.hz_levels = choice[0];
   }
   if (n > 1) {
-    if (choice[1] < 0 || choice[1] > 511 || (choice[1] & 384) == 384)
+    if (choice[1] < 0 || choice[1] > 1023 || (choice[1] & 384) == 384)
       return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     h->vd.kmarch = choice[1];
     h->vf.kmarch = choice[1];
@@ -1396,8 +1396,9 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
   double best1 = 1e30;
   int pick1 = h->elem == 8 ? h->vd.kmarch : h->vf.kmarch;
   const bool staged_ok = h->elem == 4 && h->vf.cmaps != nullptr;
-  for (int cand = 0; cand < 512; ++cand) {
+  for (int cand = 0; cand < 1024; ++cand) {
     if ((cand & 384) && (!(cand & 32) || (cand & 384) == 384)) continue;  // one staged-column variant
+    if ((cand & 512) && !(cand & 16)) continue;  // levels per warp of the fused strips
     if ((cand & 64) && (h->elem != 4 || !(cand & 8) || h->nj() % 2)) continue;  // two-column strips: FP32, jx even
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both

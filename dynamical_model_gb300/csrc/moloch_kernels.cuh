@@ -1487,6 +1487,187 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 8 : 3)
   b_divdamp_strip<T>(sv, t.y, t.z, R, threadIdx.x >> 5, 4);
 }
 
+// The same strips over NL consecutive levels k0 .. k0+NL-1 per warp
+// (kmarch bit 512, with 16).  The levels of a strip share each row's loads
+// of u and v at the levels between them (NL+2 levels instead of 3 NL), its
+// 2-D metric fields, the east shuffles of those values and the address
+// arithmetic, and s(k) at each inner level is formed once instead of
+// twice (as s(k+1) of the level above and s(k) of the level below: the
+// same sums in the same order, so the same bits).  Per level the
+// arithmetic is that of b_divdamp_strip.
+template <class T, int NL>
+__device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int bx, const int kp, const int R,
+                                                   const int wid, const int nw) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  const int lane = threadIdx.x & 31;
+  const int nj = d.nj, ni = d.ni, kz = d.kz;
+  const size_t pl = d.pl;
+  const int nsj = (nj + kDDJ - 1) / kDDJ, nsi = (ni + R - 1) / R;
+  const int w = bx * nw + wid;
+  if (w >= nsj * nsi) return;  // whole warp
+  const int sj = w % nsj, si = w / nsj;
+  const int jl = sj * kDDJ - 1 + lane;
+  const int jj = wrapn(jl, nj);
+  const bool out_lane = lane >= 1 && lane <= kDDJ && jl < nj;
+  const int i_s = si * R, i_e = min(i_s + R, ni);
+  const int k0 = kp * NL;
+  const T* __restrict__ u = d.ubuf[d.cur];
+  const T* __restrict__ v = d.vbuf[d.cur];
+  T* __restrict__ uo = d.ubuf[d.cur ^ 1];
+  T* __restrict__ vo = d.vbuf[d.cur ^ 1];
+  const bool rot = d.rotllr;
+  const T dtrdx = d.dtrdx, dtrdy = d.dtrdy, dtrdz = d.dtrdz, ddamp2 = d.ddamp2;
+  // level k0-1+l, l = 0 .. NL+1, inside the domain; level k0+l, l < NL
+  bool lin[NL + 2];
+#pragma unroll
+  for (int l = 0; l < NL + 2; ++l) lin[l] = k0 - 1 + l >= 0 && k0 - 1 + l < kz;
+  T cd[NL], gz[NL + 1];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) cd[l] = lin[l + 1] ? d.cdamp[k0 + l] : T(0);
+#pragma unroll
+  for (int l = 0; l <= NL; ++l) gz[l] = (k0 + l >= 1 && k0 + l <= kz - 1) ? d.gzitak[k0 + l] : T(0);
+  // u-part and v-part of a row of this lane's column: u, v at the levels
+  // k0-1 .. k0+NL, rfw, fmz, rfs at k0 .. k0+NL-1
+  struct Ur { T u[NL + 2], rfw[NL], fmz[NL]; T hx, mx, rmu, mu, mv, s0; };
+  struct Vr { T v[NL + 2], rfs[NL]; T rmv, hy; };
+  auto load_u = [&](int i, Ur& x) {
+    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+#pragma unroll
+    for (int l = 0; l < NL + 2; ++l) x.u[l] = lin[l] ? u[c + (size_t)(k0 - 1 + l) * pl] : T(0);
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      x.rfw[l] = lin[l + 1] ? d.rfw[c + (size_t)(k0 + l) * pl] : T(0);
+      x.fmz[l] = lin[l + 1] ? d.fmz[c + (size_t)(k0 + l) * pl] : T(0);
+    }
+    x.hx = d.hx[c]; x.mu = d.mu[c];
+    x.mx = rot ? d.mx[c] : d.mx2[c];
+    x.rmu = rot ? T(0) : d.rmu[c];
+    x.mv = rot ? T(0) : d.mv[c];
+    x.s0 = k0 == 0 ? d.s[c] : T(0);  // s at the top level is never computed here
+  };
+  auto load_v = [&](int i, Vr& x) {
+    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+#pragma unroll
+    for (int l = 0; l < NL + 2; ++l) x.v[l] = lin[l] ? v[c + (size_t)(k0 - 1 + l) * pl] : T(0);
+#pragma unroll
+    for (int l = 0; l < NL; ++l) x.rfs[l] = lin[l + 1] ? d.rfs[c + (size_t)(k0 + l) * pl] : T(0);
+    x.rmv = d.rmv[c]; x.hy = d.hy[c];
+  };
+  // zdiv2a of the levels, s at k0 .. k0+NL (the surface value -ws at kz),
+  // ws when the lowest level is kz-1 (expressions of k_sound_div)
+  struct Zr { T z[NL], s[NL + 1], ws; };
+  auto row_terms = [&](const Ur& a, const Vr& b, const Vr& bn) {
+    T ue[NL + 2];
+#pragma unroll
+    for (int l = 0; l < NL + 2; ++l) ue[l] = __shfl_down_sync(0xffffffffu, a.u[l], 1);
+    T rfw_e[NL];
+#pragma unroll
+    for (int l = 0; l < NL; ++l) rfw_e[l] = __shfl_down_sync(0xffffffffu, a.rfw[l], 1);
+    const T hx_e = __shfl_down_sync(0xffffffffu, a.hx, 1);
+    const T rmu_e = __shfl_down_sync(0xffffffffu, a.rmu, 1);
+    Zr r;
+    r.ws = T(0);
+#pragma unroll
+    for (int l = 0; l <= NL; ++l) {
+      const int kk = k0 + l;  // s(kk) from the levels kk-1 (index l) and kk (index l+1)
+      if (kk == 0) {
+        r.s[l] = a.s0;
+      } else if (kk <= kz - 1) {
+        const T zuh = prod_add(a.u[l + 1] + a.u[l], a.hx, ue[l + 1] + ue[l], hx_e);
+        const T zvh = prod_add(b.v[l + 1] + b.v[l], b.hy, bn.v[l + 1] + bn.v[l], bn.hy);
+        r.s[l] = -((T(0.25) * (zuh + zvh)) * gz[l]);
+      } else if (kk == kz) {  // surface w(kz+1) and s(kz+1) (:536-549)
+        const T zuh = prod_add(a.u[l], a.hx, ue[l], hx_e);
+        const T zvh = prod_add(b.v[l], b.hy, bn.v[l], bn.hy);
+        r.ws = T(0.5) * (zuh + zvh);
+        r.s[l] = -r.ws;
+      } else {
+        r.s[l] = T(0);
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const T uk = a.u[l + 1], uk_e = ue[l + 1];
+      if (rot) {
+        const T du = prod_sub(dtrdx * uk_e, rfw_e[l], dtrdx * uk, a.rfw[l]);
+        const T dv = prod_sub((dtrdy * bn.v[l + 1]) * bn.rfs[l], bn.rmv, (dtrdy * b.v[l + 1]) * b.rfs[l], b.rmv);
+        r.z[l] = (a.fmz[l] * a.mx) * (du + dv);
+      } else {
+        const T du = prod_sub((dtrdx * uk_e) * rmu_e, rfw_e[l], (dtrdx * uk) * a.rmu, a.rfw[l]);
+        const T dv = prod_sub((dtrdy * bn.v[l + 1]) * bn.rmv, bn.rfs[l], (dtrdy * b.v[l + 1]) * b.rmv, b.rfs[l]);
+        r.z[l] = (a.mx * a.fmz[l]) * (du + dv);
+      }
+    }
+    return r;
+  };
+  // prologue: zdiv2a of row i_s-1, all terms of row i_s
+  Ur ua, ub, un;
+  Vr va, vb, vc, vn;
+  load_u(i_s - 1, ua); load_v(i_s - 1, va); load_v(i_s, vb);
+  load_u(i_s, ub); load_v(i_s + 1, vc);
+  const Zr zfirst = row_terms(ua, va, vb);
+  T z_prev[NL];
+#pragma unroll
+  for (int l = 0; l < NL; ++l) z_prev[l] = zfirst.z[l];
+  Zr zcur = row_terms(ub, vb, vc);
+  Ur ucur = ub;
+  Vr vcur = vb;
+  if (i_s + 1 <= i_e) { load_u(i_s + 1, un); load_v(i_s + 2, vn); }
+  for (int i = i_s; i < i_e; ++i) {
+    // in registers: z(i-1); row i (ucur, vcur, zcur); v-part of row i+1 (vc);
+    // in flight: u-part of row i+1 (un), v-part of row i+2 (vn)
+    const Ur unext = un;
+    const Vr vnext = vn;
+    if (i + 2 <= i_e) { load_u(i + 2, un); load_v(i + 3, vn); }
+    const Zr znext = row_terms(unext, vc, vnext);  // row i+1
+    const size_t c = (size_t)jj + (size_t)nj * i;
+#pragma unroll
+    for (int l = 0; l < NL; ++l) {
+      const int k = k0 + l;
+      const T zc = zcur.z[l];
+      const T zw = __shfl_up_sync(0xffffffffu, zc, 1);
+      const T ze = __shfl_down_sync(0xffffffffu, zc, 1);
+      const T zs = z_prev[l], zn = znext.z[l];
+      if (out_lane && k < kz) {
+        const size_t o = (size_t)k * pl;
+        const T u0 = ucur.u[l + 1], v0 = vcur.v[l + 1];
+        if (k > 0) d.s[o + c] = zcur.s[l];
+        if (k == kz - 1) {
+          d.w[c + (size_t)kz * pl] = zcur.ws;
+          d.s[c + (size_t)kz * pl] = -zcur.ws;
+        }
+        if (jj == 0) d.eu_j[i + (size_t)ni * k] = u0;
+        if (i == ni - 1) d.eu_i[jj + (size_t)nj * k] = u0;
+        if (jj == nj - 1) d.ev_j[i + (size_t)ni * k] = v0;
+        if (i == 0) d.ev_i[jj + (size_t)nj * k] = v0;
+        uo[o + c] = u0 + ((cd[l] * ucur.mu) * (zc - zw));
+        if (rot)
+          vo[o + c] = v0 + cd[l] * (zc - zs);
+        else
+          vo[o + c] = v0 + ((cd[l] * ucur.mv) * (zc - zs));
+        const T p2d = prod_sub(T(0.125), ((zw + ze) + zs) + zn, T(0.5), zc);
+        T zd = zc + ddamp2 * p2d;
+        zd = zd + (ucur.fmz[l] * dtrdz) * (zcur.s[l] - zcur.s[l + 1]);
+        d.zdiv2b[o + c] = zd;
+      }
+      z_prev[l] = zc;
+    }
+    zcur = znext;
+    ucur = unext;
+    vcur = vc;
+    vc = vnext;
+  }
+}
+
+// 4 blocks per SM (FP32: 122 registers): 0.167 ms per launch at
+// 512 x 512 x 60 against 0.171 for the one-level strips; 5 blocks (96
+// registers, spills) 0.180
+constexpr int kDDLevels = 2;  // levels per warp of k_divdamp_strip_nl
+template <class T>
+__global__ void __launch_bounds__(128, 4) k_divdamp_strip_nl(View<T> d, int R) {
+  b_divdamp_strip_nl<T, kDDLevels>(d, blockIdx.x, blockIdx.y, R, threadIdx.x >> 5, 4);
+}
+
 // ---- advection: vertical WAF, two passes at dt/2 (:966-1073) ------------
 // wfw(k+1) of one pass from x(max(k-1,1)), x(k), x(k+1), x(min(k+2,kz))
 template <class T>
@@ -2272,7 +2453,11 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
     const int last = ns == fl.nsound;
     if (d.kmarch & 16) {
       const int nstrips = ((d.nj + kDDJ - 1) / kDDJ) * ((d.ni + kDDR - 1) / kDDR);
-      MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
+      const dim3 g2((nstrips + 3) / 4, (d.kz + kDDLevels - 1) / kDDLevels);
+      if (d.kmarch & 512)  // kDDLevels levels per warp
+        MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip_nl<T><<<g2, 128, 0, st>>>(d, kDDR));
+      else
+        MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, k_divdamp_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kDDR));
       d.cur ^= 1;  // the damped u, v are in the other buffer
       ++n;
     } else {

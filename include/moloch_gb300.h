@@ -254,7 +254,10 @@ const char* moloch_gpu_kernel_name(int kind);
  *               column state a level in TMEM and 12 or 16 compute warps
  *               per SM (the old w and zdiv2b staged again for the
  *               back-substitution; bit-identical to bit 32 alone; not both,
- *               and not in ensembles); 0 = one level per thread;
+ *               and not in ensembles), 512 (with 16) the fused
+ *               divergence/damping strips over two levels per warp
+ *               (shared row loads; not in ensembles); 0 = one level per
+ *               thread;
  *   choice[2] = advected fields per thread of the vertical WAF kernel:
  *               1, 2, 5 or 10 (the fields of a thread share the velocity
  *               loads and terms).

@@ -341,16 +341,17 @@ def test_vertical_waf_fields_per_thread_match(gpu_lib, mode, tol, fields):
 
 
 @pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
-@pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8), (9, 16), (13, 24), (10, 20)])
+@pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8), (9, 16), (13, 24), (10, 20),
+                                          (9, 528), (10, 536), (13, 536)])
 def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz, variant):
     """The k-marching divergence/damping/momentum kernels (chunks of 4
     levels, the next level prefetched), the warp-strip momentum kernel
     (30 columns x 32 rows, neighbours by shuffles, stale-halo edge buffers
     on the boundary lanes and rows) and the fused divergence/damping strips
-    (variant bit 16: 29 columns x 32 rows, damped u, v to the other buffer)
-    against the one-level-per-thread kernels: bit for bit in the exact
-    build; kz not a multiple of the chunk, jx and iy not multiples of the
-    strips."""
+    (variant bit 16: 29 columns x 32 rows, damped u, v to the other buffer;
+    with bit 512 over two levels per warp) against the one-level-per-thread
+    kernels: bit for bit in the exact build; kz not a multiple of the
+    chunk (nor of the two levels), jx and iy not multiples of the strips."""
     a = gpu_lib.Moloch(45, 37, kz, mode=mode)
     b = gpu_lib.Moloch(45, 37, kz, mode=mode)
     for g in (a, b):
