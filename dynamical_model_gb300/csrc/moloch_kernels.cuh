@@ -1501,7 +1501,7 @@ __device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int b
   if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   const int lane = threadIdx.x & 31;
   const int nj = d.nj, ni = d.ni, kz = d.kz;
-  const size_t pl = d.pl;
+  const unsigned pl = (unsigned)d.pl;  // 32-bit element offsets: a field holds at most 2^31 points
   const int nsj = (nj + kDDJ - 1) / kDDJ, nsi = (ni + R - 1) / R;
   const int w = bx * nw + wid;
   if (w >= nsj * nsi) return;  // whole warp
@@ -1531,13 +1531,13 @@ __device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int b
   struct Ur { T u[NL + 2], rfw[NL], fmz[NL]; T hx, mx, rmu, mu, mv, s0; };
   struct Vr { T v[NL + 2], rfs[NL]; T rmv, hy; };
   auto load_u = [&](int i, Ur& x) {
-    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+    const unsigned c = (unsigned)jj + (unsigned)nj * (unsigned)wrap2(i, ni);
 #pragma unroll
-    for (int l = 0; l < NL + 2; ++l) x.u[l] = lin[l] ? u[c + (size_t)(k0 - 1 + l) * pl] : T(0);
+    for (int l = 0; l < NL + 2; ++l) x.u[l] = lin[l] ? u[c + (unsigned)(k0 - 1 + l) * pl] : T(0);
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
-      x.rfw[l] = lin[l + 1] ? d.rfw[c + (size_t)(k0 + l) * pl] : T(0);
-      x.fmz[l] = lin[l + 1] ? d.fmz[c + (size_t)(k0 + l) * pl] : T(0);
+      x.rfw[l] = lin[l + 1] ? d.rfw[c + (unsigned)(k0 + l) * pl] : T(0);
+      x.fmz[l] = lin[l + 1] ? d.fmz[c + (unsigned)(k0 + l) * pl] : T(0);
     }
     x.hx = d.hx[c]; x.mu = d.mu[c];
     x.mx = rot ? d.mx[c] : d.mx2[c];
@@ -1546,11 +1546,11 @@ __device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int b
     x.s0 = k0 == 0 ? d.s[c] : T(0);  // s at the top level is never computed here
   };
   auto load_v = [&](int i, Vr& x) {
-    const size_t c = (size_t)jj + (size_t)nj * wrap2(i, ni);
+    const unsigned c = (unsigned)jj + (unsigned)nj * (unsigned)wrap2(i, ni);
 #pragma unroll
-    for (int l = 0; l < NL + 2; ++l) x.v[l] = lin[l] ? v[c + (size_t)(k0 - 1 + l) * pl] : T(0);
+    for (int l = 0; l < NL + 2; ++l) x.v[l] = lin[l] ? v[c + (unsigned)(k0 - 1 + l) * pl] : T(0);
 #pragma unroll
-    for (int l = 0; l < NL; ++l) x.rfs[l] = lin[l + 1] ? d.rfs[c + (size_t)(k0 + l) * pl] : T(0);
+    for (int l = 0; l < NL; ++l) x.rfs[l] = lin[l + 1] ? d.rfs[c + (unsigned)(k0 + l) * pl] : T(0);
     x.rmv = d.rmv[c]; x.hy = d.hy[c];
   };
   // zdiv2a of the levels, s at k0 .. k0+NL (the surface value -ws at kz),
@@ -1620,7 +1620,7 @@ __device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int b
     const Vr vnext = vn;
     if (i + 2 <= i_e) { load_u(i + 2, un); load_v(i + 3, vn); }
     const Zr znext = row_terms(unext, vc, vnext);  // row i+1
-    const size_t c = (size_t)jj + (size_t)nj * i;
+    const unsigned c = (unsigned)jj + (unsigned)nj * (unsigned)i;
 #pragma unroll
     for (int l = 0; l < NL; ++l) {
       const int k = k0 + l;
@@ -1629,12 +1629,12 @@ __device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int b
       const T ze = __shfl_down_sync(0xffffffffu, zc, 1);
       const T zs = z_prev[l], zn = znext.z[l];
       if (out_lane && k < kz) {
-        const size_t o = (size_t)k * pl;
+        const unsigned o = (unsigned)k * pl;
         const T u0 = ucur.u[l + 1], v0 = vcur.v[l + 1];
         if (k > 0) d.s[o + c] = zcur.s[l];
         if (k == kz - 1) {
-          d.w[c + (size_t)kz * pl] = zcur.ws;
-          d.s[c + (size_t)kz * pl] = -zcur.ws;
+          d.w[c + (unsigned)kz * pl] = zcur.ws;
+          d.s[c + (unsigned)kz * pl] = -zcur.ws;
         }
         if (jj == 0) d.eu_j[i + (size_t)ni * k] = u0;
         if (i == ni - 1) d.eu_i[jj + (size_t)nj * k] = u0;
@@ -1718,39 +1718,40 @@ __device__ __forceinline__ float waf_vflux<float>(float s_k1, float dtrdz, float
 template <class T, int F, int G>
 __device__ __forceinline__ void b_waf_vertical_g(const View<T>& d, const int g, const int jj, const int ii) {
   const int nj = d.nj, ni = d.ni, kz = d.kz;
-  const size_t pl = d.pl;
-  const size_t c = jj + (size_t)nj * ii;
+  // element offsets fit in 32 bits (a field holds at most 2^31 points)
+  const unsigned pl = (unsigned)d.pl;
+  const unsigned c = (unsigned)jj + (unsigned)nj * (unsigned)ii;
   const T* src[F];
   T* wz[F];
 #pragma unroll
   for (int u = 0; u < F; ++u) {
     src[u] = d.fset[d.fcur][g * F + u];
-    wz[u] = d.wz + (size_t)(g * F + u) * pl * kz;
+    wz[u] = d.wz + (size_t)(g * F + u) * d.pl * kz;
   }
   const T* __restrict__ s = d.s;
   const T* __restrict__ wafu = d.wafu;
   const T* __restrict__ wafd = d.wafd;
   const T dtrdz = d.dtrdz_a;
   auto xval = [&](const int u, const int kk) -> T {
-    const size_t o = (size_t)kk * pl;
+    const unsigned o = (unsigned)kk * pl;
     if constexpr (G < 0) {
       return src[u][c + o];
     } else {
       const int f = G * F + u;
       T x;
       if (f == 2) {
-        const T* __restrict__ us = d.ubuf[d.cur] + o + (size_t)nj * ii;
+        const T* __restrict__ us = d.ubuf[d.cur] + (o + (unsigned)nj * ii);
         x = T(0.5625) * (us[wp1(jj, nj)] + us[jj]) - T(0.0625) * (us[wp2(jj, nj)] + us[wm1(jj, nj)]);
       } else if (f == 3) {
-        const T* __restrict__ vs = d.vbuf[d.cur] + o + jj;
-        x = T(0.5625) * (vs[(size_t)nj * wp1(ii, ni)] + vs[(size_t)nj * ii]) -
-            T(0.0625) * (vs[(size_t)nj * wp2(ii, ni)] + vs[(size_t)nj * wm1(ii, ni)]);
+        const T* __restrict__ vs = d.vbuf[d.cur] + (o + jj);
+        x = T(0.5625) * (vs[(unsigned)nj * wp1(ii, ni)] + vs[(unsigned)nj * ii]) -
+            T(0.0625) * (vs[(unsigned)nj * wp2(ii, ni)] + vs[(unsigned)nj * wm1(ii, ni)]);
       } else if (f == 4) {
         const T* __restrict__ w = d.w + c;
         if (kk == 0)
           x = T(0.5) * (w[pl] + w[0]);
         else if (kk == kz - 1)
-          x = T(0.5) * (w[(size_t)kz * pl] + w[(size_t)(kz - 1) * pl]);
+          x = T(0.5) * (w[(unsigned)kz * pl] + w[(unsigned)(kz - 1) * pl]);
         else
           x = T(0.5625) * (w[(kk + 1) * pl] + w[kk * pl]) - T(0.0625) * (w[(kk + 2) * pl] + w[(kk - 1) * pl]);
       } else {
@@ -1779,9 +1780,9 @@ __device__ __forceinline__ void b_waf_vertical_g(const View<T>& d, const int g, 
     sD = T(0);
     const int m = t - 2;
     if (FAST || t <= kz) {
-      sD = s[c + (size_t)t * pl];
-      uC = wafu[c + (size_t)(t - 1) * pl];
-      dC = wafd[c + (size_t)(t - 1) * pl];
+      sD = s[c + (unsigned)t * pl];
+      uC = wafu[c + (unsigned)(t - 1) * pl];
+      dC = wafd[c + (unsigned)(t - 1) * pl];
     }
     const int t2 = FAST ? t + 2 : (t + 2 <= kz ? t + 2 : kz);
 #pragma unroll
@@ -1797,7 +1798,7 @@ __device__ __forceinline__ void b_waf_vertical_g(const View<T>& d, const int g, 
       if (FAST || m >= 1) {
         const T ym = (!FAST && m == 1) ? y1[u] : y0[u];
         const T wfw2n = (FAST || m <= kz - 1) ? waf_vflux(sB, dtrdz, ym, y1[u], y2[u], y3[u]) : T(0);
-        wz[u][c + (size_t)(m - 1) * pl] = ((y1[u] - wfw2[u] * uA) + wfw2n * dA) + (sA * uA - sB * dA) * y1[u];
+        wz[u][c + (unsigned)(m - 1) * pl] = ((y1[u] - wfw2[u] * uA) + wfw2n * dA) + (sA * uA - sB * dA) * y1[u];
         wfw2[u] = wfw2n;
       }
     }
@@ -1837,11 +1838,11 @@ __device__ __forceinline__ void b_waf_vertical(const View<T>& d, const int bx, c
 }
 
 // Blocks per SM by bulk type and fields per thread.  FP32, one field per
-// thread: 12 (40 registers, 32 to 64 bytes spilled per field-group path):
-// 1.88 ms per step at 512 x 512 x 60, against 1.99 at 14 blocks (32
-// registers, several hundred bytes spilled by the groups that form ux, vx,
-// wx) and 2.08 at 10 (48 registers); the other variants keep the occupancy
-// of their unconstrained register counts.
+// thread: 12 (40 registers; with 32-bit element offsets about 50 bytes
+// spilled, 128 with 64-bit ones): 1.69 ms per step at 512 x 512 x 60
+// (1.88 with 64-bit offsets), against 1.75 at 13 to 16 blocks, 1.76 at 10
+// (48 registers) and 2.00 at 9 (56 registers, no spills); the other
+// variants keep the occupancy of their unconstrained register counts.
 template <class T, int F>
 constexpr int vert_min_blocks() {
   if (sizeof(T) == 4) return F == 1 ? 12 : F == 2 ? 9 : F == 5 ? 5 : 3;
@@ -2226,16 +2227,17 @@ __device__ __forceinline__ void b_stag_from_x(const View<T>& d, const int bx, co
   int ii = by * kPtBY + threadIdx.y;
   const int nj = d.nj, ni = d.ni, kz = d.kz, kk = bz;
   if (jj >= nj || ii >= ni) return;
-  const size_t pl = d.pl;
-  const size_t o = (size_t)kk * pl;
-  const size_t c = jj + (size_t)nj * ii;
-  const size_t rowj = (size_t)nj * ii;
+  // 32-bit element offsets: a field holds at most 2^31 points
+  const unsigned pl = (unsigned)d.pl;
+  const unsigned o = (unsigned)kk * pl;
+  const unsigned c = (unsigned)jj + (unsigned)nj * (unsigned)ii;
+  const unsigned rowj = (unsigned)nj * (unsigned)ii;
   const T* __restrict__ ux = d.ux;
   const T* __restrict__ vx = d.vx;
   d.ubuf[0][o + c] = T(0.5625) * (ux[o + c] + ux[o + rowj + wm1(jj, nj)]) -
                      T(0.0625) * (ux[o + rowj + wp1(jj, nj)] + ux[o + rowj + wm2(jj, nj)]);
-  d.vbuf[0][o + c] = T(0.5625) * (vx[o + c] + vx[o + jj + (size_t)nj * wm1(ii, ni)]) -
-                     T(0.0625) * (vx[o + jj + (size_t)nj * wp1(ii, ni)] + vx[o + jj + (size_t)nj * wm2(ii, ni)]);
+  d.vbuf[0][o + c] = T(0.5625) * (vx[o + c] + vx[o + jj + (unsigned)nj * wm1(ii, ni)]) -
+                     T(0.0625) * (vx[o + jj + (unsigned)nj * wp1(ii, ni)] + vx[o + jj + (unsigned)nj * wm2(ii, ni)]);
   // w(k), k = 2..kz (1-based) <- wx ; level index kk = k-1 in 1..kz-1
   if (kk >= 1) {
     const T* __restrict__ wx = d.wx;
@@ -2243,7 +2245,7 @@ __device__ __forceinline__ void b_stag_from_x(const View<T>& d, const int bx, co
     if (kk == 1)
       wv = T(0.5) * (wx[c + pl] + wx[c]);
     else if (kk == kz - 1)
-      wv = T(0.5) * (wx[c + (size_t)(kz - 1) * pl] + wx[c + (size_t)(kz - 2) * pl]);
+      wv = T(0.5) * (wx[c + (unsigned)(kz - 1) * pl] + wx[c + (unsigned)(kz - 2) * pl]);
     else
       wv = T(0.5625) * (wx[c + kk * pl] + wx[c + (kk - 1) * pl]) -
            T(0.0625) * (wx[c + (kk + 1) * pl] + wx[c + (kk - 2) * pl]);

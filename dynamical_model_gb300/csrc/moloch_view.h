@@ -113,8 +113,9 @@ struct View {
   int kmarch;      // sound kernel variants, bit mask: 1 divergence, 2 damping, 4 momentum
                    // k-marching; 8 momentum as warp strips; 16 divergence + damping fused;
                    // 32 column solve staged by TMA with its column state in TMEM;
-                   // 64 momentum as TMA-staged k-marching tiles (overrides 4 and 8);
-                   // 128 with 16: the fused divergence/damping as TMA-staged tiles
+                   // 64 with 8: momentum strips with two columns per lane; 128 / 256 with
+                   // 32: two words of column state a level, 12 / 16 compute warps; 512
+                   // with 16: the fused strips over two levels per warp
   int vfields;     // advected fields per thread of k_waf_vertical: 1, 2, 5 or 10
 
   // set when a learned surrogate stands in for sound(): the plain sound
