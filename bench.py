@@ -65,12 +65,24 @@ ALG_WORDS = {
 # from an ncu capture of the kernel, and the grid points of that capture;
 # scaled by the point count to the benchmarked size (traffic grows in
 # proportion: one pass over each array per launch)
-NCU_TRAFFIC = {"k_sound_column": (847.0e6, 384 * 384 * 60), "k_sound_column_tm": (498.7e6, 384 * 384 * 60)}
+NCU_TRAFFIC = {"k_sound_column": (847.0e6, 384 * 384 * 60), "k_sound_column_tm": (498.7e6, 384 * 384 * 60),
+               "k_sound_column_tw12": (531.8e6, 384 * 384 * 60)}
 # sm__pipe_fp64_cycles_active (% of peak, active) from the same captures
 NCU_FP64_PIPE = {"k_sound_column": {"pipe_fp64_active_pct": 35.7, "capture": "384x384x60",
                                     "fp64_operations_per_level": 4},
                  "k_sound_column_tm": {"pipe_fp64_active_pct": 39.0, "capture": "384x384x60",
-                                       "fp64_operations_per_level": 4}}
+                                       "fp64_operations_per_level": 4},
+                 "k_sound_column_tw12": {"pipe_fp64_active_pct": 49.9, "capture": "384x384x60",
+                                         "fp64_operations_per_level": 4}}
+
+
+def column_variant(name, tuning):
+    """The staged column solve the tuning runs under the profile's kernel
+    kind k_sound_column_tm: bit 128 (with 32) the two-word kernel with 12
+    compute warps, bit 256 with 16, else the four-word kernel."""
+    if name != "k_sound_column_tm" or len(tuning) < 2:
+        return name
+    return "k_sound_column_tw12" if tuning[1] & 128 else "k_sound_column_tw16" if tuning[1] & 256 else name
 # the FP64 step's dominant kernels are bound by GB300's FP64 rate, not HBM:
 # their FP64-pipe activity from one-launch ncu captures at 256x256x60
 NCU_FP64_STEP = {"k_waf_vertical": {"pipe_fp64_active_pct": 87.2, "dram_pct": 1.8},
@@ -642,8 +654,9 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
     prof64 = d64.profile_step()
     peak, peak_kind = peaks()
     top = max(prof.items(), key=lambda kv: kv[1][0])
-    tname, (tms, tcount) = top
-    words = ALG_WORDS.get(tname, 0)
+    tkind, (tms, tcount) = top
+    tname = column_variant(tkind, tune_mix)
+    words = ALG_WORDS.get(tkind, 0)
     esz = 4
     alg_bytes = words * esz * gp  # per launch
     avg_ms = tms / max(tcount, 1)

@@ -295,6 +295,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.hz_levels = 1;
   v.kmarch = 0;
   v.vfields = 1;
+  v.srows = kMomR;
   v.sur_skip = nullptr;
   v.cmaps = nullptr;
   v.spin_cycles = kDefaultSpinCycles;
@@ -1325,8 +1326,10 @@ static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
 // [0] horizontal WAF shape, [1] sound kernel variants (bit mask:
 // 1 divergence, 2 damping, 4 momentum k-marching; 8 momentum warp strips;
 // 16 divergence and damping fused in warp strips, which overrides 1 and 2),
-// [2] advected fields per thread of the vertical WAF (1, 2, 5, 10)
-static const int kTuneCount = 3;
+// [2] advected fields per thread of the vertical WAF (1, 2, 5, 10),
+// [3] rows per warp strip of the momentum strips
+static const int kTuneCount = 4;
+static const int kStripRowCandidates[4] = {4, 8, 16, 32};
 static const int kVFieldCandidates[4] = {1, 2, 5, 10};
 static bool valid_vfields(int f) { return f == 1 || f == 2 || f == 5 || f == 10; }
 
@@ -1350,6 +1353,11 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
     if (!valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
     h->vd.vfields = choice[2];
     h->vf.vfields = choice[2];
+  }
+  if (n > 3) {
+    if (choice[3] < 4 || choice[3] > 64) return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
+    h->vd.srows = choice[3];
+    h->vf.srows = choice[3];
   }
   for (int q = 0; q < 2; ++q) {  // launch shapes are baked into captured graphs
     if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
@@ -1443,12 +1451,39 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
     }
     if (tot < best2) { best2 = tot; pick2 = cand; }
   }
+  h->vd.vfields = pick2;
+  h->vf.vfields = pick2;
+  // rows per warp strip of the momentum strips, timed on sound() with the
+  // variants chosen above
+  double best3 = 1e30;
+  int pick3 = h->elem == 8 ? h->vd.srows : h->vf.srows;
+  for (int cand : kStripRowCandidates) {
+    h->vd.srows = cand;
+    h->vf.srows = cand;
+    float ms = 0.f, tot = 0.f;
+    for (int rep = 0; rep < 3; ++rep) {
+      cudaEventRecord(e0, h->stream);
+      int nk = h->elem == 8 ? launch_phase(h, h->vd, 1) : launch_phase(h, h->vf, 1);
+      h->kernels += nk;
+      cudaEventRecord(e1, h->stream);
+      if (cudaEventSynchronize(e1) != cudaSuccess) {
+        cudaEventDestroy(e0); cudaEventDestroy(e1);
+        return fail(MOLOCH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+      }
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep > 0) tot += ms;
+    }
+    if (tot < best3) { best3 = tot; pick3 = cand; }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   choice[0] = pick;
   choice[1] = pick1;
   choice[2] = pick2;
-  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1 / 2.0; best_ms[2] = best2 / 2.0; }
+  choice[3] = pick3;
+  if (best_ms) {
+    best_ms[0] = best / 2.0; best_ms[1] = best1 / 2.0; best_ms[2] = best2 / 2.0; best_ms[3] = best3 / 2.0;
+  }
   return moloch_gpu_set_tuning(h, choice, kTuneCount);
 }
 
@@ -1870,7 +1905,8 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   choice[0] = pick;
   choice[1] = pick1;
   choice[2] = pick2;
-  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; }
+  choice[3] = kMomR;  // the batched momentum strips keep their rows per strip
+  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; best_ms[3] = 0.0; }
   ens_sync_members(e);
   return ens_build(e);
 }

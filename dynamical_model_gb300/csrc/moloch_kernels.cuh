@@ -2514,15 +2514,16 @@ int launch_sound(View<T>& d, cudaStream_t st, const PhaseFlags& fl) {
     bool pairs = false;
     if constexpr (sizeof(T) == 4) {
       if ((d.kmarch & 8) && (d.kmarch & 64) && d.nj % 2 == 0) {  // two columns per lane
-        const int nstrips = ((d.nj + 1 + kMom2J - 1) / kMom2J) * ((d.ni + kMomR - 1) / kMomR);
-        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip2<<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
+        const int nstrips = ((d.nj + 1 + kMom2J - 1) / kMom2J) * ((d.ni + d.srows - 1) / d.srows);
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st,
+                      k_momentum_strip2<<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, d.srows));
         pairs = true;
       }
     }
     if (pairs) {
     } else if (d.kmarch & 8) {
-      const int nstrips = ((d.nj + kMomJ - 1) / kMomJ) * ((d.ni + kMomR - 1) / kMomR);
-      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, kMomR));
+      const int nstrips = ((d.nj + kMomJ - 1) / kMomJ) * ((d.ni + d.srows - 1) / d.srows);
+      MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_momentum_strip<T><<<dim3((nstrips + 3) / 4, d.kz), 128, 0, st>>>(d, d.srows));
     } else if (d.kmarch & 4)
       MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, k_sound_momentum_km<T><<<kg, pb, 0, st>>>(d));
     else

@@ -117,6 +117,7 @@ struct View {
                    // 32: two words of column state a level, 12 / 16 compute warps; 512
                    // with 16: the fused strips over two levels per warp
   int vfields;     // advected fields per thread of k_waf_vertical: 1, 2, 5 or 10
+  int srows;       // rows per warp strip of the momentum strips
 
   // set when a learned surrogate stands in for sound(): the plain sound
   // kernels return at once while *sur_skip == 1 (the surrogate's cycle was

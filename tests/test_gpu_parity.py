@@ -340,6 +340,27 @@ def test_vertical_waf_fields_per_thread_match(gpu_lib, mode, tol, fields):
         assert e <= tol, (n, e)
 
 
+@pytest.mark.parametrize("mode", ["fp64_exact", "fp32_mixed"])
+@pytest.mark.parametrize("variant", [24, 536, 88])
+@pytest.mark.parametrize("rows", [4, 8, 24])
+def test_sound_strip_rows_match(gpu_lib, mode, variant, rows):
+    """The momentum strips with 4, 8 or 24 rows per warp (tuning slot 3)
+    against 32: the same arithmetic at every point, only the partition into
+    strips differs, so the same bits; iy not a multiple of the rows, jx
+    even (the two-column strips of variant 88)."""
+    a = gpu_lib.Moloch(46, 37, 11, mode=mode)
+    b = gpu_lib.Moloch(46, 37, 11, mode=mode)
+    for g in (a, b):
+        g.setup_idealized(hills=((400.0, 22.0, 18.0, 4.0),), u0=6.0, v0=-4.0)
+    a.set_tuning([16, variant, 1, 32])
+    b.set_tuning([16, variant, 1, rows])
+    for s in range(1, 4):
+        a.moloch(s)
+        b.moloch(s)
+    for n in PROG + ("s", "deltaw"):
+        assert np.array_equal(b.get(n), a.get(n)), n
+
+
 @pytest.mark.parametrize("mode,tol", [("fp64_exact", 0.0), ("fp64", 1e-11), ("fp32_mixed", 1e-3)])
 @pytest.mark.parametrize("kz,variant", [(9, 7), (13, 7), (9, 11), (13, 8), (9, 16), (13, 24), (10, 20),
                                           (9, 528), (10, 536), (13, 536)])
