@@ -1503,6 +1503,7 @@ struct moloch_ensemble {
   int hz_levels = 4;
   int kmarch = 0;
   int vfields = 1;
+  int mrows = kMomR;  // rows per momentum warp strip of the one-launch-per-kernel mode
   int cur = 0, fcur = 0;
   long long kernels = 0;
   int kernels_per_step = 0;
@@ -1561,9 +1562,10 @@ void ens_tiles(moloch_ensemble* e) {
       for (int x = 0; x < tj * (kNumAdvected / e->vfields); ++x)
         e->tiles[TK_VERTICAL8].push_back(make_int4(q, x, 2 * y, 0));
     {
-      const int nstrips = ((nj + kMomJ - 1) / kMomJ) * ((ni + kMomR - 1) / kMomR);
+      const int nmstrips = ((nj + kMomJ - 1) / kMomJ) * ((ni + e->mrows - 1) / e->mrows);
       for (int z = 0; z < kz; ++z)
-        for (int x = 0; x < (nstrips + 3) / 4; ++x) e->tiles[TK_MSTRIP].push_back(make_int4(q, x, z, 0));
+        for (int x = 0; x < (nmstrips + 3) / 4; ++x) e->tiles[TK_MSTRIP].push_back(make_int4(q, x, z, 0));
+      const int nstrips = ((nj + kMomJ - 1) / kMomJ) * ((ni + kMomR - 1) / kMomR);  // persistent kernel
       const int ndstrips = ((nj + kDDJ - 1) / kDDJ) * ((ni + kDDR - 1) / kDDR);
       for (int z = 0; z < kz; ++z)
         for (int x = 0; x < (ndstrips + 3) / 4; ++x) e->tiles[TK_DSTRIP].push_back(make_int4(q, x, z, 0));
@@ -1625,6 +1627,7 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     b.hstrip = e->hz_levels >= 16;
     b.kmarch = e->kmarch;
     b.vfields = e->vfields;
+    b.mrows = e->mrows;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
   if (!e->pgrid) {
@@ -1850,6 +1853,32 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
     if (tot < best2) { best2 = tot; pick2 = cand; }
   }
   e->vfields = pick2;
+  // rows per momentum warp strip (when the strips run), timed on whole steps
+  double best3 = 0.0;
+  if (e->kmarch & 8) {
+    best3 = 1e30;
+    int pick3 = e->mrows;
+    for (int cand : kStripRowCandidates) {
+      e->mrows = cand;
+      int rc = ens_build(e);
+      if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
+      float ms = 0.f, tot = 0.f;
+      for (int rep = 0; rep < 2; ++rep) {
+        cudaEventRecord(e0, e->stream);
+        e->kernels += e->elem == 8 ? kfast::blaunch_step(e->bd, e->stream, fl, e->cur, e->fcur)
+                                   : kfast::blaunch_step(e->bf, e->stream, fl, e->cur, e->fcur);
+        cudaEventRecord(e1, e->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+          cudaEventDestroy(e0); cudaEventDestroy(e1);
+          return fail(MOLOCH_ERR_CUDA, "ensemble autotune: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) tot += ms;
+      }
+      if (tot < best3) { best3 = tot; pick3 = cand; }
+    }
+    e->mrows = pick3;
+  }
   // one cooperative launch per step (the persistent kernel) against one
   // launch per kernel, timed on whole steps, when the persistent kernel
   // carries the chosen variants
@@ -1905,8 +1934,8 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   choice[0] = pick;
   choice[1] = pick1;
   choice[2] = pick2;
-  choice[3] = kMomR;  // the batched momentum strips keep their rows per strip
-  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; best_ms[3] = 0.0; }
+  choice[3] = e->mrows;
+  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; best_ms[3] = best3; }
   ens_sync_members(e);
   return ens_build(e);
 }
@@ -1925,6 +1954,10 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
   if (nchoice > 2) {
     if (!valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
     e->vfields = choice[2];
+  }
+  if (nchoice > 3) {
+    if (choice[3] < 4 || choice[3] > 64) return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
+    e->mrows = choice[3];
   }
   return ens_build(e);
 }

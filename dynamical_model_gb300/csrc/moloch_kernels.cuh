@@ -2650,7 +2650,8 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
         MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 0));
       }
       if (b.kmarch & 8)
-        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_momentum_strip<T><<<b.ntiles[TK_MSTRIP], 128, 0, st>>>(V(), b.tiles[TK_MSTRIP], kMomR));
+        MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st,
+                      kb_momentum_strip<T><<<b.ntiles[TK_MSTRIP], 128, 0, st>>>(V(), b.tiles[TK_MSTRIP], b.mrows));
       else if (b.kmarch & 4)
         MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st, kb_sound_momentum_km<T><<<nkc, pb, 0, st>>>(V(), KC));
       else

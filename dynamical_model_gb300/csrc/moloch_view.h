@@ -198,6 +198,7 @@ struct Batch {
   int hstrip = 0;               // horizontal WAF as warp strips (tiles: member, block, level)
   int kmarch = 0;               // k-marching sound kernels on TK_CHUNK tiles (bit mask as View::kmarch)
   int vfields = 1;              // fields per thread of the vertical WAF (TK_VERTICAL tiles follow it)
+  int mrows = kMomR;            // rows per momentum warp strip (TK_MSTRIP tiles follow it)
 };
 
 // launch counts per phase are returned by the launchers so the API can

@@ -263,7 +263,8 @@ const char* moloch_gpu_kernel_name(int kind);
  *               loads and terms);
  *   choice[3] = rows per warp strip of the momentum strips, 4 to 64
  *               (candidates 4, 8, 16, 32: shorter strips put more warps in
- *               flight; ensembles keep 32, and their autotuner returns 32).
+ *               flight; in ensembles the one-launch-per-kernel mode takes
+ *               it, the persistent kernel keeps 32).
  * moloch_gpu_autotune runs advection() and sound() once per candidate and
  * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the
