@@ -457,12 +457,13 @@ def run_accuracy(args, torch, dm, stream):
 def persistent_tuning(choice):
     """The nearest tuning the persistent ensemble kernel carries: horizontal
     WAF tiles (1-8 levels), 1 or 2 vertical-WAF fields per thread, no FP32
-    k-marching momentum."""
+    k-marching momentum, the one-thread column solve."""
     hz, km, vf = choice[0], choice[1], choice[2]
     hz = hz if hz < 16 else 4
     vf = vf if vf in (1, 2) else 1
     if km & 4 and not km & 8:
         km &= ~4
+    km &= ~32  # the staged column solve runs only as its own launch
     return [hz, km, vf]
 
 

@@ -1549,6 +1549,13 @@ void ens_tiles(moloch_ensemble* e) {
         for (int x = 0; x < tj; ++x) e->tiles[TK_POINT].push_back(make_int4(q, x, y, z));
     for (int y = 0; y < (ni + 3) / 4; ++y)
       for (int x = 0; x < tj; ++x) e->tiles[TK_COLUMN].push_back(make_int4(q, x, y, 0));
+    if (e->elem == 4 && e->m[q]->vf.cmaps) {
+      for (int y = 0; y < (ni + kTwRows - 1) / kTwRows; ++y)
+        for (int x = 0; x < tj; ++x) e->tiles[TK_COLTW].push_back(make_int4(q, x, y, 0));
+    } else {
+      for (int y = 0; y < (ni + 3) / 4; ++y)
+        for (int x = 0; x < tj; ++x) e->tiles[TK_COLREST].push_back(make_int4(q, x, y, 0));
+    }
     for (int y = 0; y < (ni + 3) / 4; ++y)
       for (int x = 0; x < tj * (kNumAdvected / e->vfields); ++x) e->tiles[TK_VERTICAL].push_back(make_int4(q, x, y, 0));
     for (int z = 0; z < (kz + kKC - 1) / kKC; ++z)
@@ -1593,6 +1600,13 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
   const int n = (int)e->m.size();
   size_t bytes = 4 * n * sizeof(View<T>);
   for (int t = 0; t < TK_COUNT; ++t) bytes += ((e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255));
+  // the members' tensor maps for the batched staged column solve (FP32
+  // members with maps: jx a multiple of 4, kz <= 64)
+  const size_t set_bytes = (size_t)kfast::column_map_set_bytes();
+  const size_t cm_bytes = 2 * set_bytes * (size_t)n;
+  bool staged = false;
+  for (auto* h : e->m) staged = staged || (e->elem == 4 && h->vf.cmaps != nullptr);
+  bytes += staged ? ((cm_bytes + 255) & ~size_t(255)) : 0;
   // persistent mode: two phase programs, the barrier/queue words, the error word
   const size_t prog_bytes = ((sizeof(persist::Phase) * persist::kMaxPhases + 255) & ~size_t(255));
   const size_t stamp_bytes = sizeof(unsigned long long) * (persist::kMaxPhases + 1);
@@ -1630,6 +1644,17 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
     b.mrows = e->mrows;
     off += (e->tiles[t].size() * sizeof(int4) + 255) & ~size_t(255);
   }
+  b.cmaps = nullptr;
+  if (staged) {  // the 12-row boxes (map config 1) of each member, both parities
+    std::vector<unsigned char> hm(cm_bytes, 0);
+    for (int q = 0; q < n; ++q)
+      if (e->m[q]->vf.cmaps)
+        std::memcpy(hm.data() + 2 * set_bytes * q,
+                    static_cast<const unsigned char*>(e->m[q]->vf.cmaps) + 2 * set_bytes, 2 * set_bytes);
+    CUDA_TRY(cudaMemcpy(p + off, hm.data(), cm_bytes, cudaMemcpyHostToDevice));
+    b.cmaps = p + off;
+    off += (cm_bytes + 255) & ~size_t(255);
+  }
   if (!e->pgrid) {
     int dev = 0, sms = 0;
     CUDA_TRY(cudaGetDevice(&dev));
@@ -1652,6 +1677,8 @@ int ens_upload(moloch_ensemble* e, Batch<T>& b, View<T> moloch_handle::*vm) {
   e->ctl = (persist::Ctl*)(p + off);
   off += (sizeof(persist::Ctl) + 255) & ~size_t(255);
   e->perr = (int*)(p + off);
+  b.kerr = e->perr;
+  b.spin = e->pspin > 0 ? e->pspin : kDefaultSpinCycles;
   off += 256;
   e->pstamps = (unsigned long long*)(p + off);
   CUDA_TRY(cudaMemset(e->perr, 0, sizeof(int)));
@@ -1808,9 +1835,12 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   const PhaseFlags fl = flags_of(e->m[0]);
   double best1 = 1e30;
   int pick1 = e->kmarch;
-  for (int cand = 0; cand < 32; ++cand) {
+  bool staged_ok = false;
+  for (auto* h : e->m) staged_ok = staged_ok || (e->elem == 4 && h->vf.cmaps != nullptr);
+  for (int cand = 0; cand < 64; ++cand) {
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both
+    if ((cand & 32) && !staged_ok) continue;  // batched staged column solve: FP32 members with tensor maps
     e->kmarch = cand;
     int rc = ens_build(e);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
@@ -1948,7 +1978,7 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
     e->hz_levels = choice[0];
   }
   if (nchoice > 1) {
-    if (choice[1] < 0 || choice[1] > 31) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+    if (choice[1] < 0 || choice[1] > 63) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
     e->kmarch = choice[1];
   }
   if (nchoice > 2) {
@@ -2070,7 +2100,8 @@ int moloch_gpu_ensemble_sync(moloch_ensemble_t* e) {
     CUDA_TRY(cudaMemcpy(&v, e->perr, sizeof(int), cudaMemcpyDeviceToHost));
     if (v) {
       CUDA_TRY(cudaMemset(e->perr, 0, sizeof(int)));
-      return fail(MOLOCH_ERR_TIMEOUT, "a grid-barrier wait of the persistent ensemble kernel gave up; "
+      return fail(MOLOCH_ERR_TIMEOUT, "a bounded wait of an ensemble kernel gave up (a grid barrier of the "
+                                      "persistent kernel or a staged copy of the batched column solve); "
                                       "the steps since the last sync did not complete");
     }
   }

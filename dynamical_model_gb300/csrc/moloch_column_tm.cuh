@@ -420,14 +420,40 @@ struct TwCfg {
   static_assert(ROWS % 4 == 0 && (ROWS / 4) * bank <= 512, "TMEM holds 512 columns a lane");
 };
 
-template <class T, int LAST, int ROWS>
-__global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
-    k_sound_column_tw(View<T> d, const __grid_constant__ ColumnMaps maps, int nsound) {
+// The arrays and scalars of the domain a column tile belongs to
+template <class T>
+struct TwDom {
+  const T *zdiv2b, *fmz, *qsat, *ffilt;
+  T *w, *deltaw, *tetav, *pai, *s, *ep_j, *ep_i;
+  int nj, ni, kz;
+  size_t pl;
+  T zcs2, dts, egdts, dtrdz;
+};
+template <class T>
+__device__ __forceinline__ TwDom<T> tw_dom(const View<T>& d) {
+  TwDom<T> v;
+  v.zdiv2b = d.zdiv2b; v.fmz = d.fmz; v.qsat = d.qsat; v.ffilt = d.ffilt;
+  v.w = d.w; v.deltaw = d.deltaw; v.tetav = d.tetav; v.pai = d.pai; v.s = d.s; v.ep_j = d.ep_j; v.ep_i = d.ep_i;
+  v.nj = d.nj; v.ni = d.ni; v.kz = d.kz; v.pl = d.pl;
+  v.zcs2 = d.zcs2; v.dts = d.dts; v.egdts = d.egdts; v.dtrdz = d.dtrdz;
+  return v;
+}
+
+// The body of k_sound_column_tw (one domain: BATCH false, the tiles of
+// that domain computed from the tile number) and of kb_sound_column_tw
+// (an ensemble: BATCH true, tile t is tiles[t] = {member, tile x, tile y},
+// the member's view in views[member] and its tensor maps in
+// cms[2 member + fcur]).  A CTA walks tiles blockIdx.x, + gridDim.x, ...;
+// the producer and the compute warps count the same jobs (the chunks of
+// each tile, which depend on the tile's kz).
+template <class T, int LAST, int ROWS, bool BATCH>
+__device__ __forceinline__ void column_tw_body(const View<T>* views, const ColumnMaps* cms, const int4* tiles,
+                                               int ntiles_in, int fcur, int nsound, int* kerr, long long lim,
+                                               int skip_job) {
   using C = TwCfg<ROWS>;
   constexpr int KC = C::kct, NST = C::stages, SLOTF = C::slot_bytes / 4;
   constexpr bool last = LAST != 0;  // the last substep also completes s (Equation 10)
   static_assert(sizeof(T) == 4, "FP32 storage only");
-  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
   extern __shared__ uint8_t smem_raw[];
   __shared__ uint64_t full[NST], empty[NST];
   __shared__ uint32_t tmem_base;
@@ -436,15 +462,18 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
   __shared__ float s_ff[kTmMaxKz];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 127) & ~(uintptr_t)127);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int nj = d.nj, ni = d.ni, kz = d.kz;
-  const size_t pl = d.pl;
-  const int nbx = (nj + 31) / 32, nby = (ni + ROWS - 1) / ROWS, ntiles = nbx * nby;
-  const int nd = (kz - 1 + KC - 1) / KC;  // down-sweep chunks: kk = kz-1 .. 1
-  const int nu = (kz + KC - 1) / KC;      // back-substitution chunks: kk = 1 .. kz
-  const int jpt = nd + nu;                // jobs per tile
-  const int my_tiles = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
-  const int njobs = my_tiles * jpt;
-  const long long lim = d.spin_cycles;
+  // one domain: tiles of nbx x nby
+  const int nbx1 = BATCH ? 1 : (views[0].nj + 31) / 32;
+  const int ntiles = BATCH ? ntiles_in : nbx1 * ((views[0].ni + ROWS - 1) / ROWS);
+  struct Tile { int m, x, y; };
+  auto tile_of = [&](int t) -> Tile {
+    if constexpr (BATCH) {
+      const int4 q = tiles[t];
+      return {q.x, q.y * 32, q.z * ROWS};
+    } else {
+      return {0, (t % nbx1) * 32, (t / nbx1) * ROWS};
+    }
+  };
 
   if (warp == 0) tc::tmem_alloc(&tmem_base, 512);
   if (tid == 32 * ROWS) {
@@ -457,7 +486,8 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
     s_consumed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int k = tid; k < kz; k += blockDim.x) s_ff[k] = d.ffilt[k];
+  if constexpr (!BATCH)
+    for (int k = tid; k < views[0].kz; k += blockDim.x) s_ff[k] = views[0].ffilt[k];
   tc::tc_fence_before();
   __syncthreads();
   tc::tc_fence_after();
@@ -468,64 +498,73 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
     if (lane == 0) {
       const uint64_t keep = tc::policy_evict_last(), once = tc::policy_evict_first();
       const uint32_t down_bytes = 9u * C::slot_bytes, up_bytes = (last ? 11u : 9u) * C::slot_bytes;
-      for (int g = 0; g < njobs; ++g) {
-        const int q = g % NST;
-        if (g >= NST && !tc::mbar_wait_cycles(&empty[q], ((g / NST) - 1) & 1, lim)) {
-          s_fail = 1;
-          break;
-        }
-        if (*(volatile int*)&s_fail) break;
-        if (g == d.fault_skip_job) continue;  // test hook: leave this job unissued
-        const int t = (int)blockIdx.x + (g / jpt) * (int)gridDim.x, c = g % jpt;
-        const int x = (t % nbx) * 32, y = (t / nbx) * ROWS;
-        uint8_t* stg = smem + q * C::stage_bytes;
-        auto box = [&](int slot, int map, int z, uint64_t pol) {
-          tc::tma_load_3d_hint(stg + slot * C::slot_bytes, &maps.m[map], x, y, z, &full[q], pol);
-        };
-        if (c < nd) {
-          const int kk_lo = kz - 1 - c * KC - (KC - 1);
-          tc::mbar_arrive_expect_tx(&full[q], down_bytes);
-          // level kk of w, fmzf, qv and level kk-1 of the others share a
-          // slot index; w, qv, tetav, pai, zdiv2b, fmz are read again by the
-          // back-substitution and stay in L2
-          box(0, CM_W, kk_lo, keep);
-          box(1, CM_FMZF, kk_lo, once);
-          box(2, CM_QV, kk_lo, keep);
-          box(3, CM_TET, kk_lo - 1, keep);
-          box(4, CM_PAI, kk_lo - 1, keep);
-          box(5, CM_QSAT, kk_lo - 1, once);
-          box(6, CM_ZD, kk_lo - 1, keep);
-          box(7, CM_FMZ, kk_lo - 1, keep);
-          box(8, CM_T, kk_lo - 1, once);
-        } else {
-          // levels m = m0 .. m0+KC-1 of the arrays of the update, level m+1
-          // of the old w
-          const int m0 = (c - nd) * KC;
-          tc::mbar_arrive_expect_tx(&full[q], up_bytes);
-          box(0, CM_FMZ, m0, once);
-          box(1, CM_QV, m0, once);
-          box(2, CM_TET, m0, once);
-          box(3, CM_PAI, m0, once);
-          box(4, CM_QC, m0, once);
-          box(5, CM_QWL, m0, once);
-          box(6, CM_QWI, m0, once);
-          box(7, CM_W, m0 + 1, once);
-          box(8, CM_ZD, m0, once);
-          if (last) {
-            box(9, CM_S, m0, once);
-            box(10, CM_FMZF, m0, once);
+      int g = 0;
+      bool stop = false;
+      for (int t = (int)blockIdx.x; t < ntiles && !stop; t += (int)gridDim.x) {
+        const Tile tl = tile_of(t);
+        const int kz = views[tl.m].kz;
+        const int nd = (kz - 1 + KC - 1) / KC, jpt = nd + (kz + KC - 1) / KC;
+        const CUtensorMap* mp = (BATCH ? cms[2 * tl.m + fcur] : cms[0]).m;
+        for (int c = 0; c < jpt; ++c, ++g) {
+          const int q = g % NST;
+          if (g >= NST && !tc::mbar_wait_cycles(&empty[q], ((g / NST) - 1) & 1, lim)) {
+            s_fail = 1;
+            stop = true;
+            break;
           }
+          if (*(volatile int*)&s_fail) {
+            stop = true;
+            break;
+          }
+          if (g == skip_job) continue;  // test hook: leave this job unissued
+          uint8_t* stg = smem + q * C::stage_bytes;
+          auto box = [&](int slot, int map, int z, uint64_t pol) {
+            tc::tma_load_3d_hint(stg + slot * C::slot_bytes, &mp[map], tl.x, tl.y, z, &full[q], pol);
+          };
+          if (c < nd) {
+            const int kk_lo = kz - 1 - c * KC - (KC - 1);
+            tc::mbar_arrive_expect_tx(&full[q], down_bytes);
+            // level kk of w, fmzf, qv and level kk-1 of the others share a
+            // slot index; w, qv, tetav, pai, zdiv2b, fmz are read again by
+            // the back-substitution and stay in L2
+            box(0, CM_W, kk_lo, keep);
+            box(1, CM_FMZF, kk_lo, once);
+            box(2, CM_QV, kk_lo, keep);
+            box(3, CM_TET, kk_lo - 1, keep);
+            box(4, CM_PAI, kk_lo - 1, keep);
+            box(5, CM_QSAT, kk_lo - 1, once);
+            box(6, CM_ZD, kk_lo - 1, keep);
+            box(7, CM_FMZ, kk_lo - 1, keep);
+            box(8, CM_T, kk_lo - 1, once);
+          } else {
+            // levels m = m0 .. m0+KC-1 of the arrays of the update, level
+            // m+1 of the old w
+            const int m0 = (c - nd) * KC;
+            tc::mbar_arrive_expect_tx(&full[q], up_bytes);
+            box(0, CM_FMZ, m0, once);
+            box(1, CM_QV, m0, once);
+            box(2, CM_TET, m0, once);
+            box(3, CM_PAI, m0, once);
+            box(4, CM_QC, m0, once);
+            box(5, CM_QWL, m0, once);
+            box(6, CM_QWI, m0, once);
+            box(7, CM_W, m0 + 1, once);
+            box(8, CM_ZD, m0, once);
+            if (last) {
+              box(9, CM_S, m0, once);
+              box(10, CM_FMZF, m0, once);
+            }
+          }
+          s_last_job[q] = g;
         }
-        s_last_job[q] = g;
       }
     }
   } else {
-    // ---- compute warps: warp w holds row i = ROWS by + w of the tile, lane
-    // = j; its TMEM: lane quarter w % 4, columns 128 (w / 4) .., 2 per level
+    // ---- compute warps: warp w holds row i = y + w of the tile, lane = j;
+    // its TMEM: lane quarter w % 4, columns 128 (w / 4) .., 2 per level
     const uint32_t trow = tbase + ((uint32_t)((warp & 3) * 32) << 16) + (uint32_t)((warp >> 2) * C::bank);
     const uint64_t once = tc::policy_evict_first();
     const T ns = T(nsound), ns1 = T(nsound - 1);
-    const T zcs2 = d.zcs2, dts = d.dts, egdts = d.egdts, dtrdz = d.dtrdz;
     const T rdrcv = T(kRdrcv);
     int g = 0;  // job counter, in the producer's order
     bool fail = false;
@@ -551,30 +590,42 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
     // qsat and the surface w (columns outside the domain read column 0)
     struct Init { T zd, tk, pk, fk, qsk, wsurf; };
     auto load_init = [&](int t, Init& v) {
-      const int jj = (t % nbx) * 32 + lane, ii = (t / nbx) * ROWS + warp;
-      const size_t c = (jj < nj && ii < ni) ? (size_t)jj + (size_t)nj * ii : 0;
-      const size_t o = (size_t)(kz - 1) * pl;
-      v.zd = d.zdiv2b[c + o]; v.tk = d.tetav[c + o]; v.pk = d.pai[c + o]; v.fk = d.fmz[c + o];
-      v.qsk = d.qsat[c + o]; v.wsurf = d.w[c + (size_t)kz * pl];
+      const Tile tl = tile_of(t);
+      const TwDom<T> dm = tw_dom(views[tl.m]);
+      const int jj = tl.x + lane, ii = tl.y + warp;
+      const size_t c = (jj < dm.nj && ii < dm.ni) ? (size_t)jj + (size_t)dm.nj * ii : 0;
+      const size_t o = (size_t)(dm.kz - 1) * dm.pl;
+      v.zd = dm.zdiv2b[c + o]; v.tk = dm.tetav[c + o]; v.pk = dm.pai[c + o]; v.fk = dm.fmz[c + o];
+      v.qsk = dm.qsat[c + o]; v.wsurf = dm.w[c + (size_t)dm.kz * dm.pl];
     };
     Init nx{};
-    if (my_tiles > 0) load_init((int)blockIdx.x, nx);
-    const int nfull = (kz - 1) / KC;  // back-substitution chunks whose levels all lie below kz
+    if ((int)blockIdx.x < ntiles) load_init((int)blockIdx.x, nx);
 
-    for (int tl = 0; tl < my_tiles && !fail; ++tl) {
-      const int t = (int)blockIdx.x + tl * (int)gridDim.x;
-      const int jj = (t % nbx) * 32 + lane, ii = (t / nbx) * ROWS + warp;
+    for (int t = (int)blockIdx.x; t < ntiles && !fail; t += (int)gridDim.x) {
+      const Tile tl = tile_of(t);
+      const TwDom<T> v = tw_dom(views[tl.m]);
+      const int nj = v.nj, ni = v.ni, kz = v.kz;
+      const size_t pl = v.pl;
+      const T zcs2 = v.zcs2, dts = v.dts, egdts = v.egdts, dtrdz = v.dtrdz;
+      const int nd = (kz - 1 + KC - 1) / KC;  // down-sweep chunks: kk = kz-1 .. 1
+      const int nu = (kz + KC - 1) / KC;      // back-substitution chunks: kk = 1 .. kz
+      const int nfull = (kz - 1) / KC;        // back-substitution chunks whose levels all lie below kz
+      const int jj = tl.x + lane, ii = tl.y + warp;
       const bool own = jj < nj && ii < ni;
       const size_t c = own ? (size_t)jj + (size_t)nj * ii : 0;
       T zd_k = nx.zd, tk = nx.tk, pk = nx.pk, fk = nx.fk, qsk = nx.qsk;
       const T wsurf = nx.wsurf;
       float wkp1 = wsurf;
       double cwp1 = 1.0;  // 1 - wwkw(kz+1)
+      auto ffilt = [&](int kk) -> T {
+        if constexpr (BATCH) return v.ffilt[kk];
+        else return s_ff[kk];
+      };
 
       // one level kk of the down-sweep from slot index q; the record of
       // level kk (wp, ww) goes to rec[0..1]
       auto dn_level = [&](const float* st, const int q, const int kk, uint32_t* rec) {
-        const T wk = S_(st, 0, q), fz = S_(st, 1, q), qvk = S_(st, 2, q), ff = s_ff[kk];
+        const T wk = S_(st, 0, q), fz = S_(st, 1, q), qvk = S_(st, 2, q), ff = ffilt(kk);
         const T tkm = S_(st, 3, q), pkm = S_(st, 4, q), qskm = S_(st, 5, q), zd_km = S_(st, 6, q);
         const T fkm = S_(st, 7, q), tm = S_(st, 8, q);
         T zrom1w = ((T(0.5) * T(kCpd)) * fz) * (tkm + tk);
@@ -620,7 +671,7 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
       if (fail) break;
       tc::tmem_wait_st();
       // the next tile's starting values, loaded while this one finishes
-      if (tl + 1 < my_tiles) load_init(t + (int)gridDim.x, nx);
+      if (t + (int)gridDim.x < ntiles) load_init(t + (int)gridDim.x, nx);
 
       // (c) back-substitution (:681-686) fused with the Exner/theta update
       // of the level above (:690-728); w(1) = 0 always (init_moloch :260-262).
@@ -631,11 +682,11 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
       T wlo = T(0);
       uint32_t cur[2 * KC], nxt[2 * KC];
       if (nfull > 0) tc::tmem_ld8p(trow + 2u, nxt);
-      T* __restrict__ pw = d.w + c;
-      T* __restrict__ pdw = d.deltaw + c;
-      T* __restrict__ ptet = d.tetav + c;
-      T* __restrict__ ppai = d.pai + c;
-      T* __restrict__ psv = d.s + c;
+      T* __restrict__ pw = v.w + c;
+      T* __restrict__ pdw = v.deltaw + c;
+      T* __restrict__ ptet = v.tetav + c;
+      T* __restrict__ ppai = v.pai + c;
+      T* __restrict__ psv = v.s + c;
       // level kk (record rec when kk < kz) and the update of level kk-1
       auto up_level = [&](const float* st, const int q, const int kk, const uint32_t* rec) {
         const int m = kk - 1;
@@ -660,8 +711,8 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
           const size_t qm = (size_t)m * pl;
           tc::st_hint(ptet + qm,
                       ftet * (T(1) + (rdrcv * zd) * (prod_add(T(0.25), fqv, T(4.2), fqwl) + T(2.1) * fqwi)), once);
-          if (jj == nj - 1) d.ep_j[ii + (size_t)ni * m] = fpai;
-          if (ii == ni - 1) d.ep_i[jj + (size_t)nj * m] = fpai;
+          if (jj == nj - 1) v.ep_j[ii + (size_t)ni * m] = fpai;
+          if (ii == ni - 1) v.ep_i[jj + (size_t)nj * m] = fpai;
           tc::st_hint(ppai + qm, fpai * (T(1) - rdrcv * zd), once);
           if (last) tc::st_hint(psv + qm, m == 0 ? T(0) : (wlo + S_(st, 9, q)) * S_(st, 10, q), once);  // Eq. 10
         }
@@ -693,7 +744,7 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
         release(g);
       }
       if (fail) break;
-      if (last && own) d.s[c + (size_t)kz * pl] = T(0);
+      if (last && own) v.s[c + (size_t)kz * pl] = T(0);
     }
     // no TMEM load or store of this thread may be in flight when TMEM is
     // freed (a wait that gave up can leave one of either)
@@ -706,7 +757,7 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
   if (tid == 32 * ROWS && s_fail) {
     // a wait gave up: flag it and let the copies still in flight land
     // before the CTA's shared memory is released (bounded)
-    atomicExch(d.kerr, 1);
+    atomicExch(kerr, 1);
     for (int q = 0; q < NST; ++q) {
       const int j = s_last_job[q];
       if (j >= s_consumed) tc::mbar_wait_cycles(&full[q], (j / NST) & 1, lim);
@@ -716,6 +767,24 @@ __global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
   __syncthreads();
   tc::tc_fence_after();
   if (warp == 0) tc::tmem_dealloc(tbase, 512);
+}
+
+template <class T, int LAST, int ROWS>
+__global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
+    k_sound_column_tw(const __grid_constant__ View<T> d, const __grid_constant__ ColumnMaps maps, int nsound) {
+  if (d.sur_skip && *d.sur_skip) return;  // the surrogate took this cycle
+  column_tw_body<T, LAST, ROWS, false>(&d, &maps, nullptr, 0, 0, nsound, d.kerr, d.spin_cycles, d.fault_skip_job);
+}
+
+// An ensemble's column tiles in one persistent launch: the tile table
+// lists (member, tile x, tile y) heaviest member first; cms holds each
+// member's tensor maps for the 12-row boxes, two buffer-set parities per
+// member.  A wait that gives up sets *kerr (the ensemble's error word).
+template <class T, int LAST, int ROWS>
+__global__ void __launch_bounds__(TwCfg<ROWS>::threads, 1)
+    kb_sound_column_tw(const View<T>* __restrict__ views, const ColumnMaps* __restrict__ cms,
+                       const int4* __restrict__ tiles, int ntiles, int fcur, int nsound, int* kerr, long long lim) {
+  column_tw_body<T, LAST, ROWS, true>(views, cms, tiles, ntiles, fcur, nsound, kerr, lim, -1);
 }
 
 }  // namespace MOLOCH_KNS

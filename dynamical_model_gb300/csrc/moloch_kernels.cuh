@@ -2429,7 +2429,8 @@ template <class T>
 inline bool column_tm_ok(const View<T>& d) {
   return sizeof(T) == 4 && (d.kmarch & 32) && d.cmaps != nullptr;
 }
-inline int column_tm_grid(int nj, int ni) {
+// persistent column kernels: one CTA per SM, at most one per tile
+inline int persistent_grid(int ntiles) {
   static int nsm = 0;
   if (!nsm) {
     int dev = 0;
@@ -2437,9 +2438,9 @@ inline int column_tm_grid(int nj, int ni) {
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (nsm <= 0) nsm = 1;
   }
-  const int ntiles = ((nj + 31) / 32) * ((ni + 3) / 4);
   return ntiles < nsm ? ntiles : nsm;
 }
+inline int column_tm_grid(int nj, int ni) { return persistent_grid(((nj + 31) / 32) * ((ni + 3) / 4)); }
 template <class T>
 inline int column_tm_grid(const View<T>& d) { return column_tm_grid(d.nj, d.ni); }
 
@@ -2647,7 +2648,34 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
         MOLOCH_LAUNCH(KK_PAI_UPDATE, st, kb_pai_update<T><<<npt, pb, 0, st>>>(V(), PT));
         n += 2;
       } else {
-        MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 0));
+        bool staged = false;
+        if constexpr (sizeof(T) == 4) {
+          if ((b.kmarch & 32) && b.cmaps) {
+            // the staged column solve over the tiles of the members with
+            // tensor maps, the one-thread kernel over the others
+            using TC = TwCfg<kTwRows>;
+            const int ntw = b.ntiles[TK_COLTW], nrest = b.ntiles[TK_COLREST];
+            const ColumnMaps* cms = static_cast<const ColumnMaps*>(b.cmaps);
+            if (ntw > 0) {
+              const int grid = persistent_grid(ntw);
+              if (last)
+                MOLOCH_LAUNCH(KK_SOUND_COLUMN, st,
+                              kb_sound_column_tw<T, 1, kTwRows><<<grid, TC::threads, TC::smem, st>>>(
+                                  V(), cms, b.tiles[TK_COLTW], ntw, fcur, ns, b.kerr, b.spin));
+              else
+                MOLOCH_LAUNCH(KK_SOUND_COLUMN, st,
+                              kb_sound_column_tw<T, 0, kTwRows><<<grid, TC::threads, TC::smem, st>>>(
+                                  V(), cms, b.tiles[TK_COLTW], ntw, fcur, ns, b.kerr, b.spin));
+            }
+            if (nrest > 0) {
+              MOLOCH_LAUNCH(KK_SOUND_COLUMN, st,
+                            kb_sound_column<T><<<nrest, cb, 0, st>>>(V(), b.tiles[TK_COLREST], ns, last, 0));
+              if (ntw > 0) ++n;
+            }
+            staged = true;
+          }
+        }
+        if (!staged) MOLOCH_LAUNCH(KK_SOUND_COLUMN, st, kb_sound_column<T><<<nco, cb, 0, st>>>(V(), CO, ns, last, 0));
       }
       if (b.kmarch & 8)
         MOLOCH_LAUNCH(KK_SOUND_MOMENTUM, st,

@@ -57,6 +57,7 @@ bool map3(EncodeTiledFn fn, CUtensorMap* m, const float* base, int nj, int ni, i
 }  // namespace
 
 int column_maps_bytes() { return (int)(2 * kColumnMapConfigs * sizeof(ColumnMaps)); }
+int column_map_set_bytes() { return (int)sizeof(ColumnMaps); }
 
 // the box shapes of the staged column kernels, in the order of the configs
 // (ColumnMaps sets 2 cfg + buffer-set parity)
@@ -79,6 +80,10 @@ bool build_column_maps(const View<float>& v, void* out) {
                          TwCfg<16>::smem);
     cudaFuncSetAttribute(k_sound_column_tw<float, 1, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          TwCfg<16>::smem);
+    cudaFuncSetAttribute(kb_sound_column_tw<float, 0, kTwRows>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TwCfg<kTwRows>::smem);
+    cudaFuncSetAttribute(kb_sound_column_tw<float, 1, kTwRows>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         TwCfg<kTwRows>::smem);
   });
   ColumnMaps* cm = static_cast<ColumnMaps*>(out);
   const int nj = v.nj, ni = v.ni, kz = v.kz;

@@ -26,6 +26,8 @@ namespace kfast {
 // bytes, 64-byte aligned); false when the domain does not qualify (kz > 64,
 // jx not a multiple of 4) or the driver cannot encode them
 int column_maps_bytes();
+// bytes of one set of tensor maps (one box shape, one buffer-set parity)
+int column_map_set_bytes();
 bool build_column_maps(const View<float>& v, void* out);
 template <class T> int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& cur, int& fcur);
 template <class T> int blaunch_advection(const Batch<T>& b, cudaStream_t st, int& cur, int& fcur);

@@ -183,12 +183,17 @@ struct KernelTimer {
 // rows high, given as (member, bx, 2 by8, .) so that the 32 x 4 column
 // bodies' row index by * 4 + threadIdx.y covers rows 8 by8 .. 8 by8 + 7, and
 // its strip tiles (TK_MSTRIP8, TK_DSTRIP8) are blocks of 8 warp strips.
+// TK_COLTW tiles are the 32 x kTwRows column tiles of the batched staged
+// column solve, (member, tile x, tile y, .), of the FP32 members with tensor
+// maps (jx a multiple of 4, kz <= 64); TK_COLREST the TK_COLUMN tiles of the
+// other members, which the one-thread column kernel takes beside it.
 constexpr int kKC = 4;
+constexpr int kTwRows = 12;
 constexpr int kMomJ = 30, kMomR = 32;
 constexpr int kDDJ = 29, kDDR = 32;
 enum TileKind {
   TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_DSTRIP,
-  TK_COLUMN8, TK_VERTICAL8, TK_MSTRIP8, TK_DSTRIP8, TK_COUNT
+  TK_COLUMN8, TK_VERTICAL8, TK_MSTRIP8, TK_DSTRIP8, TK_COLTW, TK_COLREST, TK_COUNT
 };
 template <class T>
 struct Batch {
@@ -199,6 +204,13 @@ struct Batch {
   int kmarch = 0;               // k-marching sound kernels on TK_CHUNK tiles (bit mask as View::kmarch)
   int vfields = 1;              // fields per thread of the vertical WAF (TK_VERTICAL tiles follow it)
   int mrows = kMomR;            // rows per momentum warp strip (TK_MSTRIP tiles follow it)
+  // batched staged column solve (FP32 members with tensor maps): device
+  // array of ColumnMaps, two buffer-set parities per member (zeros for the
+  // members without), or nullptr when no member has maps; its bounded waits
+  // report through kerr
+  const void* cmaps = nullptr;
+  int* kerr = nullptr;
+  long long spin = 0;
 };
 
 // launch counts per phase are returned by the launchers so the API can

@@ -179,3 +179,64 @@ def test_persistent_autotune_picks_a_mode(gpu_lib, stream):
     e.close()
     for m in ms:
         m.close()
+
+
+# ---- the staged column solve over all members' tiles ----------------------
+SHAPES_TW = [(40, 33, 16, 3.0, 11), (24, 20, 12, 7.5, 12), (36, 29, 10, 0.5, 13), (64, 48, 61, 5.0, 14)]
+
+
+def members_tw(dm, stream=None):
+    out = []
+    for jx, iy, kz, u0, seed in SHAPES_TW:
+        m = dm.Moloch(jx, iy, kz, mode="fp32_mixed", stream=stream)
+        m.setup_idealized(pert_amp=1.0, pert_levels=kz, seed=seed, u0=u0, v0=0.5 * u0,
+                          hills=((300.0, jx / 2.0, iy / 2.0, 4.0),))
+        out.append(m)
+    return out
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_ensemble_staged_column_matches_members(gpu_lib, stream, graph):
+    """kb_sound_column_tw (tuning bit 32 in an ensemble: one persistent
+    launch over the 32 x 12 column tiles of every member, each member's
+    tensor maps read from device memory) against the members run alone
+    with the single-domain two-word staged solve (bits 32 + 128): the same
+    arithmetic, so the same bits.  Members of uneven jx, iy and kz (partial
+    tiles, kz 10 to 61), four steps (every substep parity and the
+    last-substep path)."""
+    ms = members_tw(gpu_lib, stream=stream.cuda_stream)
+    solo = members_tw(gpu_lib)
+    e = gpu_lib.Ensemble(ms)
+    e.set_tuning([16, 56, 1])
+    e.run(4, graph=graph)
+    e.sync()
+    for m in solo:
+        m.set_tuning([16, 56 | 128, 1])
+        m.run(4, graph=graph)
+        m.sync()
+    same = True
+    for m, s in zip(ms, solo):
+        for f in FIELDS + ("s", "deltaw"):
+            a, b = m.get(f), s.get(f)
+            same = same and np.array_equal(a, b)
+            assert rel_l2(a, b) <= 1e-6, (f, m.jx, m.iy, m.kz)
+    print("batched staged column solve bit-identical to the members alone:", same)
+    e.close()
+    for m in ms + solo:
+        m.close()
+
+
+def test_ensemble_autotune_may_pick_staged_column(gpu_lib, stream):
+    """The ensemble autotuner offers the batched staged column solve when
+    every member has tensor maps, and the chosen tuning runs."""
+    ms = members_tw(gpu_lib, stream=stream.cuda_stream)
+    e = gpu_lib.Ensemble(ms)
+    choice = e.autotune()
+    print("ensemble autotune:", choice)
+    e.run(2)
+    e.sync()
+    for m in ms:
+        assert np.isfinite(m.get("t")).all()
+    e.close()
+    for m in ms:
+        m.close()
