@@ -306,6 +306,7 @@ def e2e_steps(torch, dm, d, stream, steps, warmup=3, reps=5):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     runs = []
+    split = []  # (device ms, host wall ms) of each loop
     out = None
     for rep in range(reps):  # the host side of the copies varies with the machine's other work
         d.sync()
@@ -323,6 +324,7 @@ def e2e_steps(torch, dm, d, stream, steps, warmup=3, reps=5):
         e1.synchronize()
         wall = time.perf_counter() - t0
         runs.append(max(e0.elapsed_time(e1), 1e3 * wall))
+        split.append((round(e0.elapsed_time(e1), 2), round(1e3 * wall, 2)))
     # the raw DMA rate from one registered host array in the same process,
     # for reading a slow run
     src = torch.from_numpy(host["t"].reshape(-1))
@@ -339,7 +341,7 @@ def e2e_steps(torch, dm, d, stream, steps, warmup=3, reps=5):
         d.host_unregister(a)
     h2d = sum(host[n].nbytes for n in names_in)
     d2h = out[0].nbytes + out[1].nbytes
-    return runs, h2d, d2h, dma
+    return runs, h2d, d2h, dma, split
 
 
 def ensemble_members(dm, stream, n=64, seed=2024):
@@ -688,12 +690,13 @@ def run_single(args, dist, rank, ws, torch, dm, stream, local, device):
     e2e = None
     if not args.no_e2e:
         n_e2e = max(2, args.steps)
-        runs, h2d, d2h, dma = e2e_steps(torch, dm, dsur, stream, n_e2e, args.warmup)
+        runs, h2d, d2h, dma, split = e2e_steps(torch, dm, dsur, stream, n_e2e, args.warmup)
         ms_e2e = reduce_max(dist, sorted(runs)[len(runs) // 2], device)
         e2e = {"value": n_dom * gp * n_e2e / (ms_e2e / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "steps": n_e2e,
                "repeats": "median of %d timed loops of %d steps" % (len(runs), n_e2e),
                "ms_per_step_runs": [round(r / n_e2e, 3) for r in runs],  # in the order they ran
+               "loop_device_and_wall_ms": split,
                "h2d_dma_GBps": round(dma, 1),
                "path": "moloch_gpu_upload(u,v,w,pai,t,qx) from registered (pinned) FP64 host arrays + "
                        "moloch_gpu_step + moloch_gpu_output_start/finish(t,ps) into registered arrays, "
