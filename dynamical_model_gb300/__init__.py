@@ -80,6 +80,7 @@ _PROTOS = {
     "moloch_gpu_sync": (ctypes.c_int, [ctypes.c_void_p]),
     "moloch_gpu_set_wait_limit": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_longlong, ctypes.c_int]),
     "moloch_gpu_check_division": (ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_void_p]),
+    "moloch_gpu_check_division_f64": (ctypes.c_int, [ctypes.c_void_p] * 4 + [ctypes.c_int, ctypes.c_void_p]),
     "moloch_gpu_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "moloch_gpu_kernel_count": (ctypes.c_longlong, [ctypes.c_void_p]),
     "moloch_gpu_phase": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),

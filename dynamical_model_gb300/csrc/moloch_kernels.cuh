@@ -96,7 +96,6 @@ template <class T> __device__ __forceinline__ T superbee(T r) {
 // the reference.  FP32 storage: the fast approximate quotient (2 ulp); the
 // ratio only selects and scales the limiter, and the FP32 error is measured
 // against the FP64 step anyway.
-__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ float qdiv(float a, float b) { return __fdividef(a, b); }
 
 // sign(max(abs(z), minden), z)   (:992)
@@ -326,6 +325,33 @@ __device__ __forceinline__ float div_corr(float a, float b) {
   return fmaf(fmaf(-b, q, a), r, q);
 }
 __device__ __forceinline__ double div_corr(double a, double b) { return a / b; }
+
+// FP64 quotient of the WAF limiter's slope ratio.  The exact build divides
+// as the reference does (IEEE).  The contracting build (MOLOCH_NR_DDIV)
+// refines an FP32 estimate of 1/b by two Newton-Raphson steps,
+// x <- x + x (1 - b x), each of which doubles the correct bits (about 2^-22,
+// 2^-44, then the FP64 precision), forms q = a x and applies one residual
+// correction q + (a - b q) x (Markstein's quotient correction, as div_corr
+// above): within one ulp of the IEEE quotient, with seven FP64 operations
+// and no slow path, for |b| in the FP32 normal range, where the limiter's
+// denominators lie (|b| >= kMinden = 1e-30); other b divide as IEEE.  The
+// conversions run on the integer pipe (widen_f32, narrow_trunc).
+__device__ __forceinline__ double div_nr(double a, double b) {
+  const double ab = fabs(b);
+  if (!(ab >= 1.2e-38 && ab <= 3.0e38)) return a / b;
+  float rf;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rf) : "f"(narrow_trunc(b)));
+  double x = widen_f32(rf);
+  x = fma(x, fma(-b, x, 1.0), x);
+  x = fma(x, fma(-b, x, 1.0), x);
+  const double q = a * x;
+  return fma(fma(-b, q, a), x, q);
+}
+#if defined(MOLOCH_NR_DDIV)
+__device__ __forceinline__ double qdiv(double a, double b) { return div_nr(a, b); }
+#else
+__device__ __forceinline__ double qdiv(double a, double b) { return a / b; }
+#endif
 
 // zrom1w of the implicit w with the latent-heat term of saturated rising
 // air (:641-652).  FP32 storage: the term is evaluated on every level (fast

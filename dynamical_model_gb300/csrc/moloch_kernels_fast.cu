@@ -1,5 +1,6 @@
 // FP64 and FP32-storage kernels with multiply-add contraction allowed.
 #define MOLOCH_KNS kfast
+#define MOLOCH_NR_DDIV 1  // FP64 WAF limiter quotient by Newton-Raphson (div_nr)
 #include "../../include/moloch_gb300.h"
 #include "moloch_kernels.cuh"
 
@@ -118,6 +119,13 @@ __global__ void k_check_division(const float* __restrict__ a, const float* __res
     qi[q] = a[q] / b[q];
   }
 }
+__global__ void k_check_division_f64(const double* __restrict__ a, const double* __restrict__ b,
+                                     double* __restrict__ qn, double* __restrict__ qi, int n) {
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    qn[q] = qdiv(a[q], b[q]);  // div_nr in this build
+    qi[q] = a[q] / b[q];
+  }
+}
 }  // namespace kfast
 }  // namespace moloch
 
@@ -129,5 +137,13 @@ extern "C" int moloch_gpu_check_division(const float* a, const float* b, float* 
   if (n == 0) return MOLOCH_OK;
   const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
   moloch::kfast::k_check_division<<<blocks, 256, 0, (cudaStream_t)stream>>>(a, b, q_corr, q_ieee, n);
+  return cudaPeekAtLastError() == cudaSuccess ? MOLOCH_OK : MOLOCH_ERR_CUDA;
+}
+extern "C" int moloch_gpu_check_division_f64(const double* a, const double* b, double* q_nr, double* q_ieee, int n,
+                                             void* stream) {
+  if (!a || !b || !q_nr || !q_ieee || n < 0) return MOLOCH_ERR_ARG;
+  if (n == 0) return MOLOCH_OK;
+  const int blocks = (n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024;
+  moloch::kfast::k_check_division_f64<<<blocks, 256, 0, (cudaStream_t)stream>>>(a, b, q_nr, q_ieee, n);
   return cudaPeekAtLastError() == cudaSuccess ? MOLOCH_OK : MOLOCH_ERR_CUDA;
 }

@@ -25,6 +25,7 @@
 // its next barrier, and a launch that starts with *err set returns at once,
 // so a failed step never waits longer than one limit per block.
 #define MOLOCH_KNS kpersist
+#define MOLOCH_NR_DDIV 1  // FP64 WAF limiter quotient by Newton-Raphson (div_nr)
 #include "../../include/moloch_gb300.h"
 #include "moloch_kernels.cuh"
 #include "moloch_persist.h"

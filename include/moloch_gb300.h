@@ -212,6 +212,13 @@ int moloch_gpu_set_wait_limit(moloch_handle_t* h, long long cycles, int skip_job
  * counterpart. */
 int moloch_gpu_check_division(const float* a, const float* b, float* q_corr, float* q_ieee, int n, void* stream);
 
+/* The same for FP64 (tests): q_nr = the quotient the contracting build's
+ * WAF limiter uses (FP32 reciprocal estimate, two Newton-Raphson steps, one
+ * residual correction) and q_ieee = CUDA's IEEE FP64 quotient.  No
+ * reference counterpart. */
+int moloch_gpu_check_division_f64(const double* a, const double* b, double* q_nr, double* q_ieee, int n,
+                                  void* stream);
+
 /* The stream the handle launches on (a cudaStream_t). */
 void* moloch_gpu_stream(moloch_handle_t* h);
 

@@ -146,3 +146,32 @@ def test_corrected_quotient_within_one_ulp(gpu_lib):
         ulps = np.abs(c.astype(np.int64) - i.astype(np.int64))
         print(f"b in [{lo}, {hi}]: {float(np.mean(ulps == 0)):.6f} identical, max {ulps.max()} ulp")
         assert ulps.max() <= 1
+
+
+def test_fp64_limiter_quotient_within_one_ulp(gpu_lib):
+    """The contracting build's FP64 WAF limiter divides by an FP32
+    reciprocal estimate refined by two Newton-Raphson steps with one
+    residual correction.  Against CUDA's IEEE FP64 quotient on 2^20 seeded
+    values: at most 1 ulp apart, for the denominators the limiter sees
+    (|b| from its floor 1e-30 up, both signs, field differences of many
+    magnitudes) and for denominators outside the FP32 range (the IEEE path)."""
+    torch = pytest.importorskip("torch")
+    import ctypes
+    L = gpu_lib.lib()
+    rng = np.random.default_rng(23)
+    n = 1 << 20
+    dev = torch.device("cuda", 0)
+    sign = lambda: np.where(rng.random(n) < 0.5, -1.0, 1.0)  # noqa: E731
+    cases = ((-30, 3), (-8, 8), (-300, -40))
+    for lo, hi in cases:
+        a = sign() * rng.uniform(0.5, 1.0, n) * 10.0 ** rng.uniform(-12, 6, n)
+        b = sign() * rng.uniform(0.5, 1.0, n) * 10.0 ** rng.uniform(lo, hi, n)
+        ta, tb = torch.from_numpy(a).to(dev), torch.from_numpy(b).to(dev)
+        qn, qi = torch.empty_like(ta), torch.empty_like(ta)
+        P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+        assert L.moloch_gpu_check_division_f64(P(ta), P(tb), P(qn), P(qi), n, None) == 0
+        torch.cuda.synchronize()
+        c, i = qn.cpu().numpy().view(np.int64), qi.cpu().numpy().view(np.int64)
+        ulps = np.abs(c - i)
+        print(f"|b| in 1e{lo}..1e{hi}: {float(np.mean(ulps == 0)):.6f} identical, max {ulps.max()} ulp")
+        assert ulps.max() <= 1
