@@ -85,8 +85,8 @@ def column_variant(name, tuning):
     return "k_sound_column_tw12" if tuning[1] & 128 else "k_sound_column_tw16" if tuning[1] & 256 else name
 # the FP64 step's dominant kernels are bound by GB300's FP64 rate, not HBM:
 # their FP64-pipe activity from one-launch ncu captures at 256x256x60
-NCU_FP64_STEP = {"k_waf_vertical": {"pipe_fp64_active_pct": 87.2, "dram_pct": 1.8},
-                 "k_waf_horizontal": {"pipe_fp64_active_pct": 83.7, "dram_pct": 2.2}}
+NCU_FP64_STEP = {"k_waf_vertical": {"pipe_fp64_active_pct": 84.3, "dram_pct": 2.0},
+                 "k_waf_horizontal": {"pipe_fp64_active_pct": 81.4, "dram_pct": 2.4}}
 # whole-step algorithmic words per grid point of the fused design target
 # (pre-diag 11 + 3 sound cycles x 91 + 3 advection steps x 23 + post-diag 11)
 B_ALG_WORDS = 364
