@@ -312,9 +312,13 @@ long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);
 /* persistent mode: 0 off; 2, 3 or 4 on, with the kernel built for that many
  * resident blocks of 256 threads per SM (register budgets 128, 80, 64);
  * 1 on with the last build chosen (3 at first).  It carries the horizontal WAF as tiles
- * (choice[0] 1..8), 1 or 2 vertical-WAF fields per thread, and in FP32 no
- * k-marching momentum (choice[1] bit 4 without 8), in FP64 no fused
- * divergence/damping strips (bit 16); other tunings give MOLOCH_ERR_ARG.
+ * (choice[0] 1..8), 1 or 2 vertical-WAF fields per thread, the one-thread
+ * column solve (no bit 32), and in FP32 no k-marching momentum (choice[1]
+ * bit 4 without 8), in FP64 no fused divergence/damping strips (bit 16);
+ * other tunings give MOLOCH_ERR_ARG.  In the one-launch-per-kernel mode an
+ * ensemble takes choice[1] bits 1 to 32 (bit 32: the staged column solve
+ * for its FP32 members with tensor maps) and choice[3], the rows per
+ * momentum strip.
  * moloch_gpu_ensemble_autotune times one launch per kernel and the three
  * builds on whole steps and keeps the fastest; moloch_gpu_ensemble_persistent
  * returns the blocks per SM of the build in use, 0 when the mode is off. */
