@@ -1338,27 +1338,17 @@ int moloch_gpu_tuning_count(void) { return kTuneCount; }
 int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
   g_err.clear();
   if (!h || (n > 0 && !choice)) return fail(MOLOCH_ERR_ARG, "null argument");
-  if (n > 0) {
-    if (choice[0] < 1 || choice[0] > 64) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
-    h->vd.hz_levels = choice[0];
-    h->vf.hz_levels = choice[0];
-  }
-  if (n > 1) {
-    if (choice[1] < 0 || choice[1] > 1023 || (choice[1] & 384) == 384)
-      return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
-    h->vd.kmarch = choice[1];
-    h->vf.kmarch = choice[1];
-  }
-  if (n > 2) {
-    if (!valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
-    h->vd.vfields = choice[2];
-    h->vf.vfields = choice[2];
-  }
-  if (n > 3) {
-    if (choice[3] < 4 || choice[3] > 64) return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
-    h->vd.srows = choice[3];
-    h->vf.srows = choice[3];
-  }
+  // every slot is checked before any is applied
+  if (n > 0 && (choice[0] < 1 || choice[0] > 64)) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
+  if (n > 1 && (choice[1] < 0 || choice[1] > 1023 || (choice[1] & 384) == 384))
+    return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+  if (n > 2 && !valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
+  if (n > 3 && (choice[3] < 4 || choice[3] > 64))
+    return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
+  if (n > 0) { h->vd.hz_levels = choice[0]; h->vf.hz_levels = choice[0]; }
+  if (n > 1) { h->vd.kmarch = choice[1]; h->vf.kmarch = choice[1]; }
+  if (n > 2) { h->vd.vfields = choice[2]; h->vf.vfields = choice[2]; }
+  if (n > 3) { h->vd.srows = choice[3]; h->vf.srows = choice[3]; }
   for (int q = 0; q < 2; ++q) {  // launch shapes are baked into captured graphs
     if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
     if (h->graph[q]) { cudaGraphDestroy(h->graph[q]); h->graph[q] = nullptr; }
@@ -1973,22 +1963,17 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
 int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int nchoice) {
   g_err.clear();
   if (!e || (nchoice > 0 && !choice)) return fail(MOLOCH_ERR_ARG, "null argument");
-  if (nchoice > 0) {
-    if (choice[0] < 1 || choice[0] > 64) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
-    e->hz_levels = choice[0];
-  }
-  if (nchoice > 1) {
-    if (choice[1] < 0 || choice[1] > 63) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
-    e->kmarch = choice[1];
-  }
-  if (nchoice > 2) {
-    if (!valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
-    e->vfields = choice[2];
-  }
-  if (nchoice > 3) {
-    if (choice[3] < 4 || choice[3] > 64) return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
-    e->mrows = choice[3];
-  }
+  // every slot is checked before any is applied
+  if (nchoice > 0 && (choice[0] < 1 || choice[0] > 64)) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
+  if (nchoice > 1 && (choice[1] < 0 || choice[1] > 63)) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+  if (nchoice > 2 && !valid_vfields(choice[2]))
+    return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
+  if (nchoice > 3 && (choice[3] < 4 || choice[3] > 64))
+    return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
+  if (nchoice > 0) e->hz_levels = choice[0];
+  if (nchoice > 1) e->kmarch = choice[1];
+  if (nchoice > 2) e->vfields = choice[2];
+  if (nchoice > 3) e->mrows = choice[3];
   return ens_build(e);
 }
 

@@ -385,3 +385,37 @@ def test_kmarching_sound_kernels_match(gpu_lib, mode, tol, kz, variant):
     for n in PROG + ("s", "deltaw"):
         e = rel_l2(b.get(n), a.get(n))
         assert e <= tol, (n, e)
+
+
+def test_tuning_arguments_are_checked(gpu_lib):
+    """set_tuning refuses what no kernel runs, with MOLOCH_ERR_ARG (1) and
+    the handle's tuning unchanged (every slot is checked before any is
+    applied): both two-word staged variants at once, rows per momentum
+    strip outside 4..64, fields per thread other than 1, 2, 5, 10, bits
+    beyond the variants; the tuning count has four slots; a valid
+    four-slot tuning runs."""
+    g = gpu_lib.Moloch(32, 24, 10, mode="fp32_mixed")
+    g.setup_idealized(device=True)
+    assert g.L.moloch_gpu_tuning_count() == 4
+    g.set_tuning([16, 24, 1, 32])
+    a = g.get("t")
+    for bad in ([32, 32 | 128 | 256], [32, 56, 1, 3], [32, 56, 1, 65], [32, 56, 3], [32, 1024], [0]):
+        with pytest.raises(gpu_lib.MolochError) as ei:
+            g.set_tuning(bad)
+        assert ei.value.code == 1, bad
+    # the refused calls left [16, 24, 1, 32]: a step matches a second
+    # handle set to it
+    h = gpu_lib.Moloch(32, 24, 10, mode="fp32_mixed")
+    h.setup_idealized(device=True)
+    h.set_tuning([16, 24, 1, 32])
+    g.moloch(1)
+    h.moloch(1)
+    for n in ("u", "v", "w", "t"):
+        assert np.array_equal(g.get(n), h.get(n)), n
+    h.close()
+    assert np.isfinite(a).all()
+    g.set_tuning([16, 760, 1, 8])
+    g.moloch(1)
+    g.sync()
+    assert np.isfinite(g.get("t")).all()
+    g.close()
