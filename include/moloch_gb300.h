@@ -275,8 +275,10 @@ const char* moloch_gpu_kernel_name(int kind);
  * moloch_gpu_autotune runs advection() and sound() once per candidate and
  * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the
- * caller and applied to new handles with moloch_gpu_set_tuning.  No
- * reference counterpart (the reference has no GPU launch shapes). */
+ * caller and applied to new handles with moloch_gpu_set_tuning, which
+ * refuses an out-of-range slot with MOLOCH_ERR_ARG and then leaves every
+ * slot as it was.  No reference counterpart (the reference has no GPU
+ * launch shapes). */
 int moloch_gpu_tuning_count(void);
 int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int nchoice);
 int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int nchoice);
