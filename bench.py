@@ -465,7 +465,7 @@ def persistent_tuning(choice):
     vf = vf if vf in (1, 2) else 1
     if km & 4 and not km & 8:
         km &= ~4
-    km &= ~32  # the staged column solve runs only as its own launch
+    km &= ~(32 | 512)  # the staged column solve and the two-level strips run only as their own launches
     return [hz, km, vf]
 
 

@@ -1566,6 +1566,8 @@ void ens_tiles(moloch_ensemble* e) {
       const int ndstrips = ((nj + kDDJ - 1) / kDDJ) * ((ni + kDDR - 1) / kDDR);
       for (int z = 0; z < kz; ++z)
         for (int x = 0; x < (ndstrips + 3) / 4; ++x) e->tiles[TK_DSTRIP].push_back(make_int4(q, x, z, 0));
+      for (int z = 0; z < (kz + kDDLevels - 1) / kDDLevels; ++z)
+        for (int x = 0; x < (ndstrips + 3) / 4; ++x) e->tiles[TK_DSTRIP2].push_back(make_int4(q, x, z, 0));
       for (int z = 0; z < kz; ++z)
         for (int x = 0; x < (nstrips + 7) / 8; ++x) e->tiles[TK_MSTRIP8].push_back(make_int4(q, x, z, 0));
       for (int z = 0; z < kz; ++z)
@@ -1827,10 +1829,12 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   int pick1 = e->kmarch;
   bool staged_ok = false;
   for (auto* h : e->m) staged_ok = staged_ok || (e->elem == 4 && h->vf.cmaps != nullptr);
-  for (int cand = 0; cand < 64; ++cand) {
+  for (int c2 = 0; c2 < 128; ++c2) {
+    const int cand = (c2 & 63) | ((c2 & 64) ? 512 : 0);
     if ((cand & 12) == 12) continue;  // strips replace the k-marching momentum
     if ((cand & 16) && (cand & 3)) continue;  // the fused kernel replaces both
     if ((cand & 32) && !staged_ok) continue;  // batched staged column solve: FP32 members with tensor maps
+    if ((cand & 512) && !(cand & 16)) continue;  // two levels per warp of the fused strips
     e->kmarch = cand;
     int rc = ens_build(e);
     if (rc) { cudaEventDestroy(e0); cudaEventDestroy(e1); return rc; }
@@ -1965,7 +1969,8 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
   if (!e || (nchoice > 0 && !choice)) return fail(MOLOCH_ERR_ARG, "null argument");
   // every slot is checked before any is applied
   if (nchoice > 0 && (choice[0] < 1 || choice[0] > 64)) return fail(MOLOCH_ERR_ARG, "hz_levels %d", choice[0]);
-  if (nchoice > 1 && (choice[1] < 0 || choice[1] > 63)) return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
+  if (nchoice > 1 && (choice[1] < 0 || (choice[1] & ~(63 | 512))))
+    return fail(MOLOCH_ERR_ARG, "kmarch %d", choice[1]);
   if (nchoice > 2 && !valid_vfields(choice[2]))
     return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
   if (nchoice > 3 && (choice[3] < 4 || choice[3] > 64))

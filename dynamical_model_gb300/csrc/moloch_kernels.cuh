@@ -1688,10 +1688,18 @@ __device__ __forceinline__ void b_divdamp_strip_nl(const View<T>& d, const int b
 // 4 blocks per SM (FP32: 122 registers): 0.167 ms per launch at
 // 512 x 512 x 60 against 0.171 for the one-level strips; 5 blocks (96
 // registers, spills) 0.180
-constexpr int kDDLevels = 2;  // levels per warp of k_divdamp_strip_nl
 template <class T>
 __global__ void __launch_bounds__(128, 4) k_divdamp_strip_nl(View<T> d, int R) {
   b_divdamp_strip_nl<T, kDDLevels>(d, blockIdx.x, blockIdx.y, R, threadIdx.x >> 5, 4);
+}
+template <class T>
+__global__ void __launch_bounds__(128, 4)
+    kb_divdamp_strip_nl(const View<T>* __restrict__ views, const int4* __restrict__ tiles, int R) {
+  __shared__ View<T> sv;
+  const int4 t = tiles[blockIdx.x];
+  copy_view(&sv, views + t.x);
+  __syncthreads();
+  b_divdamp_strip_nl<T, kDDLevels>(sv, t.y, t.z, R, threadIdx.x >> 5, 4);
 }
 
 // ---- advection: vertical WAF, two passes at dt/2 (:966-1073) ------------
@@ -2655,7 +2663,12 @@ int blaunch_step(const Batch<T>& b, cudaStream_t st, const PhaseFlags& fl, int& 
     for (int ns = 1; ns <= fl.nsound; ++ns) {
       const int last = ns == fl.nsound;
       if (b.kmarch & 16) {
-        MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st, kb_divdamp_strip<T><<<b.ntiles[TK_DSTRIP], 128, 0, st>>>(V(), b.tiles[TK_DSTRIP], kDDR));
+        if (b.kmarch & 512)  // two levels per warp
+          MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st,
+                        kb_divdamp_strip_nl<T><<<b.ntiles[TK_DSTRIP2], 128, 0, st>>>(V(), b.tiles[TK_DSTRIP2], kDDR));
+        else
+          MOLOCH_LAUNCH(KK_SOUND_DIVDAMP, st,
+                        kb_divdamp_strip<T><<<b.ntiles[TK_DSTRIP], 128, 0, st>>>(V(), b.tiles[TK_DSTRIP], kDDR));
         cur ^= 1;  // the damped u, v are in the other buffer
         --n;
       } else {

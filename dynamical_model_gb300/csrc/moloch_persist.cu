@@ -156,7 +156,7 @@ __global__ void __launch_bounds__(256, MINB) k_ensemble_persistent(const __grid_
 template <class T>
 bool supports(int hz_levels, int kmarch, int vfields) {
   if (hz_levels >= 16 || (vfields != 1 && vfields != 2)) return false;
-  if (kmarch & 32) return false;  // the staged column solve runs only as its own launch
+  if (kmarch & (32 | 512)) return false;  // the staged column solve and the two-level strips run as own launches
   if ((kmarch & 16) && !has_fused_divdamp<T>()) return false;
   if ((kmarch & 4) && !(kmarch & 8) && !has_momentum_km<T>()) return false;
   return true;

@@ -187,13 +187,16 @@ struct KernelTimer {
 // column solve, (member, tile x, tile y, .), of the FP32 members with tensor
 // maps (jx a multiple of 4, kz <= 64); TK_COLREST the TK_COLUMN tiles of the
 // other members, which the one-thread column kernel takes beside it.
+// TK_DSTRIP2 tiles are blocks of 4 divergence/damping warp strips over a
+// pair of levels, (member, block, level pair, .).
 constexpr int kKC = 4;
 constexpr int kTwRows = 12;
 constexpr int kMomJ = 30, kMomR = 32;
 constexpr int kDDJ = 29, kDDR = 32;
+constexpr int kDDLevels = 2;  // levels per warp of the two-level fused divergence/damping strips
 enum TileKind {
   TK_POINT = 0, TK_COLUMN, TK_VERTICAL, TK_HORIZONTAL, TK_CHUNK, TK_MSTRIP, TK_DSTRIP,
-  TK_COLUMN8, TK_VERTICAL8, TK_MSTRIP8, TK_DSTRIP8, TK_COLTW, TK_COLREST, TK_COUNT
+  TK_COLUMN8, TK_VERTICAL8, TK_MSTRIP8, TK_DSTRIP8, TK_COLTW, TK_COLREST, TK_DSTRIP2, TK_COUNT
 };
 template <class T>
 struct Batch {

@@ -318,9 +318,10 @@ long long moloch_gpu_ensemble_kernel_count(moloch_ensemble_t* e);
  * column solve (no bit 32), and in FP32 no k-marching momentum (choice[1]
  * bit 4 without 8), in FP64 no fused divergence/damping strips (bit 16);
  * other tunings give MOLOCH_ERR_ARG.  In the one-launch-per-kernel mode an
- * ensemble takes choice[1] bits 1 to 32 (bit 32: the staged column solve
- * for its FP32 members with tensor maps) and choice[3], the rows per
- * momentum strip.
+ * ensemble takes choice[1] bits 1 to 32 and 512 (bit 32: the staged column
+ * solve for its FP32 members with tensor maps; bit 512 with 16: the fused
+ * strips over two levels per warp) and choice[3], the rows per momentum
+ * strip.
  * moloch_gpu_ensemble_autotune times one launch per kernel and the three
  * builds on whole steps and keeps the fastest; moloch_gpu_ensemble_persistent
  * returns the blocks per SM of the build in use, 0 when the mode is off. */

@@ -70,13 +70,14 @@ def test_ensemble_autotune(gpu_lib, stream):
         m.close()
 
 
-@pytest.mark.parametrize("tuning", [[32, 11], [32, 7], [32, 24, 5], [32, 24, 1, 8]])
+@pytest.mark.parametrize("tuning", [[32, 11], [32, 7], [32, 24, 5], [32, 24, 1, 8], [32, 536, 1]])
 def test_ensemble_strip_shape_matches_members(gpu_lib, stream, tuning):
     """Ensemble with the warp-strip horizontal WAF, the k-marching,
     warp-strip or fused divergence/damping sound kernels, five fields per
-    thread in the vertical WAF (third case) and momentum strips of 8 rows
-    (last case) against the same members run alone with the tile kernel and
-    the one-level-per-thread kernels.
+    thread in the vertical WAF (third case), momentum strips of 8 rows
+    (fourth) and the fused strips over two levels per warp (last) against
+    the same members run alone with the tile kernel and the
+    one-level-per-thread kernels.
     Different kernels contract different multiply-adds in the FP64 build,
     so the bound is 1e-12 rather than the 1e-13 of identical kernels."""
     ms = members(gpu_lib, "fp64", stream=stream.cuda_stream)
