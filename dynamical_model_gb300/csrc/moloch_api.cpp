@@ -296,6 +296,7 @@ size_t layout(View<T>& v, char* base, const moloch_handle* h) {
   v.kmarch = 0;
   v.vfields = 1;
   v.srows = kMomR;
+  v.stag4 = 0;
   v.sur_skip = nullptr;
   v.cmaps = nullptr;
   v.spin_cycles = kDefaultSpinCycles;
@@ -1327,8 +1328,9 @@ static const int kTuneCandidates[][7] = {{1, 2, 4, 8, 16, 32, 64}};
 // 1 divergence, 2 damping, 4 momentum k-marching; 8 momentum warp strips;
 // 16 divergence and damping fused in warp strips, which overrides 1 and 2),
 // [2] advected fields per thread of the vertical WAF (1, 2, 5, 10),
-// [3] rows per warp strip of the momentum strips
-static const int kTuneCount = 4;
+// [3] rows per warp strip of the momentum strips, [4] the staggering back
+// from the cross points four columns per thread (1) or one (0)
+static const int kTuneCount = 5;
 static const int kStripRowCandidates[4] = {4, 8, 16, 32};
 static const int kVFieldCandidates[4] = {1, 2, 5, 10};
 static bool valid_vfields(int f) { return f == 1 || f == 2 || f == 5 || f == 10; }
@@ -1345,10 +1347,12 @@ int moloch_gpu_set_tuning(moloch_handle_t* h, const int* choice, int n) {
   if (n > 2 && !valid_vfields(choice[2])) return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
   if (n > 3 && (choice[3] < 4 || choice[3] > 64))
     return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
+  if (n > 4 && (choice[4] < 0 || choice[4] > 1)) return fail(MOLOCH_ERR_ARG, "staggering variant %d", choice[4]);
   if (n > 0) { h->vd.hz_levels = choice[0]; h->vf.hz_levels = choice[0]; }
   if (n > 1) { h->vd.kmarch = choice[1]; h->vf.kmarch = choice[1]; }
   if (n > 2) { h->vd.vfields = choice[2]; h->vf.vfields = choice[2]; }
   if (n > 3) { h->vd.srows = choice[3]; h->vf.srows = choice[3]; }
+  if (n > 4) { h->vd.stag4 = choice[4]; h->vf.stag4 = choice[4]; }
   for (int q = 0; q < 2; ++q) {  // launch shapes are baked into captured graphs
     if (h->gexec[q]) { cudaGraphExecDestroy(h->gexec[q]); h->gexec[q] = nullptr; }
     if (h->graph[q]) { cudaGraphDestroy(h->graph[q]); h->graph[q] = nullptr; }
@@ -1465,14 +1469,41 @@ int moloch_gpu_autotune(moloch_handle_t* h, int* choice, double* best_ms, int n)
     }
     if (tot < best3) { best3 = tot; pick3 = cand; }
   }
+  h->vd.srows = pick3;
+  h->vf.srows = pick3;
+  // staggering back from the cross points (FP32, jx a multiple of 4), timed
+  // on advection()
+  double best4 = 0.0;
+  int pick4 = 0;
+  if (h->elem == 4 && h->nj() % 4 == 0) {
+    best4 = 1e30;
+    for (int cand = 0; cand < 2; ++cand) {
+      h->vf.stag4 = cand;
+      float ms = 0.f, tot = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {
+        cudaEventRecord(e0, h->stream);
+        h->kernels += launch_phase(h, h->vf, 2);
+        cudaEventRecord(e1, h->stream);
+        if (cudaEventSynchronize(e1) != cudaSuccess) {
+          cudaEventDestroy(e0); cudaEventDestroy(e1);
+          return fail(MOLOCH_ERR_CUDA, "autotune: %s", cudaGetErrorString(cudaGetLastError()));
+        }
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0) tot += ms;
+      }
+      if (tot < best4) { best4 = tot; pick4 = cand; }
+    }
+  }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   choice[0] = pick;
   choice[1] = pick1;
   choice[2] = pick2;
   choice[3] = pick3;
+  choice[4] = pick4;
   if (best_ms) {
     best_ms[0] = best / 2.0; best_ms[1] = best1 / 2.0; best_ms[2] = best2 / 2.0; best_ms[3] = best3 / 2.0;
+    best_ms[4] = best4 / 2.0;
   }
   return moloch_gpu_set_tuning(h, choice, kTuneCount);
 }
@@ -1959,7 +1990,10 @@ int moloch_gpu_ensemble_autotune(moloch_ensemble_t* e, int* choice, double* best
   choice[1] = pick1;
   choice[2] = pick2;
   choice[3] = e->mrows;
-  if (best_ms) { best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; best_ms[3] = best3; }
+  choice[4] = 0;  // the batched staggering kernel takes one column per thread
+  if (best_ms) {
+    best_ms[0] = best / 2.0; best_ms[1] = best1; best_ms[2] = best2 / 2.0; best_ms[3] = best3; best_ms[4] = 0.0;
+  }
   ens_sync_members(e);
   return ens_build(e);
 }
@@ -1975,6 +2009,7 @@ int moloch_gpu_ensemble_set_tuning(moloch_ensemble_t* e, const int* choice, int 
     return fail(MOLOCH_ERR_ARG, "vertical fields per thread %d", choice[2]);
   if (nchoice > 3 && (choice[3] < 4 || choice[3] > 64))
     return fail(MOLOCH_ERR_ARG, "rows per momentum strip %d", choice[3]);
+  if (nchoice > 4 && (choice[4] < 0 || choice[4] > 1)) return fail(MOLOCH_ERR_ARG, "staggering variant %d", choice[4]);
   if (nchoice > 0) e->hz_levels = choice[0];
   if (nchoice > 1) e->kmarch = choice[1];
   if (nchoice > 2) e->vfields = choice[2];

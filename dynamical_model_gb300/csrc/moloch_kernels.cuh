@@ -2292,6 +2292,53 @@ __global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_from_x(View<T> d) {
   b_stag_from_x<T>(d, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
+// The same for FP32 storage with jx a multiple of 4 (View::stag4): each
+// thread takes four consecutive columns j0 .. j0+3 of one row and level,
+// with 16-byte loads and stores -- ux of columns j0-4 .. j0+7 (periodic:
+// the neighbouring quads wrap whole, since jx is a multiple of 4), vx of
+// rows i-2 .. i+1 and wx of levels k-2 .. k+1 -- and the expressions of
+// b_stag_from_x per column: 14 vector memory instructions per four points
+// instead of 60 scalar ones.
+__global__ void __launch_bounds__(kPtBX* kPtBY) k_stag_from_x4(View<float> d) {
+  const int nj = d.nj, ni = d.ni, kz = d.kz, kk = blockIdx.z;
+  const int nq = nj >> 2;
+  const int qj = blockIdx.x * kPtBX + threadIdx.x, ii = blockIdx.y * kPtBY + threadIdx.y;
+  if (qj >= nq || ii >= ni) return;
+  const unsigned pl = (unsigned)d.pl, o = (unsigned)kk * pl;
+  const int j0 = 4 * qj;
+  const unsigned row = (unsigned)nj * (unsigned)ii;
+  const unsigned c = (unsigned)j0 + row;
+  auto ld4 = [](const float* p) { return *reinterpret_cast<const float4*>(p); };
+  auto st4 = [](float* p, float4 v) { *reinterpret_cast<float4*>(p) = v; };
+  auto f = [](float a, float b, float cc, float dd) { return 0.5625f * (a + b) - 0.0625f * (cc + dd); };
+  {  // u(j) <- ux(j-2 .. j+1)
+    const float* ux = d.ux + o + row;
+    const float4 A = ld4(ux + (j0 == 0 ? nj - 4 : j0 - 4)), B = ld4(ux + j0), C = ld4(ux + (j0 + 4 == nj ? 0 : j0 + 4));
+    st4(d.ubuf[0] + o + c, make_float4(f(B.x, A.w, B.y, A.z), f(B.y, B.x, B.z, A.w), f(B.z, B.y, B.w, B.x),
+                                       f(B.w, B.z, C.x, B.y)));
+  }
+  {  // v(i) <- vx(i-2 .. i+1)
+    const float* vx = d.vx + o + j0;
+    const float4 P = ld4(vx + row), M1 = ld4(vx + (unsigned)nj * wm1(ii, ni)), P1 = ld4(vx + (unsigned)nj * wp1(ii, ni)),
+                 M2 = ld4(vx + (unsigned)nj * wm2(ii, ni));
+    st4(d.vbuf[0] + o + c, make_float4(f(P.x, M1.x, P1.x, M2.x), f(P.y, M1.y, P1.y, M2.y), f(P.z, M1.z, P1.z, M2.z),
+                                       f(P.w, M1.w, P1.w, M2.w)));
+  }
+  if (kk >= 1) {  // w(k), k = 2..kz (1-based) <- wx; level index kk = k-1 in 1..kz-1
+    const float* wx = d.wx + c;
+    float4 wv;
+    if (kk == 1 || kk == kz - 1) {
+      const float4 a = ld4(wx + (unsigned)kk * pl), b = ld4(wx + (unsigned)(kk - 1) * pl);
+      wv = make_float4(0.5f * (a.x + b.x), 0.5f * (a.y + b.y), 0.5f * (a.z + b.z), 0.5f * (a.w + b.w));
+    } else {
+      const float4 a = ld4(wx + (unsigned)kk * pl), b = ld4(wx + (unsigned)(kk - 1) * pl);
+      const float4 e = ld4(wx + (unsigned)(kk + 1) * pl), g = ld4(wx + (unsigned)(kk - 2) * pl);
+      wv = make_float4(f(a.x, b.x, e.x, g.x), f(a.y, b.y, e.y, g.y), f(a.z, b.z, e.z, g.z), f(a.w, b.w, e.w, g.w));
+    }
+    st4(d.w + c + (unsigned)kk * pl, wv);
+  }
+}
+
 template <class T>
 __global__ void __launch_bounds__(kPtBX* kPtBY)
     kb_stag_from_x(const View<T>* __restrict__ views, const int4* __restrict__ tiles) {
@@ -2610,7 +2657,15 @@ int launch_advection(View<T>& d, cudaStream_t st) {
   }
   d.fcur ^= 1;
   d.bind_fields();
-  MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pg, pb, 0, st>>>(d));
+  bool vec = false;
+  if constexpr (sizeof(T) == 4) {
+    if (d.stag4 && d.nj % 4 == 0) {  // four columns per thread
+      const dim3 g4((d.nj / 4 + kPtBX - 1) / kPtBX, (d.ni + kPtBY - 1) / kPtBY, d.kz);
+      MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x4<<<g4, pb, 0, st>>>(d));
+      vec = true;
+    }
+  }
+  if (!vec) MOLOCH_LAUNCH(KK_STAG_FROM_X, st, k_stag_from_x<T><<<pg, pb, 0, st>>>(d));
   d.cur = 0;
   return 3;
 }

@@ -118,6 +118,7 @@ struct View {
                    // with 16: the fused strips over two levels per warp
   int vfields;     // advected fields per thread of k_waf_vertical: 1, 2, 5 or 10
   int srows;       // rows per warp strip of the momentum strips
+  int stag4;       // 1: k_stag_from_x4 (FP32, jx a multiple of 4)
 
   // set when a learned surrogate stands in for sound(): the plain sound
   // kernels return at once while *sur_skip == 1 (the surrogate's cycle was

@@ -271,7 +271,11 @@ const char* moloch_gpu_kernel_name(int kind);
  *   choice[3] = rows per warp strip of the momentum strips, 4 to 64
  *               (candidates 4, 8, 16, 32: shorter strips put more warps in
  *               flight; in ensembles the one-launch-per-kernel mode takes
- *               it, the persistent kernel keeps 32).
+ *               it, the persistent kernel keeps 32);
+ *   choice[4] = 1: the staggering back from the cross points with four
+ *               columns per thread and 16-byte loads and stores (FP32
+ *               storage, jx a multiple of 4; elsewhere, and in ensembles,
+ *               ignored), 0: one column per thread.
  * moloch_gpu_autotune runs advection() and sound() once per candidate and
  * repeat, so it advances the model state: call it on a scratch handle or before the
  * initial state is uploaded again.  The chosen values can be cached by the

@@ -392,14 +392,15 @@ def test_tuning_arguments_are_checked(gpu_lib):
     the handle's tuning unchanged (every slot is checked before any is
     applied): both two-word staged variants at once, rows per momentum
     strip outside 4..64, fields per thread other than 1, 2, 5, 10, bits
-    beyond the variants; the tuning count has four slots; a valid
-    four-slot tuning runs."""
+    beyond the variants, a staggering variant other than 0 and 1; the
+    tuning count has five slots; a valid tuning runs."""
     g = gpu_lib.Moloch(32, 24, 10, mode="fp32_mixed")
     g.setup_idealized(device=True)
-    assert g.L.moloch_gpu_tuning_count() == 4
+    assert g.L.moloch_gpu_tuning_count() == 5
     g.set_tuning([16, 24, 1, 32])
     a = g.get("t")
-    for bad in ([32, 32 | 128 | 256], [32, 56, 1, 3], [32, 56, 1, 65], [32, 56, 3], [32, 1024], [0]):
+    for bad in ([32, 32 | 128 | 256], [32, 56, 1, 3], [32, 56, 1, 65], [32, 56, 3], [32, 1024], [0],
+                [32, 56, 1, 8, 2]):
         with pytest.raises(gpu_lib.MolochError) as ei:
             g.set_tuning(bad)
         assert ei.value.code == 1, bad
@@ -419,3 +420,23 @@ def test_tuning_arguments_are_checked(gpu_lib):
     g.sync()
     assert np.isfinite(g.get("t")).all()
     g.close()
+
+
+@pytest.mark.parametrize("jx", [48, 46])
+def test_staggering_four_columns_per_thread_matches(gpu_lib, jx):
+    """The staggering back from the cross points with four columns per
+    thread (tuning slot 4, FP32, jx a multiple of 4; 16-byte loads and
+    stores, the neighbouring quads wrapped whole at the periodic edges)
+    against one column per thread: the same expression per column, so the
+    same bits; jx = 46 falls back to the one-column kernel."""
+    a = gpu_lib.Moloch(jx, 37, 11, mode="fp32_mixed")
+    b = gpu_lib.Moloch(jx, 37, 11, mode="fp32_mixed")
+    for g in (a, b):
+        g.setup_idealized(hills=((400.0, jx / 2.0, 18.0, 4.0),), u0=6.0, v0=-4.0)
+    a.set_tuning([16, 24, 1, 32, 0])
+    b.set_tuning([16, 24, 1, 32, 1])
+    for s in range(1, 4):
+        a.moloch(s)
+        b.moloch(s)
+    for n in PROG:
+        assert np.array_equal(b.get(n), a.get(n)), n
