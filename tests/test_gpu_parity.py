@@ -440,4 +440,3 @@ def test_staggering_four_columns_per_thread_matches(gpu_lib, jx):
         b.moloch(s)
     for n in PROG:
         assert np.array_equal(b.get(n), a.get(n)), n
-
